@@ -1,0 +1,243 @@
+"""mm3e_cuda — GB300 (sm_103a) drop-in for MM3E's per-pixel SDF render path.
+
+Host-side mirror of the reference's render interface over the C ABI (include/mm3e_cuda.h):
+
+    scene = Scene(960, 540)              # mm3e_orchestrator::Scene
+    ...                                  # materials / objects / lights as in the reference
+    fb = render(scene, camera)           # mm3e_orchestrator::render -> RGBA f32 (h, w, 4)
+
+    renderer = CudaRenderer()            # CpuParallelRenderer counterpart (mm3e-cpu-parallel)
+    compiled = renderer.compile(scene)   # CpuParallelRenderer::compile / GpuRenderer::compile
+    fb = compiled.try_render(camera, dyn_spheres)   # CpuParallelScene::try_render
+
+Every call runs on the GPU through libmm3e_cuda.so; there is no CPU fallback. Errors from the
+checked reference calls (`Err(String)`) surface as RenderError with the library's message.
+"""
+import ctypes as C
+import weakref
+
+import numpy as np
+
+from . import abi
+from .native import NativeLibraryMissing, lib
+from .scene import (DynSphere, Expr, GiVolume, Light, Marcher, Material, Object, Post, Prim, Scene, SdfVolume,
+                    Transform, directional, look_at, mat3_from_euler, normalize_f32, orbit_camera, quat_to_mat3,
+                    radians)
+
+RenderMode = abi  # RenderMode.MODE_* constants
+
+
+class RenderError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"{message} (code {code})")
+        self.code = code
+        self.message = message
+
+
+class Context:
+    """One CUDA stream on one device (mm3e_ctx)."""
+
+    def __init__(self, device=0):
+        self._ptr = C.c_void_p()
+        self._scenes = weakref.WeakSet()
+        rc = lib().mm3e_ctx_create(device, C.byref(self._ptr))
+        if rc != abi.OK:
+            raise RenderError(rc, f"mm3e_ctx_create(device={device}) failed")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._ptr
+
+    def check(self, rc):
+        if rc != abi.OK:
+            raise RenderError(rc, lib().mm3e_last_error(self._ptr).decode(errors="replace"))
+
+    def sync(self):
+        self.check(lib().mm3e_ctx_sync(self._ptr))
+
+    def set_stream(self, cuda_stream_handle):
+        """Issue all work on a caller-owned cudaStream_t (an int handle, e.g. torch's
+        `stream.cuda_stream`); None restores the context's own stream."""
+        self.check(lib().mm3e_ctx_set_stream(self._ptr, C.c_void_p(cuda_stream_handle or 0)))
+
+    def device_info(self):
+        sm, clk = C.c_int(), C.c_int()
+        self.check(lib().mm3e_ctx_device_info(self._ptr, C.byref(sm), C.byref(clk)))
+        return {"sm_count": sm.value, "clock_khz": clk.value}
+
+    def close(self):
+        """Destroy the context; scenes compiled on it are destroyed first."""
+        if self._ptr:
+            for sc in list(self._scenes):
+                sc.close()
+            lib().mm3e_ctx_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class CompiledScene:
+    """A scene lowered to a device-resident tape (mm3e_scene)."""
+
+    def __init__(self, ctx, scene):
+        self.ctx = ctx
+        self.width, self.height = scene.width, scene.height
+        self.mode = scene.mode
+        self.n_materials = len(scene.materials)
+        handle = scene.desc()
+        self._ptr = C.c_void_p()
+        ctx.check(lib().mm3e_scene_compile(ctx.handle, handle.ptr, C.byref(self._ptr)))
+        ctx._scenes.add(self)
+
+    def close(self):
+        if self._ptr:
+            if self.ctx.handle:
+                lib().mm3e_scene_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, camera, dyn_spheres=(), fmt=abi.FB_RGBA_F32, stats=False):
+        """Framebuffer of the frame: (h, w, 4) f32 RGBA, or (h, w, 4) u8 for FB_RGBA8."""
+        h, w = self.height, self.width
+        out = np.empty((h, w, 4), dtype=np.float32 if fmt == abi.FB_RGBA_F32 else np.uint8)
+        dyn = (abi.DynSphere * max(1, len(dyn_spheres)))(*[s.to_abi() for s in dyn_spheres])
+        st = abi.RenderStats()
+        rc = lib().mm3e_render(self._ptr, C.byref(camera), dyn, len(dyn_spheres), fmt,
+                               out.ctypes.data_as(C.c_void_p), out.nbytes, C.byref(st))
+        self.ctx.check(rc)
+        if stats:
+            return out, {"device_ms": st.device_ms, "total_ms": st.total_ms, "d2h_bytes": st.d2h_bytes,
+                         "kernel_launches": st.kernel_launches}
+        return out
+
+    # CpuParallelScene::try_render (mm3e-cpu-parallel/src/lib.rs:50-65)
+    def try_render(self, camera, dyn_spheres=()):
+        return self.render(camera, dyn_spheres)
+
+    def render_linear(self, camera):
+        """render_linear: beauty radiance before post, (h, w, 3) f32."""
+        out = np.empty((self.height, self.width, 3), dtype=np.float32)
+        self.ctx.check(lib().mm3e_render_linear(self._ptr, C.byref(camera),
+                                                out.ctypes.data_as(C.POINTER(C.c_float)), out.size))
+        return out
+
+    def render_device(self, camera, fmt, device_ptr, nbytes):
+        self.ctx.check(lib().mm3e_render_device(self._ptr, C.byref(camera), fmt, C.c_void_p(device_ptr), nbytes))
+
+    def render_hits(self, camera):
+        n = self.width * self.height
+        t = np.empty(n, np.float32)
+        m = np.empty(n, np.uint32)
+        s = np.empty(n, np.uint32)
+        nrm = np.empty(3 * n, np.float32)
+        P = C.POINTER
+        self.ctx.check(lib().mm3e_render_hits(self._ptr, C.byref(camera), t.ctypes.data_as(P(C.c_float)),
+                                              m.ctypes.data_as(P(C.c_uint32)), s.ctypes.data_as(P(C.c_uint32)),
+                                              nrm.ctypes.data_as(P(C.c_float))))
+        shape = (self.height, self.width)
+        return {"t": t.reshape(shape), "mat": m.reshape(shape), "steps": s.reshape(shape),
+                "normal": nrm.reshape(shape + (3,))}
+
+    def march_rays(self, rays6):
+        rays6 = np.ascontiguousarray(rays6, dtype=np.float32).reshape(-1, 6)
+        n = len(rays6)
+        t = np.empty(n, np.float32)
+        m = np.empty(n, np.uint32)
+        s = np.empty(n, np.uint32)
+        P = C.POINTER
+        self.ctx.check(lib().mm3e_march_rays(self._ptr, rays6.ctypes.data_as(P(C.c_float)), n,
+                                             t.ctypes.data_as(P(C.c_float)), m.ctypes.data_as(P(C.c_uint32)),
+                                             s.ctypes.data_as(P(C.c_uint32))))
+        return t, m, s
+
+    def field(self, points3):
+        pts = np.ascontiguousarray(points3, dtype=np.float32).reshape(-1, 3)
+        n = len(pts)
+        d = np.empty(n, np.float32)
+        m = np.empty(n, np.uint32)
+        P = C.POINTER
+        self.ctx.check(lib().mm3e_field(self._ptr, pts.ctypes.data_as(P(C.c_float)), n,
+                                        d.ctypes.data_as(P(C.c_float)), m.ctypes.data_as(P(C.c_uint32))))
+        return d, m
+
+    def bake_gi(self, dims, samples):
+        """Scene::bake_gi on the GPU (replaces the compiled scene's GI)."""
+        self.ctx.check(lib().mm3e_bake_gi(self._ptr, dims[0], dims[1], dims[2], samples))
+
+    def get_gi(self):
+        mn = (C.c_float * 3)()
+        sz = (C.c_float * 3)()
+        dims = (C.c_uint32 * 3)()
+        self.ctx.check(lib().mm3e_scene_get_gi(self._ptr, mn, sz, dims, None, 0))
+        n = dims[0] * dims[1] * dims[2] * 18
+        cubes = np.empty(n, np.float32)
+        self.ctx.check(lib().mm3e_scene_get_gi(self._ptr, mn, sz, dims, cubes.ctypes.data_as(C.POINTER(C.c_float)),
+                                               n))
+        return GiVolume(tuple(mn), tuple(sz), tuple(dims), cubes)
+
+
+class CudaRenderer:
+    """CpuParallelRenderer counterpart: compile scenes for one GPU context."""
+
+    def __init__(self, device=0, ctx=None):
+        self.ctx = ctx or (default_context() if device == 0 else Context(device))
+
+    def compile(self, scene):
+        return CompiledScene(self.ctx, scene)
+
+
+def validate(scene):
+    """mm3e_scene_validate: (code, message) without touching a GPU."""
+    buf = C.create_string_buffer(512)
+    h = scene.desc()
+    rc = lib().mm3e_scene_validate(h.ptr, buf, len(buf))
+    return rc, buf.value.decode(errors="replace")
+
+
+def render(scene, camera, ctx=None):
+    """mm3e_orchestrator::render_checked: compile + render one frame, RGBA f32 (h, w, 4)."""
+    return CompiledScene(ctx or default_context(), scene).render(camera)
+
+
+def render_linear(scene, camera, ctx=None):
+    return CompiledScene(ctx or default_context(), scene).render_linear(camera)
+
+
+def to_rgba8(fb):
+    """Framebuffer::to_rgba8 over black (framebuffer.rs:308-319) for an RGBA f32 frame."""
+    fb = np.asarray(fb, dtype=np.float32)
+    a = np.clip(fb[..., 3:4], 0.0, 1.0).astype(np.float32)
+    rgb = (fb[..., :3] * a + np.float32(0.0) * (np.float32(1.0) - a)).astype(np.float32)
+    q = (np.clip(rgb, 0.0, 1.0) * np.float32(255.0) + np.float32(0.5)).astype(np.float32)
+    out = np.empty(fb.shape[:-1] + (4,), np.uint8)
+    out[..., :3] = np.floor(q).astype(np.uint8)
+    out[..., 3] = 255
+    return out
+
+
+__all__ = [
+    "abi", "lib", "NativeLibraryMissing", "RenderError", "Context", "CompiledScene", "CudaRenderer", "render",
+    "render_linear", "validate", "to_rgba8", "Scene", "Object", "Prim", "Material", "Light", "directional", "Marcher",
+    "Post", "Transform", "Expr", "SdfVolume", "GiVolume", "DynSphere", "look_at", "orbit_camera", "mat3_from_euler",
+    "quat_to_mat3", "normalize_f32", "radians",
+]

@@ -1,0 +1,89 @@
+"""Loader for the in-tree C-ABI library libmm3e_cuda.so (built by mm3e_cuda.build).
+
+There is no fallback: if the library is missing, every entry point raises. The library is
+never installed into site-packages, so the process maps it from this package directory.
+"""
+import ctypes as C
+import os
+
+from . import abi
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "_lib", "libmm3e_cuda.so")
+
+_lib = None
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+def _declare(lib):
+    P = C.POINTER
+    f = C.c_float
+    sig = {
+        "mm3e_abi_version": (C.c_int, []),
+        "mm3e_camera_look_at": (None, [P(f), P(f), P(f), f, P(abi.Camera)]),
+        "mm3e_orbit_camera": (None, [P(f), f, f, f, f, P(abi.Camera)]),
+        "mm3e_mat3_from_euler": (None, [f, f, f, P(f)]),
+        "mm3e_quat_to_mat3": (None, [P(f), P(f)]),
+        "mm3e_light_directional": (None, [P(f), P(f), P(abi.Light)]),
+        "mm3e_scene_validate": (C.c_int, [P(abi.SceneDesc), C.c_char_p, C.c_size_t]),
+        "mm3e_scene_tape_bytes": (C.c_int, [P(abi.SceneDesc), P(C.c_size_t)]),
+        "mm3e_ctx_create": (C.c_int, [C.c_int, P(C.c_void_p)]),
+        "mm3e_ctx_destroy": (None, [C.c_void_p]),
+        "mm3e_last_error": (C.c_char_p, [C.c_void_p]),
+        "mm3e_ctx_sync": (C.c_int, [C.c_void_p]),
+        "mm3e_ctx_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "mm3e_ctx_device_info": (C.c_int, [C.c_void_p, P(C.c_int), P(C.c_int)]),
+        "mm3e_scene_compile": (C.c_int, [C.c_void_p, P(abi.SceneDesc), P(C.c_void_p)]),
+        "mm3e_scene_destroy": (None, [C.c_void_p]),
+        "mm3e_render": (C.c_int, [C.c_void_p, P(abi.Camera), P(abi.DynSphere), C.c_size_t, C.c_uint32, C.c_void_p,
+                                  C.c_size_t, P(abi.RenderStats)]),
+        "mm3e_render_linear": (C.c_int, [C.c_void_p, P(abi.Camera), P(f), C.c_size_t]),
+        "mm3e_render_device": (C.c_int, [C.c_void_p, P(abi.Camera), C.c_uint32, C.c_void_p, C.c_size_t]),
+        "mm3e_bake_gi": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]),
+        "mm3e_scene_get_gi": (C.c_int, [C.c_void_p, P(f), P(f), P(C.c_uint32), P(f), C.c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _declare_extra(lib)
+
+
+def _declare_extra(lib):
+    """Entry points beyond the core set (diagnostics, batched and served forms)."""
+    P = C.POINTER
+    extra = {
+        "mm3e_render_hits": (C.c_int, [C.c_void_p, P(abi.Camera), P(C.c_float), P(C.c_uint32), P(C.c_uint32),
+                                       P(C.c_float)]),
+        "mm3e_march_rays": (C.c_int, [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_uint32),
+                                      P(C.c_uint32)]),
+        "mm3e_field": (C.c_int, [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_uint32)]),
+    }
+    for name, (res, args) in extra.items():
+        fn = getattr(lib, name, None)
+        if fn is not None:
+            fn.restype = res
+            fn.argtypes = args
+
+
+def lib():
+    """The loaded library (raises NativeLibraryMissing if it was never built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeLibraryMissing(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        l = C.CDLL(LIB_PATH)
+        _declare(l)
+        if l.mm3e_abi_version() != abi.ABI_VERSION:
+            raise NativeLibraryMissing("libmm3e_cuda.so ABI version mismatch; rebuild")
+        _lib = l
+    return _lib
+
+
+def fptr(seq, n=None):
+    arr = (C.c_float * (n if n is not None else len(seq)))(*seq)
+    return arr

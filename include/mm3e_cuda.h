@@ -1,0 +1,333 @@
+/*
+ * mm3e_cuda.h — C ABI of the GB300 (sm_103a) per-pixel SDF render path.
+ *
+ * This is the drop-in boundary for MM3E's CPU render call. A caller marshals its
+ * `mm3e_orchestrator::Scene` into the flat POD `mm3e_scene_desc` below, compiles it once
+ * into a device-resident scene tape, and renders per camera. The returned framebuffer is
+ * the one the reference returns: straight-alpha RGBA f32 with alpha = 1 (or its RGBA8
+ * quantisation, `Framebuffer::to_rgba8` over black).
+ *
+ * Reference interfaces each entry point replaces (paths inside the MM3E repository):
+ *   mm3e_render            <- mm3e_orchestrator::render_with_threads_checked
+ *                             (mm3e-orchestrator/src/lib.rs:866-871) and
+ *                             mm3e_cpu_parallel::CpuParallelScene::try_render
+ *                             (mm3e-cpu-parallel/src/lib.rs:50-65, dynamic spheres)
+ *   mm3e_render_linear     <- render_linear_with_threads_checked (lib.rs:902-907)
+ *   mm3e_scene_compile     <- CpuParallelRenderer::compile (mm3e-cpu-parallel/src/lib.rs:101)
+ *                             and GpuRenderer::compile_checked (mm3e-gpu/src/lib.rs:138-285)
+ *   mm3e_bake_gi           <- Scene::bake_gi_checked (mm3e-orchestrator/src/appearance.rs:193-200)
+ *   mm3e_camera_look_at    <- Camera::look_at (mm3e-kit/src/camera.rs:50-55)
+ *   mm3e_orbit_camera      <- orbit_camera (mm3e-orchestrator/src/lib.rs:1426-1435)
+ *   mm3e_mat3_from_euler   <- Mat3::from_euler (mm3e-kit/src/vec.rs:144-149)
+ *   mm3e_quat_to_mat3      <- Quat::to_mat3 (mm3e-kit/src/vec.rs:318-326)
+ *   mm3e_light_directional <- Light::directional (mm3e-orchestrator/src/lib.rs:513-515)
+ *   mm3e_scene_validate    <- Scene::validate_appearance + GPU codegen checks
+ *                             (appearance.rs:250-269, mm3e-gpu/src/wgsl.rs:41-47,
+ *                             mm3e-gpu/src/lib.rs:139-141, csg.rs:154-236)
+ *   mm3e_last_error        <- the `Err(String)` of every checked reference call
+ *
+ * Conventions: 0 = success, negative = error (message via mm3e_last_error). Contexts are not
+ * thread-safe: use one context per host thread. All floats are IEEE binary32.
+ */
+#ifndef MM3E_CUDA_H
+#define MM3E_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MM3E_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------------- */
+enum {
+    MM3E_OK = 0,
+    MM3E_ERR_INVALID = -1,     /* bad scene / camera / argument (reference: Err(String)) */
+    MM3E_ERR_UNSUPPORTED = -2, /* valid MM3E input this path does not render (UV maps, surfaces) */
+    MM3E_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+    MM3E_ERR_NO_MEMORY = -4,   /* device or host allocation failed */
+    MM3E_ERR_BUDGET = -5,      /* request refused by the HBM admission budget */
+    MM3E_ERR_TIMEOUT = -6,     /* a bounded device-side wait gave up */
+    MM3E_ERR_CANCELLED = -7,   /* request cancelled before completion */
+    MM3E_ERR_BUSY = -8         /* no free slot right now (retry) */
+};
+
+/* ---- scene model (mirrors mm3e_orchestrator::{Prim, Combine, Modifiers, Object, Light,
+ *      Scene}, mm3e_kit::{Material, Marcher}, post::Post) ---------------------------------- */
+
+/* Prim (mm3e-orchestrator/src/lib.rs:157-212). Parameter packing in mm3e_object.params:
+ *   SPHERE r | BOX hx hy hz | ROUND_BOX hx hy hz radius | TORUS major minor | CYLINDER h r |
+ *   CAPSULE ax ay az bx by bz r | CONE r1 r2 h | ELLIPSOID rx ry rz | OCTAHEDRON s |
+ *   HEX_PRISM r h | PLANE nx ny nz h | CSG (id = expression index) | VOLUME (id = volume index) */
+enum {
+    MM3E_PRIM_SPHERE = 0,
+    MM3E_PRIM_BOX = 1,
+    MM3E_PRIM_ROUND_BOX = 2,
+    MM3E_PRIM_TORUS = 3,
+    MM3E_PRIM_CYLINDER = 4,
+    MM3E_PRIM_CAPSULE = 5,
+    MM3E_PRIM_CONE = 6,
+    MM3E_PRIM_ELLIPSOID = 7,
+    MM3E_PRIM_OCTAHEDRON = 8,
+    MM3E_PRIM_HEX_PRISM = 9,
+    MM3E_PRIM_PLANE = 10,
+    MM3E_PRIM_CSG = 11,
+    MM3E_PRIM_VOLUME = 12,
+    MM3E_PRIM_SURFACE = 13 /* native triangle shell: rejected, as the GPU twin does */
+};
+
+/* Combine (lib.rs:297-304) */
+enum { MM3E_COMBINE_UNION = 0, MM3E_COMBINE_SMOOTH = 1, MM3E_COMBINE_SUBTRACT = 2 };
+
+/* RenderMode (lib.rs:49-61) */
+enum {
+    MM3E_MODE_BEAUTY = 0,
+    MM3E_MODE_NORMAL = 1,
+    MM3E_MODE_DEPTH = 2,
+    MM3E_MODE_AO = 3,
+    MM3E_MODE_STEPS = 4,
+    MM3E_MODE_ALBEDO = 5
+};
+
+/* Output framebuffer formats. */
+enum {
+    MM3E_FB_RGBA_F32 = 0, /* Framebuffer pixels: 4 x f32, straight alpha (= 1) */
+    MM3E_FB_RGBA8 = 1,    /* Framebuffer::to_rgba8 over black: 4 x u8 */
+    MM3E_FB_LINEAR_F32 = 2 /* render_linear radiance before post: 4 x f32 (rgb, 1); device output only */
+};
+
+/* Object (lib.rs:330-336) with Transform (vec.rs:165-169) and Modifiers (lib.rs:311-319). */
+typedef struct mm3e_object {
+    uint32_t prim;      /* MM3E_PRIM_* */
+    uint32_t id;        /* CSG expression / volume index for CSG and VOLUME prims */
+    uint32_t mat;       /* material index (reduced modulo the material count, as the reference) */
+    uint32_t combine;   /* MM3E_COMBINE_* */
+    float smooth_k;     /* Combine::Smooth(k) */
+    float params[7];    /* primitive parameters, packed as documented above */
+    float rot[9];       /* Mat3 columns: cols[0].xyz, cols[1].xyz, cols[2].xyz */
+    float pos[3];
+    float scale;
+    uint32_t mirror;    /* bit 0 = x, bit 1 = y, bit 2 = z */
+    float repeat[3];
+    float twist;
+    float bend;
+    float elongate[3];
+    float round;
+    float onion;
+} mm3e_object;
+
+/* Material (mm3e-kit/src/color.rs:153-162) */
+typedef struct mm3e_material {
+    float albedo[3];
+    float metallic;
+    float specular;
+    float roughness;
+    float reflectivity;
+    float emissive[3];
+    uint32_t checker;
+} mm3e_material;
+
+/* Light (lib.rs:503-510). `vec` is the unit direction toward the light (directional) or the
+ * light position (point / sphere). */
+typedef struct mm3e_light {
+    float vec[3];
+    float color[3];
+    uint32_t directional;
+    float radius;
+} mm3e_light;
+
+/* Marcher (mm3e-kit/src/march.rs:42-79) */
+typedef struct mm3e_marcher {
+    uint32_t max_steps;
+    float max_dist;
+    float eps;
+    float step_scale;
+    uint32_t shadow_steps;
+    uint32_t ao_samples;
+    float lod_footprint;
+    float subitize;
+    uint32_t secant;
+    float normal_h;
+} mm3e_marcher;
+
+/* Post (mm3e-orchestrator/src/post.rs:14-29) */
+typedef struct mm3e_post {
+    float exposure;
+    uint32_t bloom;
+    float bloom_threshold;
+    float bloom_intensity;
+    uint32_t bloom_radius;
+} mm3e_post;
+
+/* csg::Expr node (mm3e-kit/src/csg.rs:17-92), stored in an array; children by index.
+ * kind: the 11 primitive kinds use MM3E_PRIM_* values 0..10 with `params` packed as for
+ * objects; the operators below use `a`/`b` child indices. */
+enum {
+    MM3E_CSG_TRANSFORM = 100, /* child a, rot/pos/scale */
+    MM3E_CSG_UNION = 101,     /* children a, b */
+    MM3E_CSG_INTERSECT = 102,
+    MM3E_CSG_SUBTRACT = 103,
+    MM3E_CSG_SMOOTH_UNION = 104, /* params[0] = k */
+    MM3E_CSG_OFFSET = 105,       /* child a, params[0] = distance */
+    MM3E_CSG_SHELL = 106         /* child a, params[0] = thickness */
+};
+typedef struct mm3e_csg_node {
+    uint32_t kind;
+    uint32_t a;
+    uint32_t b;
+    uint32_t pad;
+    float params[7];
+    float rot[9];
+    float pos[3];
+    float scale;
+} mm3e_csg_node;
+
+/* SdfVolume (mm3e-kit/src/volume.rs:14-23); data row-major (k*ny + j)*nx + i. */
+typedef struct mm3e_volume {
+    uint32_t nx, ny, nz;
+    float min[3];
+    float cell[3];
+    const float* data;
+} mm3e_volume;
+
+/* GiVolume (mm3e-orchestrator/src/gi.rs:17-23); cubes[((k*ny + j)*nx + i)*18 + face*3 + c],
+ * faces +x, -x, +y, -y, +z, -z. */
+typedef struct mm3e_gi {
+    float min[3];
+    float size[3];
+    uint32_t nx, ny, nz;
+    const float* cubes;
+} mm3e_gi;
+
+/* Scene (lib.rs:561-592). UV appearance bindings and native triangle surfaces are not part
+ * of this path (the reference GPU twin rejects them too). */
+typedef struct mm3e_scene_desc {
+    uint32_t width;
+    uint32_t height;
+    const mm3e_object* objects;
+    uint32_t n_objects;
+    const mm3e_material* materials;
+    uint32_t n_materials;
+    const mm3e_light* lights;
+    uint32_t n_lights;
+    float sun_dir[3];
+    float ambient[3];
+    float sky_ambient[3];
+    float fog[3];
+    float fog_density;
+    uint32_t aa;
+    uint32_t bounces;
+    uint32_t shadows;
+    uint32_t ao;
+    mm3e_marcher marcher;
+    mm3e_post post;
+    uint32_t mode;                  /* MM3E_MODE_* */
+    const mm3e_gi* gi;              /* NULL = no baked GI */
+    const mm3e_volume* volumes;
+    uint32_t n_volumes;
+    const mm3e_csg_node* csg_nodes; /* all expressions' nodes */
+    uint32_t n_csg_nodes;
+    const uint32_t* csg_roots;      /* root node index of expression i */
+    uint32_t n_csgs;
+} mm3e_scene_desc;
+
+/* Camera (mm3e-kit/src/camera.rs:39-45) */
+typedef struct mm3e_camera {
+    float eye[3];
+    float forward[3];
+    float right[3];
+    float up[3];
+    float fov_scale; /* tan(fov_y / 2) */
+} mm3e_camera;
+
+/* DynSphere (mm3e-cpu-parallel/src/lib.rs:18-23) */
+typedef struct mm3e_dyn_sphere {
+    float pos[3];
+    float radius;
+    float albedo[3];
+    float metallic;
+} mm3e_dyn_sphere;
+
+/* Per-render statistics (optional out-parameter). */
+typedef struct mm3e_render_stats {
+    double device_ms;      /* render + post kernels, CUDA events on the render stream */
+    double total_ms;       /* host wall time of the call including copies */
+    uint64_t h2d_bytes;
+    uint64_t d2h_bytes;
+    uint32_t kernel_launches;
+} mm3e_render_stats;
+
+typedef struct mm3e_ctx mm3e_ctx;
+typedef struct mm3e_scene mm3e_scene;
+
+/* ---- host-only helpers (no GPU needed) ---------------------------------------------------- */
+int mm3e_abi_version(void);
+void mm3e_camera_look_at(const float eye[3], const float target[3], const float up_hint[3], float fov_y,
+                         mm3e_camera* out);
+void mm3e_orbit_camera(const float target[3], float radius, float yaw, float pitch, float fov_y,
+                       mm3e_camera* out);
+void mm3e_mat3_from_euler(float x, float y, float z, float out_cols[9]);
+void mm3e_quat_to_mat3(const float q_xyzw[4], float out_cols[9]);
+void mm3e_light_directional(const float toward[3], const float color[3], mm3e_light* out);
+/* Validates a scene description exactly as mm3e_scene_compile does, without a device. */
+int mm3e_scene_validate(const mm3e_scene_desc* desc, char* err, size_t err_len);
+/* Size in bytes of the lowered scene tape (host-side lowering, no device). */
+int mm3e_scene_tape_bytes(const mm3e_scene_desc* desc, size_t* out_bytes);
+
+/* ---- context ----------------------------------------------------------------------------- */
+int mm3e_ctx_create(int device, mm3e_ctx** out);
+/* Destroys the context and every scene still compiled on it (their handles become invalid). */
+void mm3e_ctx_destroy(mm3e_ctx* ctx);
+const char* mm3e_last_error(const mm3e_ctx* ctx);
+int mm3e_ctx_sync(mm3e_ctx* ctx);
+/* Run the context's work on a caller-owned cudaStream_t (NULL restores the context's own
+ * stream); like cublasSetStream, for callers that order rendering with their own work. */
+int mm3e_ctx_set_stream(mm3e_ctx* ctx, void* cuda_stream);
+/* SM count and clock of the context's device (for roofline reporting). */
+int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
+
+/* ---- scenes ------------------------------------------------------------------------------- */
+/* Validates and lowers `desc` into a device-resident scene tape; `desc` may be freed after. */
+int mm3e_scene_compile(mm3e_ctx* ctx, const mm3e_scene_desc* desc, mm3e_scene** out);
+void mm3e_scene_destroy(mm3e_scene* scene);
+
+/* Render one frame of `scene` (scene->width x height, scene->mode) into host memory.
+ * `dyn`/`n_dyn` append dynamic spheres exactly as CpuParallelScene::try_render does.
+ * host_out must hold width*height*16 (RGBA_F32) or width*height*4 (RGBA8) bytes.
+ * `stats` may be NULL. Blocking. */
+int mm3e_render(mm3e_scene* scene, const mm3e_camera* camera, const mm3e_dyn_sphere* dyn, size_t n_dyn,
+                uint32_t format, void* host_out, size_t out_bytes, mm3e_render_stats* stats);
+
+/* Beauty radiance before post (render_linear): width*height*3 floats, row-major RGB. */
+int mm3e_render_linear(mm3e_scene* scene, const mm3e_camera* camera, float* host_rgb, size_t n_floats);
+
+/* Device-resident variant: writes into a device buffer on the context's stream (asynchronous;
+ * call mm3e_ctx_sync before reading). Used by benchmarks and the batched/served forms. */
+int mm3e_render_device(mm3e_scene* scene, const mm3e_camera* camera, uint32_t format, void* device_out,
+                       size_t out_bytes);
+
+/* Bake the GI ambient-cube probe volume on the GPU from the scene tape (Scene::bake_gi).
+ * Replaces any GI the scene was compiled with. samples = rays per cube face (1 or 5). */
+int mm3e_bake_gi(mm3e_scene* scene, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t samples);
+/* Read back the scene's GI volume (e.g. after mm3e_bake_gi). `cubes` may be NULL to query dims. */
+int mm3e_scene_get_gi(mm3e_scene* scene, float min[3], float size[3], uint32_t dims[3], float* cubes,
+                      size_t n_floats);
+
+/* ---- diagnostics: primary hits, arbitrary rays, field samples ------------------------------- */
+/* Primary pinhole ray through every pixel centre (the ray RenderMode AOVs and the pinhole film
+ * use, lib.rs:1179): hit distance t, material id (0xFFFFFFFF on a miss), march steps and the
+ * hit normal (3 floats, zero on a miss). Any output pointer except `t` and `mat` may be NULL.
+ * Replaces render_film's depth / matId AOVs for the pinhole lens (film.rs:89-146). */
+int mm3e_render_hits(mm3e_scene* scene, const mm3e_camera* camera, float* t, uint32_t* mat, uint32_t* steps,
+                     float* normal3);
+/* March `n` rays (origin xyz, unit direction xyz) with the scene's Marcher (march.rs:120-209). */
+int mm3e_march_rays(mm3e_scene* scene, const float* rays6, size_t n, float* t, uint32_t* mat, uint32_t* steps);
+/* World field (accelerated plan) at `n` points: Scene::field (lib.rs:715-717). */
+int mm3e_field(mm3e_scene* scene, const float* points3, size_t n, float* dist, uint32_t* mat);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MM3E_CUDA_H */

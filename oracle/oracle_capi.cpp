@@ -1,0 +1,349 @@
+// oracle_capi.cpp — C entry points of the CPU oracle (liboracle_mm3e.so).
+//
+// TEST INFRASTRUCTURE ONLY. Loaded by the tests, by __graft_entry__.smoke() and by bench.py's
+// CPU-baseline leg, always as the checker or the timed CPU reference — never by the product
+// library. Every function takes the same `mm3e_scene_desc` / `mm3e_camera` as the C ABI.
+#include <chrono>
+#include <cstring>
+#include <mutex>
+
+#include "oracle_count.hpp"
+#include "oracle_scene.hpp"
+
+using namespace oracle;
+
+namespace {
+
+template <class T> Camera<T> cam_from(const mm3e_camera& c) {
+    Camera<T> k;
+    k.eye = v3f<T>(c.eye);
+    k.forward = v3f<T>(c.forward);
+    k.right = v3f<T>(c.right);
+    k.up = v3f<T>(c.up);
+    k.fov_scale = T(c.fov_scale);
+    return k;
+}
+
+// Rust f32 `rem_euclid` (core::f32::rem_euclid).
+float rem_euclid_f32(float a, float b) {
+    float r = std::fmod(a, b);
+    return r < 0.0f ? r + std::fabs(b) : r;
+}
+
+// vec.rs:136-141 Rodrigues
+M3<float> from_axis_angle(V3<float> axis, float angle) {
+    V3<float> k = normalize(axis);
+    float s = o_sin(angle), c = o_cos(angle);
+    auto col = [&](V3<float> e) { return scale(e, c) + scale(cross(k, e), s) + scale(k, dot(k, e) * (1.0f - c)); };
+    M3<float> m;
+    m.c[0] = col(V3<float>{1, 0, 0});
+    m.c[1] = col(V3<float>{0, 1, 0});
+    m.c[2] = col(V3<float>{0, 0, 1});
+    return m;
+}
+M3<float> mat_mul(const M3<float>& a, const M3<float>& b) {
+    M3<float> r;
+    for (int i = 0; i < 3; ++i) r.c[i] = mul_vec(a, b.c[i]);
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_abi_version(void) { return MM3E_ABI_VERSION; }
+
+// Camera::look_at (camera.rs:50-55)
+void oracle_camera_look_at(const float eye[3], const float target[3], const float up[3], float fov_y, mm3e_camera* out) {
+    Camera<float> c = camera_look_at(v3f<float>(eye), v3f<float>(target), v3f<float>(up), fov_y);
+    const V3<float>* vs[4] = {&c.eye, &c.forward, &c.right, &c.up};
+    float* dst[4] = {out->eye, out->forward, out->right, out->up};
+    for (int i = 0; i < 4; ++i) {
+        dst[i][0] = vs[i]->x;
+        dst[i][1] = vs[i]->y;
+        dst[i][2] = vs[i]->z;
+    }
+    out->fov_scale = c.fov_scale;
+}
+
+// orbit_camera + wrap_orbit_yaw (mm3e-orchestrator/src/lib.rs:1414-1435)
+void oracle_orbit_camera(const float target[3], float radius, float yaw, float pitch, float fov_y, mm3e_camera* out) {
+    const float PI = 3.14159265358979323846f, TAU = 6.28318530717958647692f, FRAC_PI_2 = 1.57079632679489661923f;
+    yaw = std::isfinite(yaw) ? rem_euclid_f32(yaw + PI, TAU) - PI : 0.0f;
+    float pitch_limit = FRAC_PI_2 - 1.0e-4f;
+    pitch = std::isfinite(pitch) ? o_clamp(pitch, -pitch_limit, pitch_limit) : 0.0f;
+    radius = std::isfinite(radius) ? o_max(std::fabs(radius), 1.0e-4f) : 1.0f;
+    fov_y = std::isfinite(fov_y) ? o_clamp(fov_y, 1.0e-4f, PI - 1.0e-4f) : 45.0f * (PI / 180.0f);
+    V3<float> t = v3f<float>(target);
+    V3<float> eye = t + V3<float>{radius * o_cos(yaw) * o_cos(pitch), radius * o_sin(pitch), radius * o_sin(yaw) * o_cos(pitch)};
+    float e[3] = {eye.x, eye.y, eye.z};
+    float up[3] = {0.0f, 1.0f, 0.0f};
+    oracle_camera_look_at(e, target, up, fov_y, out);
+}
+
+// Mat3::from_euler (vec.rs:144-149)
+void oracle_mat3_from_euler(float x, float y, float z, float out_cols[9]) {
+    M3<float> m = mat_mul(mat_mul(from_axis_angle(V3<float>{1, 0, 0}, x), from_axis_angle(V3<float>{0, 1, 0}, y)),
+                          from_axis_angle(V3<float>{0, 0, 1}, z));
+    for (int c = 0; c < 3; ++c) {
+        out_cols[3 * c + 0] = m.c[c].x;
+        out_cols[3 * c + 1] = m.c[c].y;
+        out_cols[3 * c + 2] = m.c[c].z;
+    }
+}
+
+// Full frame through the reference's render() semantics: beauty (with post) or a debug AOV.
+// rgba: w*h*4 floats (Framebuffer pixels). hdr3 (optional): beauty radiance before post.
+int oracle_render(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, float* rgba, float* hdr3) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    if (s.materials.empty()) return -1;
+    size_t n = (size_t)s.width * s.height;
+    std::vector<V3<float>> hdr(hdr3 ? n : 0);
+    render_frame(s, cam_from<float>(*cam), threads, rgba, hdr3 ? hdr.data() : nullptr);
+    if (hdr3)
+        for (size_t i = 0; i < n; ++i) {
+            hdr3[3 * i] = hdr[i].x;
+            hdr3[3 * i + 1] = hdr[i].y;
+            hdr3[3 * i + 2] = hdr[i].z;
+        }
+    return 0;
+}
+
+// Beauty radiance (render_linear) for rows [y0, y1): the bounded CPU-baseline sample.
+int oracle_render_rows(const mm3e_scene_desc* d, const mm3e_camera* cam, uint32_t y0, uint32_t y1, unsigned threads, float* hdr3) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    if (s.materials.empty() || y1 < y0 || y1 > s.height) return -1;
+    std::vector<V3<float>> rows((size_t)(y1 - y0) * s.width);
+    render_linear_rows(s, cam_from<float>(*cam), y0, y1, threads, rows.data());
+    for (size_t i = 0; i < rows.size(); ++i) {
+        hdr3[3 * i] = rows[i].x;
+        hdr3[3 * i + 1] = rows[i].y;
+        hdr3[3 * i + 2] = rows[i].z;
+    }
+    return 0;
+}
+
+// post::resolve on a given HDR buffer.
+int oracle_post(const mm3e_scene_desc* d, const float* hdr3, float* rgba) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    size_t n = (size_t)s.width * s.height;
+    std::vector<V3<float>> hdr(n);
+    for (size_t i = 0; i < n; ++i) hdr[i] = V3<float>{hdr3[3 * i], hdr3[3 * i + 1], hdr3[3 * i + 2]};
+    post_resolve(hdr, s.width, s.height, s.post, rgba);
+    return 0;
+}
+
+// Primary pinhole ray through each pixel centre (the AOV / film ray): hit mask, t, matId,
+// steps and normal. mat of a miss is reported as 0xFFFFFFFF.
+int oracle_primary_hits(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, float* t, uint32_t* mat,
+                        uint32_t* steps, float* normal3) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    Camera<float> c = cam_from<float>(*cam);
+    bool dual_safe = scene_dual_safe(s);
+    for_row_bands(0, s.height, threads, [&](uint32_t a, uint32_t b, size_t) {
+        World<float> w(s);
+        for (uint32_t y = a; y < b; ++y)
+            for (uint32_t x = 0; x < s.width; ++x) {
+                Ray<float> ray = camera_ray(c, (float)x + 0.5f, (float)y + 0.5f, s.width, s.height);
+                Hit<float> h = march_scene(s, w, dual_safe, ray);
+                size_t i = (size_t)y * s.width + x;
+                t[i] = h.t;
+                mat[i] = h.hit ? h.mat : 0xFFFFFFFFu;
+                if (steps) steps[i] = h.steps;
+                if (normal3) {
+                    normal3[3 * i] = h.normal.x;
+                    normal3[3 * i + 1] = h.normal.y;
+                    normal3[3 * i + 2] = h.normal.z;
+                }
+            }
+    });
+    return 0;
+}
+
+// March arbitrary rays (origin xyz, dir xyz per ray) in f32 or f64 (the FP64 re-march).
+int oracle_march_rays(const mm3e_scene_desc* d, const float* rays6, size_t n, int use_double, unsigned threads,
+                      double* t, uint32_t* mat, uint32_t* steps, double* normal3) {
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        Scene<T> s = scene_from_desc<T>(*d);
+        bool dual_safe = scene_dual_safe(s);
+        for_row_bands(0, (uint32_t)n, threads, [&](uint32_t a, uint32_t b, size_t) {
+            World<T> w(s);
+            for (uint32_t i = a; i < b; ++i) {
+                Ray<T> r{v3f<T>(rays6 + 6 * i), v3f<T>(rays6 + 6 * i + 3)};
+                Hit<T> h = march_scene(s, w, dual_safe, r);
+                t[i] = o_value(h.t);
+                mat[i] = h.hit ? h.mat : 0xFFFFFFFFu;
+                if (steps) steps[i] = h.steps;
+                if (normal3) {
+                    normal3[3 * i] = o_value(h.normal.x);
+                    normal3[3 * i + 1] = o_value(h.normal.y);
+                    normal3[3 * i + 2] = o_value(h.normal.z);
+                }
+            }
+        });
+    };
+    if (use_double) run(double(0));
+    else run(float(0));
+    return 0;
+}
+
+// World field at points (accelerated WorldPlan, or the linear reference fold).
+int oracle_field(const mm3e_scene_desc* d, const float* pts3, size_t n, int linear, float* dist, uint32_t* mat) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    World<float> w(s);
+    for (size_t i = 0; i < n; ++i) {
+        V3<float> p = v3f<float>(pts3 + 3 * i);
+        Field<float> f = linear ? w.linear(p) : w(p);
+        dist[i] = f.dist;
+        mat[i] = f.mat;
+    }
+    return 0;
+}
+
+// Operation counts for one full frame, f32 semantics: 14 values for the render phase
+// (tape interpretation + shading) followed by 14 for the post phase (bloom + tone map):
+// [fp32, add, mul, cmp, minmax, div, sqrt, trans, field_evals, dual_evals,
+//  primary_rays, reflection_rays, shadow_rays, gi_rays]
+int oracle_count_frame(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, uint64_t* counts) {
+    Scene<CountF> s = scene_from_desc<CountF>(*d);
+    Camera<CountF> c = cam_from<CountF>(*cam);
+    size_t n = (size_t)s.width * s.height;
+    std::vector<V3<CountF>> hdr(n);
+    OpCounts render, post;
+    std::mutex mu;
+    bool dual_safe = scene_dual_safe(s);
+    for_row_bands(0, s.height, threads, [&](uint32_t a, uint32_t b, size_t) {
+        op_counts() = OpCounts();
+        World<CountF> w(s);
+        for (uint32_t y = a; y < b; ++y)
+            for (uint32_t x = 0; x < s.width; ++x) {
+                if (s.mode == MM3E_MODE_BEAUTY) hdr[(size_t)y * s.width + x] = shade_pixel(s, w, c, x, y, dual_safe);
+                else (void)aov_pixel(s, w, c, x, y, dual_safe);
+            }
+        std::lock_guard<std::mutex> lk(mu);
+        render.merge(op_counts());
+    });
+    if (s.mode == MM3E_MODE_BEAUTY) {
+        op_counts() = OpCounts();
+        std::vector<float> rgba(4 * n);
+        post_resolve(hdr, s.width, s.height, s.post, rgba.data());
+        post.merge(op_counts());
+    }
+    const OpCounts* phases[2] = {&render, &post};
+    for (int ph = 0; ph < 2; ++ph) {
+        const OpCounts& t = *phases[ph];
+        uint64_t v[14] = {t.fp32(), t.add, t.mul, t.cmp, t.minmax, t.div, t.sqrt, t.trans, t.field_evals, t.dual_evals,
+                          t.primary_rays, t.reflection_rays, t.shadow_rays, t.gi_rays};
+        std::memcpy(counts + 14 * ph, v, sizeof(v));
+    }
+    return 0;
+}
+
+// Scene::bake_gi (lib.rs:665-682). cubes: nx*ny*nz*18 floats. Returns 1 if baked, 0 if the
+// scene has nothing bounded (no GI), negative on error.
+int oracle_bake_gi(const mm3e_scene_desc* d, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t samples, unsigned threads,
+                   float* min3, float* size3, uint32_t* dims3, float* cubes) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    GiVolume<float> g;
+    if (!bake_gi(s, nx, ny, nz, samples, threads, g)) return 0;
+    min3[0] = g.min.x; min3[1] = g.min.y; min3[2] = g.min.z;
+    size3[0] = g.size.x; size3[1] = g.size.y; size3[2] = g.size.z;
+    dims3[0] = (uint32_t)g.nx; dims3[1] = (uint32_t)g.ny; dims3[2] = (uint32_t)g.nz;
+    if (cubes)
+        for (size_t i = 0; i < g.cubes.size(); ++i)
+            for (int f = 0; f < 6; ++f) {
+                cubes[i * 18 + f * 3 + 0] = g.cubes[i][f].x;
+                cubes[i * 18 + f * 3 + 1] = g.cubes[i][f].y;
+                cubes[i * 18 + f * 3 + 2] = g.cubes[i][f].z;
+            }
+    return 1;
+}
+
+// GiVolume::sample on the scene's GI at given points/normals (known-answer tests).
+int oracle_gi_sample(const mm3e_scene_desc* d, const float* pts3, const float* nrm3, size_t n, float* out3) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    if (!s.gi) return -1;
+    for (size_t i = 0; i < n; ++i) {
+        V3<float> r = s.gi->sample(v3f<float>(pts3 + 3 * i), v3f<float>(nrm3 + 3 * i));
+        out3[3 * i] = r.x;
+        out3[3 * i + 1] = r.y;
+        out3[3 * i + 2] = r.z;
+    }
+    return 0;
+}
+
+// ---- kit-level entry points for the reference's known-answer tests ----------------------
+// sdf.rs primitive distance in local space (kind = MM3E_PRIM_* 0..10).
+float oracle_sdf(uint32_t kind, const float* params, float x, float y, float z) {
+    return prim_distance<float>(kind, params, V3<float>{x, y, z});
+}
+// sdf.rs combinators: op 0 union, 1 intersect, 2 subtract, 3 smooth_union, 4 smooth_subtract,
+// 5 smooth_intersect.
+void oracle_combine(uint32_t op, float ad, uint32_t am, float bd, uint32_t bm, float k, float* od, uint32_t* om) {
+    Field<float> a{ad, am}, b{bd, bm}, r;
+    switch (op) {
+        case 0: r = f_union(a, b); break;
+        case 1: r = f_intersect(a, b); break;
+        case 2: r = f_subtract(a, b); break;
+        case 3: r = f_smooth_union(a, b, k); break;
+        case 4: {  // sdf.rs:163-170
+            if (k <= 0.0f) { r = f_subtract(a, b); break; }
+            float h = o_clamp(0.5f - 0.5f * (a.dist + b.dist) / k, 0.0f, 1.0f);
+            r = Field<float>{a.dist * (1.0f - h) + (-b.dist) * h + k * h * (1.0f - h), a.mat};
+            break;
+        }
+        default: {  // sdf.rs:173-181
+            if (k <= 0.0f) { r = f_intersect(a, b); break; }
+            float h = o_clamp(0.5f - 0.5f * (a.dist - b.dist) / k, 0.0f, 1.0f);
+            r = Field<float>{a.dist * (1.0f - h) + b.dist * h + k * h * (1.0f - h), h > 0.5f ? b.mat : a.mat};
+            break;
+        }
+    }
+    *od = r.dist;
+    *om = r.mat;
+}
+// sdf.rs domain ops: op 0 round(d=x, r=a), 1 onion(d=x, t=a), 2 elongate, 3 repeat, 4 twist,
+// 5 bend, 6 mirror (a,b,c as booleans). p = xyz in/out.
+void oracle_domain(uint32_t op, float* p, float a, float b, float c) {
+    V3<float> v{p[0], p[1], p[2]};
+    switch (op) {
+        case 0: p[0] = op_round(p[0], a); return;
+        case 1: p[0] = op_onion(p[0], a); return;
+        case 2: v = op_elongate(v, V3<float>{a, b, c}); break;
+        case 3: v = op_repeat(v, V3<float>{a, b, c}); break;
+        case 4: v = op_twist(v, a); break;
+        case 5: v = op_bend(v, a); break;
+        default: v = op_mirror(v, a != 0.0f, b != 0.0f, c != 0.0f); break;
+    }
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+// shade.rs: brdf / fresnel_schlick / aces
+void oracle_brdf(const float* n, const float* l, const float* v, const float* albedo, float metallic, float roughness,
+                 float reflectance, float* out3) {
+    V3<float> r = brdf(v3f<float>(n), v3f<float>(l), v3f<float>(v), v3f<float>(albedo), metallic, roughness, reflectance);
+    out3[0] = r.x;
+    out3[1] = r.y;
+    out3[2] = r.z;
+}
+float oracle_fresnel(float cos_theta, float f0) { return fresnel_schlick(cos_theta, f0); }
+void oracle_aces(const float* in3, float* out3) {
+    V3<float> r = aces(v3f<float>(in3));
+    out3[0] = r.x;
+    out3[1] = r.y;
+    out3[2] = r.z;
+}
+
+// Wall-clock of a CPU render of rows [y0, y1) in seconds (bench CPU-baseline helper).
+double oracle_time_rows(const mm3e_scene_desc* d, const mm3e_camera* cam, uint32_t y0, uint32_t y1, unsigned threads) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    std::vector<V3<float>> rows((size_t)(y1 - y0) * s.width);
+    auto t0 = std::chrono::steady_clock::now();
+    render_linear_rows(s, cam_from<float>(*cam), y0, y1, threads, rows.data());
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"

@@ -1,0 +1,207 @@
+"""Python binding of the CPU oracle (liboracle_mm3e.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg, as the checker or the timed CPU reference. It takes the same scene descriptions
+(`Scene.desc()`) and cameras as the CUDA library.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import build_oracle  # noqa: E402
+
+_lib = None
+P = C.POINTER
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        l = C.CDLL(path)
+        vp = C.c_void_p
+        l.oracle_render.argtypes = [vp, vp, C.c_uint, P(C.c_float), P(C.c_float)]
+        l.oracle_render_rows.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint, P(C.c_float)]
+        l.oracle_post.argtypes = [vp, P(C.c_float), P(C.c_float)]
+        l.oracle_primary_hits.argtypes = [vp, vp, C.c_uint, P(C.c_float), P(C.c_uint32), P(C.c_uint32), P(C.c_float)]
+        l.oracle_march_rays.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_int, C.c_uint, P(C.c_double),
+                                        P(C.c_uint32), P(C.c_uint32), P(C.c_double)]
+        l.oracle_sdf.argtypes = [C.c_uint32, P(C.c_float), C.c_float, C.c_float, C.c_float]
+        l.oracle_sdf.restype = C.c_float
+        l.oracle_combine.argtypes = [C.c_uint32, C.c_float, C.c_uint32, C.c_float, C.c_uint32, C.c_float,
+                                     P(C.c_float), P(C.c_uint32)]
+        l.oracle_domain.argtypes = [C.c_uint32, P(C.c_float), C.c_float, C.c_float, C.c_float]
+        l.oracle_brdf.argtypes = [P(C.c_float)] * 4 + [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        l.oracle_fresnel.argtypes = [C.c_float, C.c_float]
+        l.oracle_fresnel.restype = C.c_float
+        l.oracle_aces.argtypes = [P(C.c_float), P(C.c_float)]
+        l.oracle_field.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_int, P(C.c_float), P(C.c_uint32)]
+        l.oracle_count_frame.argtypes = [vp, vp, C.c_uint, P(C.c_uint64)]
+        l.oracle_bake_gi.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint, P(C.c_float),
+                                     P(C.c_float), P(C.c_uint32), P(C.c_float)]
+        l.oracle_gi_sample.argtypes = [vp, P(C.c_float), P(C.c_float), C.c_size_t, P(C.c_float)]
+        l.oracle_time_rows.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint]
+        l.oracle_time_rows.restype = C.c_double
+        l.oracle_camera_look_at.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_float, vp]
+        l.oracle_orbit_camera.argtypes = [P(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float, vp]
+        l.oracle_mat3_from_euler.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        _lib = l
+    return _lib
+
+
+def threads_default():
+    return os.cpu_count() or 1
+
+
+def _f(a):
+    return a.ctypes.data_as(P(C.c_float))
+
+
+def render(handle, cam, threads=None, want_hdr=False):
+    """Reference render(): RGBA f32 framebuffer (h, w, 4) [, HDR (h, w, 3)]."""
+    d = handle.desc
+    h, w = d.height, d.width
+    rgba = np.zeros((h, w, 4), np.float32)
+    hdr = np.zeros((h, w, 3), np.float32) if want_hdr else None
+    rc = lib().oracle_render(C.addressof(d), C.addressof(cam), threads or threads_default(), _f(rgba),
+                             _f(hdr) if want_hdr else None)
+    if rc != 0:
+        raise RuntimeError(f"oracle_render failed ({rc})")
+    return (rgba, hdr) if want_hdr else rgba
+
+
+def render_rows(handle, cam, y0, y1, threads=None):
+    d = handle.desc
+    out = np.zeros((y1 - y0, d.width, 3), np.float32)
+    rc = lib().oracle_render_rows(C.addressof(d), C.addressof(cam), y0, y1, threads or threads_default(), _f(out))
+    if rc != 0:
+        raise RuntimeError("oracle_render_rows failed")
+    return out
+
+
+def post(handle, hdr):
+    d = handle.desc
+    hdr = np.ascontiguousarray(hdr, np.float32)
+    rgba = np.zeros((d.height, d.width, 4), np.float32)
+    lib().oracle_post(C.addressof(d), _f(hdr), _f(rgba))
+    return rgba
+
+
+def primary_hits(handle, cam, threads=None):
+    d = handle.desc
+    n = d.width * d.height
+    t = np.zeros(n, np.float32)
+    m = np.zeros(n, np.uint32)
+    s = np.zeros(n, np.uint32)
+    nrm = np.zeros(3 * n, np.float32)
+    lib().oracle_primary_hits(C.addressof(d), C.addressof(cam), threads or threads_default(), _f(t),
+                              m.ctypes.data_as(P(C.c_uint32)), s.ctypes.data_as(P(C.c_uint32)), _f(nrm))
+    shape = (d.height, d.width)
+    return {"t": t.reshape(shape), "mat": m.reshape(shape), "steps": s.reshape(shape),
+            "normal": nrm.reshape(shape + (3,))}
+
+
+def march_rays(handle, rays6, use_double=False, threads=None, normals=False):
+    rays6 = np.ascontiguousarray(rays6, np.float32).reshape(-1, 6)
+    n = len(rays6)
+    t = np.zeros(n, np.float64)
+    m = np.zeros(n, np.uint32)
+    s = np.zeros(n, np.uint32)
+    nrm = np.zeros(3 * n, np.float64) if normals else None
+    lib().oracle_march_rays(C.addressof(handle.desc), _f(rays6), n, 1 if use_double else 0, threads or threads_default(),
+                            t.ctypes.data_as(P(C.c_double)), m.ctypes.data_as(P(C.c_uint32)),
+                            s.ctypes.data_as(P(C.c_uint32)),
+                            nrm.ctypes.data_as(P(C.c_double)) if normals else None)
+    if normals:
+        return t, m, s, nrm.reshape(n, 3)
+    return t, m, s
+
+
+def sdf(kind, params, p):
+    q = (C.c_float * 7)(*(list(params) + [0.0] * (7 - len(params))))
+    return lib().oracle_sdf(kind, q, p[0], p[1], p[2])
+
+
+def combine(op, a, b, k=0.0):
+    """a, b = (dist, mat); op 0 union, 1 intersect, 2 subtract, 3 smooth_union, 4 smooth_subtract,
+    5 smooth_intersect."""
+    d = C.c_float()
+    m = C.c_uint32()
+    lib().oracle_combine(op, a[0], a[1], b[0], b[1], k, C.byref(d), C.byref(m))
+    return d.value, m.value
+
+
+def domain(op, p, a=0.0, b=0.0, c=0.0):
+    v = (C.c_float * 3)(*p)
+    lib().oracle_domain(op, v, a, b, c)
+    return tuple(v)
+
+
+def brdf(n, l, v, albedo, metallic, roughness, reflectance):
+    out = (C.c_float * 3)()
+    F3 = C.c_float * 3
+    lib().oracle_brdf(F3(*n), F3(*l), F3(*v), F3(*albedo), metallic, roughness, reflectance, out)
+    return tuple(out)
+
+
+def fresnel(c, f0):
+    return lib().oracle_fresnel(c, f0)
+
+
+def aces(x):
+    out = (C.c_float * 3)()
+    lib().oracle_aces((C.c_float * 3)(*x), out)
+    return tuple(out)
+
+
+def field(handle, pts, linear=False):
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    d = np.zeros(len(pts), np.float32)
+    m = np.zeros(len(pts), np.uint32)
+    lib().oracle_field(C.addressof(handle.desc), _f(pts), len(pts), 1 if linear else 0, _f(d),
+                       m.ctypes.data_as(P(C.c_uint32)))
+    return d, m
+
+
+COUNT_KEYS = ["fp32", "add", "mul", "cmp", "minmax", "div", "sqrt", "trans", "field_evals", "dual_evals",
+              "primary_rays", "reflection_rays", "shadow_rays", "gi_rays"]
+
+
+def count_frame(handle, cam, threads=None):
+    """Algorithmic work of one frame: {"render": {...}, "post": {...}} (f32 op counts, rays)."""
+    out = (C.c_uint64 * 28)()
+    lib().oracle_count_frame(C.addressof(handle.desc), C.addressof(cam), threads or threads_default(), out)
+    vals = [int(v) for v in out]
+    return {"render": dict(zip(COUNT_KEYS, vals[:14])), "post": dict(zip(COUNT_KEYS, vals[14:]))}
+
+
+def bake_gi(handle, dims, samples, threads=None):
+    """Scene::bake_gi on the CPU: (min, size, dims, cubes[n*18]) or None if nothing is bounded."""
+    mn = np.zeros(3, np.float32)
+    sz = np.zeros(3, np.float32)
+    dd = np.zeros(3, np.uint32)
+    n = max(1, dims[0]) * max(1, dims[1]) * max(1, dims[2])
+    cubes = np.zeros(n * 18, np.float32)
+    rc = lib().oracle_bake_gi(C.addressof(handle.desc), dims[0], dims[1], dims[2], samples,
+                              threads or threads_default(), _f(mn), _f(sz), dd.ctypes.data_as(P(C.c_uint32)), _f(cubes))
+    if rc == 0:
+        return None
+    return tuple(mn), tuple(sz), tuple(int(x) for x in dd), cubes
+
+
+def gi_sample(handle, pts, nrm):
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    out = np.zeros_like(pts)
+    rc = lib().oracle_gi_sample(C.addressof(handle.desc), _f(pts), _f(nrm), len(pts), _f(out))
+    if rc != 0:
+        raise RuntimeError("scene has no GI")
+    return out
+
+
+def time_rows(handle, cam, y0, y1, threads=None):
+    return lib().oracle_time_rows(C.addressof(handle.desc), C.addressof(cam), y0, y1, threads or threads_default())

@@ -1,0 +1,189 @@
+"""CUDA render path vs the CPU oracle on the same seeded scenes (spec acceptance bars).
+
+(i)   hit/miss mask and matId identical except on silhouette pixels (mismatch <= 0.1%)
+(ii)  hit distance within 1e-4 relative on agreed hits
+(iii) final RGB8 within 1 LSB on >= 99.9% of pixels, PSNR >= 50 dB
+All calls go through the C ABI (libmm3e_cuda.so).
+"""
+import json
+
+import numpy as np
+import pytest
+
+import mm3e_cuda
+import oracle_py
+from mm3e_cuda import abi, scenes
+from mm3e_cuda.scene import DynSphere, GiVolume
+from parity import hit_metrics, image_metrics
+
+pytestmark = pytest.mark.gpu
+
+PSNR_MIN = 50.0
+WITHIN1_MIN = 0.999
+MISMATCH_MAX = 0.001
+T_WITHIN_MIN = 0.999
+
+
+def _render_pair(ctx, scene, cam, threads=None):
+    compiled = mm3e_cuda.CompiledScene(ctx, scene)
+    gpu = compiled.render(cam, fmt=abi.FB_RGBA8)
+    ref = mm3e_cuda.to_rgba8(oracle_py.render(scene.desc(), cam, threads=threads))
+    return compiled, gpu, ref
+
+
+def _check_image(name, gpu, ref):
+    m = image_metrics(gpu, ref)
+    print(name, json.dumps(m))
+    assert m["psnr"] >= PSNR_MIN, (name, m)
+    assert m["within1_px"] >= WITHIN1_MIN, (name, m)
+    return m
+
+
+def _check_hits(name, compiled, scene, cam):
+    g = compiled.render_hits(cam)
+    r = oracle_py.primary_hits(scene.desc(), cam)
+    m = hit_metrics(g, r)
+    print(name, "hits", json.dumps(m))
+    assert m["mismatch_frac"] <= MISMATCH_MAX, (name, m)
+    assert m["t_within_1e-4"] >= T_WITHIN_MIN, (name, m)
+    return m
+
+
+SCENES = {
+    "spheres": lambda: scenes.spheres_scene(240, 135),
+    "gallery": lambda: scenes.gallery_scene(320, 180),
+    "hero_aa2_b2": lambda: scenes.hero_scene(240, 135, 2, 2),
+    "demo": scenes.demo_scene,
+    "canonical_assets": scenes.canonical_asset_scene,
+}
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_beauty_parity(gpu_ctx, name):
+    scene, cam = SCENES[name]()
+    compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image(name, gpu, ref)
+    _check_hits(name, compiled, scene, cam)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_procedural_parity(gpu_ctx, seed):
+    scene, cam = scenes.procedural_scene(seed, 160, 90)
+    compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image(f"procedural{seed}", gpu, ref)
+    _check_hits(f"procedural{seed}", compiled, scene, cam)
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_NORMAL, abi.MODE_DEPTH, abi.MODE_AO, abi.MODE_STEPS, abi.MODE_ALBEDO])
+def test_aov_modes(gpu_ctx, mode):
+    scene, cam = scenes.demo_scene()
+    scene.mode = mode
+    _, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image(f"aov{mode}", gpu, ref)
+
+
+def test_render_linear_hdr(gpu_ctx):
+    scene, cam = scenes.spheres_scene(160, 90)
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    gpu = compiled.render_linear(cam)
+    _, ref = oracle_py.render(scene.desc(), cam, want_hdr=True)
+    rel = np.abs(gpu - ref) / np.maximum(np.abs(ref), 1e-3)
+    frac = float((rel <= 1e-3).mean())
+    print("hdr within 1e-3 rel:", frac, "max", float(rel.max()))
+    assert frac >= 0.999
+
+
+def test_dynamic_spheres(gpu_ctx):
+    """CpuParallelScene::try_render semantics (canonical.rs:102-117)."""
+    scene, cam = scenes.canonical_scene()
+    scene.light(mm3e_cuda.directional((0.4, 0.2, 1.0), (1.0, 1.0, 1.0)))
+    dyn = [DynSphere((0.0, 0.0, 0.0), 0.9, (0.9, 0.02, 0.01), 0.0)]
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    gpu = compiled.render(cam, dyn, fmt=abi.FB_RGBA8)
+    ref_scene = scene.copy()
+    mid = ref_scene.material(mm3e_cuda.Material(albedo=(0.9, 0.02, 0.01), metallic=0.0))
+    ref_scene.add(mm3e_cuda.Object(mm3e_cuda.Prim.sphere(0.9), mm3e_cuda.Transform.at((0.0, 0.0, 0.0)), mid))
+    ref = mm3e_cuda.to_rgba8(oracle_py.render(ref_scene.desc(), cam))
+    _check_image("dyn", gpu, ref)
+    px = gpu[20, 32]
+    assert int(px[0]) > int(px[1]) + 60  # the red dynamic sphere is lit
+
+
+def test_invalid_dynamic_spheres_rejected(gpu_ctx):
+    """canonical.rs:205-226: invalid dynamic inputs fail without poisoning the source."""
+    scene, cam = scenes.canonical_scene()
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    valid = DynSphere((0.0, 0.0, 0.0), 0.5, (1.0, 1.0, 1.0), 0.0)
+    bad = [DynSphere((float("nan"), 0.0, 0.0), 0.5, (1, 1, 1), 0.0), DynSphere((0, 0, 0), 0.0, (1, 1, 1), 0.0),
+           DynSphere((0, 0, 0), -0.5, (1, 1, 1), 0.0), DynSphere((0, 0, 0), float("inf"), (1, 1, 1), 0.0),
+           DynSphere((0, 0, 0), 0.5, (0.1, float("nan"), 0.2), 0.0), DynSphere((0, 0, 0), 0.5, (1.1, 0, 0), 0.0),
+           DynSphere((0, 0, 0), 0.5, (1, 1, 1), -0.1)]
+    before = compiled.render(cam, fmt=abi.FB_RGBA8)
+    for b in bad:
+        with pytest.raises(mm3e_cuda.RenderError) as e:
+            compiled.render(cam, [valid, b])
+        assert e.value.code == abi.ERR_INVALID
+    after = compiled.render(cam, fmt=abi.FB_RGBA8)
+    assert np.array_equal(before, after)
+
+
+def test_field_matches_oracle(gpu_ctx):
+    scene, cam = scenes.gallery_scene(64, 36)
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    rng = np.random.default_rng(7)
+    pts = rng.uniform([-8, -1, -8], [8, 4, 8], size=(20000, 3)).astype(np.float32)
+    gd, gm = compiled.field(pts)
+    rd, rm = oracle_py.field(scene.desc(), pts)
+    rel = np.abs(gd - rd) / np.maximum(np.abs(rd), 1e-3)
+    print("field rel max", float(rel.max()), "mat agree", float((gm == rm).mean()))
+    assert float((rel <= 1e-4).mean()) >= 0.999
+    assert float((gm == rm).mean()) >= 0.999
+
+
+def test_fp64_remarch_report(gpu_ctx):
+    """(iv): an FP64 re-march of seeded rays reports the error of both implementations."""
+    scene, cam = scenes.gallery_scene(64, 36)
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    rng = np.random.default_rng(11)
+    n = 4096
+    org = np.tile(np.array(cam.eye, np.float32), (n, 1))
+    d = rng.normal(size=(n, 3)) * [0.35, 0.15, 0.35] + np.array(cam.forward)
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    rays = np.concatenate([org, d], axis=1).astype(np.float32)
+    gt, gm, _ = compiled.march_rays(rays)
+    ot, om, _ = oracle_py.march_rays(scene.desc(), rays)
+    dt, dm, _ = oracle_py.march_rays(scene.desc(), rays, use_double=True)
+    both = (gm != 0xFFFFFFFF) & (om != 0xFFFFFFFF) & (dm != 0xFFFFFFFF) & (gm == dm) & (om == dm)
+    eg = np.abs(gt[both] - dt[both]) / dt[both]
+    eo = np.abs(ot[both] - dt[both]) / dt[both]
+    report = {"rays": n, "common_hits": int(both.sum()), "gpu_rel_err_p50": float(np.median(eg)),
+              "gpu_rel_err_max": float(eg.max()), "oracle_rel_err_p50": float(np.median(eo)),
+              "oracle_rel_err_max": float(eo.max()), "mat_agree_gpu_vs_f64": float((gm == dm).mean())}
+    print("fp64", json.dumps(report))
+    assert report["common_hits"] > n // 4
+    assert float(np.median(eg)) <= 10 * max(float(np.median(eo)), 1e-6)
+
+
+def test_gi_bake_matches_oracle(gpu_ctx):
+    scene, cam = scenes.cornell_scene(160, 90)
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    compiled.bake_gi((8, 8, 8), 5)
+    g = compiled.get_gi()
+    r = oracle_py.bake_gi(scene.desc(), (8, 8, 8), 5)
+    assert g.dims == r[2]
+    assert np.allclose(g.min, r[0]) and np.allclose(g.size, r[1])
+    rel = np.abs(g.cubes - r[3]) / np.maximum(np.abs(r[3]), 1e-3)
+    print("gi cubes within 1e-3 rel:", float((rel <= 1e-3).mean()), "max", float(rel.max()))
+    assert float((rel <= 1e-3).mean()) >= 0.99
+    # render with the GPU-baked GI vs the oracle with the same cubes
+    scene.gi = GiVolume(g.min, g.size, g.dims, g.cubes)
+    compiled2, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image("cornell_gi", gpu, ref)
+
+
+def test_unsupported_surface_rejected(gpu_ctx):
+    scene, _ = scenes.canonical_scene()
+    scene.add(mm3e_cuda.Object(mm3e_cuda.Prim.surface(0), mm3e_cuda.Transform.IDENTITY, 0))
+    with pytest.raises(mm3e_cuda.RenderError) as e:
+        mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    assert e.value.code == abi.ERR_UNSUPPORTED
