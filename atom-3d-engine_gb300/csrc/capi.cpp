@@ -18,6 +18,7 @@
 #include "../../include/mm3e_cuda.h"
 #include "kernels.h"
 #include "lower.h"
+#include "noalloc.h"
 
 using namespace mm3e;
 
@@ -928,6 +929,21 @@ int mm3e_field(mm3e_scene* s, const float* points3, size_t n, float* dist, uint3
     cudaFree(d_d);
     cudaFree(d_m);
     return e == cudaSuccess ? MM3E_OK : cuda_fail(c, e, "field");
+}
+
+// Allocation-free ray queries: the scratch lives in noalloc.cu's fixed __device__ array.
+int mm3e_march_rays_noalloc(mm3e_scene* s, const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat,
+                            uint32_t* d_steps) {
+    if (!s || (n && (!d_rays6 || !d_t || !d_mat))) return MM3E_ERR_INVALID;
+    mm3e_ctx* c = s->ctx;
+    cudaSetDevice(c->device);
+    const char* what = "";
+    int rc = noalloc_march_rays(s->d_tape, (uint32_t)s->low.blob.size(), c->device, c->sm_count, c->stream, d_rays6, n,
+                                d_t, d_mat, d_steps, &what);
+    if (rc == 1) return fail(c, MM3E_ERR_INVALID, what);
+    if (rc == 2) return fail(c, MM3E_ERR_CUDA, what);
+    if (rc == 3) return fail(c, MM3E_ERR_TIMEOUT, what);
+    return MM3E_OK;
 }
 
 }  // extern "C"

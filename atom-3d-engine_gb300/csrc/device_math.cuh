@@ -211,7 +211,7 @@ MD float volume_sample(const DevVolume& v, V p) {
 }
 
 // csg.rs:95-118 as a post-order stack program.
-__device__ __noinline__ float csg_eval(const DevCsgOp* op, V p) {
+static __device__ __noinline__ float csg_eval(const DevCsgOp* op, V p) {
     float vals[MAX_CSG_STACK];
     V pts[MAX_CSG_STACK];
     int vs = 0, ps = 0;
@@ -518,7 +518,7 @@ MD D dd_box(D x, D y, D z, V half) {
     return dadd(out, in);
 }
 // Prim::distance_dual (lib.rs:244-261; dual.rs:129-232)
-__device__ __noinline__ D prim_dual(uint32_t kind, const float* q, D x, D y, D z) {
+static __device__ __noinline__ D prim_dual(uint32_t kind, const float* q, D x, D y, D z) {
     switch (kind) {
         case 0: return dadds(dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z))), -q[0]);
         case 1: return dd_box(x, y, z, V{q[0], q[1], q[2]});
@@ -618,7 +618,7 @@ MD D object_dual(const DevObject& o, V p) {
     return d;
 }
 // Scene::normal_dual (lib.rs:820-835): every object, no pruning; combine mode in flags bits 16-17.
-__device__ __noinline__ V normal_dual(const DevObject* objs, uint32_t n, V p) {
+static __device__ __noinline__ V normal_dual(const DevObject* objs, uint32_t n, V p) {
     if (n == 0) return V{0.f, 0.f, 0.f};
     D acc = object_dual(objs[0], p);
     for (uint32_t i = 1; i < n; ++i) {

@@ -103,4 +103,5 @@ EXPORTED_SYMBOLS = [
     "mm3e_ctx_create", "mm3e_ctx_destroy", "mm3e_last_error", "mm3e_ctx_sync", "mm3e_ctx_set_stream", "mm3e_ctx_device_info",
     "mm3e_scene_compile", "mm3e_scene_destroy", "mm3e_render", "mm3e_render_linear", "mm3e_render_device",
     "mm3e_bake_gi", "mm3e_scene_get_gi", "mm3e_render_hits", "mm3e_march_rays", "mm3e_field",
+    "mm3e_march_rays_noalloc",
 ]

@@ -61,6 +61,8 @@ def _declare_extra(lib):
         "mm3e_march_rays": (C.c_int, [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_uint32),
                                       P(C.c_uint32)]),
         "mm3e_field": (C.c_int, [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_uint32)]),
+        "mm3e_march_rays_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
+                                              C.c_void_p]),
     }
     for name, (res, args) in extra.items():
         fn = getattr(lib, name, None)

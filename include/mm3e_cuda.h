@@ -327,6 +327,23 @@ int mm3e_march_rays(mm3e_scene* scene, const float* rays6, size_t n, float* t, u
 /* World field (accelerated plan) at `n` points: Scene::field (lib.rs:715-717). */
 int mm3e_field(mm3e_scene* scene, const float* points3, size_t n, float* dist, uint32_t* mat);
 
+/* ---- allocation-free ray queries --------------------------------------------------------- */
+/* No counterpart in the reference: an addition for callers that cannot allocate device memory
+ * while they query, e.g. a game or simulation loop casting picking / collision rays every frame
+ * (cudaMalloc and cudaFree synchronise the device and can stall it for milliseconds) or a
+ * service whose device memory is fully reserved up front by a pool or budget.
+ * Marches `n` rays exactly as mm3e_march_rays does, but every pointer is DEVICE memory:
+ * d_rays6 holds origin xyz + unit direction xyz per ray; d_t, d_mat (0xFFFFFFFF on a miss) and
+ * d_steps (may be NULL) receive the results. The call allocates nothing: the ray queue and hit
+ * records live in one fixed __device__ array (about 14.7 MB, held by every GPU that loads the
+ * library until the process exits), so n is limited to 262144 rays per call (larger n returns
+ * MM3E_ERR_INVALID). The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. Every call shares the
+ * array and overwrites it; calls that overlap on the GPU race on it, so serialise them.
+ * Blocking: returns after the results are written. */
+int mm3e_march_rays_noalloc(mm3e_scene* scene, const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat,
+                            uint32_t* d_steps);
+
 #ifdef __cplusplus
 }
 #endif
