@@ -1,10 +1,10 @@
 // capi.cpp — the C ABI (include/mm3e_cuda.h): contexts, compiled scenes and frame rendering.
 //
 // A context owns one CUDA stream on one device. A compiled scene owns its device tape, the
-// uploaded payloads (SDF volume samples, GI probe cubes), the per-frame buffers (HDR, bloom
-// scratch, output) and a pinned staging buffer for host copies, so a render call allocates
-// nothing. Host-side arithmetic that mirrors Rust constructors is binary32 without
-// contraction (this file is compiled with -ffp-contract=off).
+// uploaded payloads (SDF volume samples, GI probe cubes), its pass buffers (ray queues, hit
+// records, HDR and bloom arrays), an output framebuffer and a pinned staging buffer for host
+// copies, so a render call allocates nothing. Host-side arithmetic that mirrors Rust
+// constructors is binary32 without contraction (this file is compiled with -ffp-contract=off).
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -15,89 +15,59 @@
 #include <string>
 #include <vector>
 
-#include "../../include/mm3e_cuda.h"
-#include "kernels.h"
-#include "lower.h"
+#include "batch.h"
+#include "capi_internal.h"
 #include "noalloc.h"
 
 using namespace mm3e;
 
-struct mm3e_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;      // stream all work is issued on
-    cudaStream_t own_stream = nullptr;  // the context's own stream
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    int sm_count = 0, clock_khz = 0;
-    uint32_t* d_counter = nullptr;  // [0] work counter, [1] status word
-    std::string err;
-    std::set<mm3e_scene*> scenes;   // live scenes; destroyed with the context
-};
+mm3e_ctx::~mm3e_ctx() = default;
 
-namespace {
+namespace mm3e {
 
-// Owned deep copy of a scene description (host), so dynamic spheres and GI bakes can
-// re-lower the scene after the caller has released its arrays.
-struct SceneCopy {
-    mm3e_scene_desc d{};
-    std::vector<mm3e_object> objects;
-    std::vector<mm3e_material> materials;
-    std::vector<mm3e_light> lights;
-    std::vector<mm3e_volume> volumes;
-    std::vector<std::vector<float>> volume_data;
-    std::vector<mm3e_csg_node> csg_nodes;
-    std::vector<uint32_t> csg_roots;
-    bool has_gi = false;
-    mm3e_gi gi{};
-    std::vector<float> gi_cubes;
-
-    void assign(const mm3e_scene_desc& s) {
-        d = s;
-        objects.assign(s.objects, s.objects + s.n_objects);
-        materials.assign(s.materials, s.materials + s.n_materials);
-        lights.assign(s.lights, s.lights + s.n_lights);
-        volumes.assign(s.volumes, s.volumes + s.n_volumes);
-        volume_data.resize(s.n_volumes);
-        for (uint32_t i = 0; i < s.n_volumes; ++i) {
-            size_t n = (size_t)s.volumes[i].nx * s.volumes[i].ny * s.volumes[i].nz;
-            volume_data[i].assign(s.volumes[i].data, s.volumes[i].data + n);
-        }
-        csg_nodes.assign(s.csg_nodes, s.csg_nodes + s.n_csg_nodes);
-        csg_roots.assign(s.csg_roots, s.csg_roots + s.n_csgs);
-        has_gi = s.gi != nullptr;
-        if (has_gi) {
-            gi = *s.gi;
-            size_t n = (size_t)gi.nx * gi.ny * gi.nz * 18;
-            gi_cubes.assign(s.gi->cubes, s.gi->cubes + n);
-        }
-        fix();
+void SceneCopy::assign(const mm3e_scene_desc& s) {
+    d = s;
+    objects.assign(s.objects, s.objects + s.n_objects);
+    materials.assign(s.materials, s.materials + s.n_materials);
+    lights.assign(s.lights, s.lights + s.n_lights);
+    volumes.assign(s.volumes, s.volumes + s.n_volumes);
+    volume_data.resize(s.n_volumes);
+    for (uint32_t i = 0; i < s.n_volumes; ++i) {
+        size_t n = (size_t)s.volumes[i].nx * s.volumes[i].ny * s.volumes[i].nz;
+        volume_data[i].assign(s.volumes[i].data, s.volumes[i].data + n);
     }
-    void fix() {
-        d.objects = objects.data();
-        d.materials = materials.data();
-        d.lights = lights.data();
-        for (size_t i = 0; i < volumes.size(); ++i) volumes[i].data = volume_data[i].data();
-        d.volumes = volumes.data();
-        d.csg_nodes = csg_nodes.data();
-        d.csg_roots = csg_roots.data();
-        if (has_gi) {
-            gi.cubes = gi_cubes.data();
-            d.gi = &gi;
-        } else {
-            d.gi = nullptr;
-        }
+    csg_nodes.assign(s.csg_nodes, s.csg_nodes + s.n_csg_nodes);
+    csg_roots.assign(s.csg_roots, s.csg_roots + s.n_csgs);
+    has_gi = s.gi != nullptr;
+    if (has_gi) {
+        gi = *s.gi;
+        size_t n = (size_t)gi.nx * gi.ny * gi.nz * 18;
+        gi_cubes.assign(s.gi->cubes, s.gi->cubes + n);
     }
-};
+    fix();
+}
 
-template <class T> T* dmalloc(size_t n, cudaError_t& e) {
-    void* p = nullptr;
-    e = cudaMalloc(&p, n * sizeof(T) + 16);
-    return e == cudaSuccess ? static_cast<T*>(p) : nullptr;
+void SceneCopy::fix() {
+    d.objects = objects.data();
+    d.materials = materials.data();
+    d.lights = lights.data();
+    for (size_t i = 0; i < volumes.size(); ++i) volumes[i].data = volume_data[i].data();
+    d.volumes = volumes.data();
+    d.csg_nodes = csg_nodes.data();
+    d.csg_roots = csg_roots.data();
+    if (has_gi) {
+        gi.cubes = gi_cubes.data();
+        d.gi = &gi;
+    } else {
+        d.gi = nullptr;
+    }
 }
 
 int fail(mm3e_ctx* c, int code, const std::string& msg) {
     if (c) c->err = msg;
     return code;
 }
+
 int cuda_fail(mm3e_ctx* c, cudaError_t e, const char* what) {
     return fail(c, e == cudaErrorMemoryAllocation ? MM3E_ERR_NO_MEMORY : MM3E_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
@@ -118,54 +88,61 @@ std::vector<float> gaussian_kernel(uint32_t radius) {
     return k;
 }
 
-}  // namespace
+void fill_camera(CameraArgs& a, const mm3e_camera& c) {
+    std::memcpy(a.eye, c.eye, 12);
+    std::memcpy(a.fwd, c.forward, 12);
+    std::memcpy(a.right, c.right, 12);
+    std::memcpy(a.up, c.up, 12);
+    a.fov_scale = c.fov_scale;
+}
 
-// Device buffers of the wavefront passes for up to `cap` rays (queues double-buffered).
-struct WaveStore {
-    size_t cap = 0, lights = 0, levels = 0;
-    float4 *qa_o = nullptr, *qa_d = nullptr, *qb_o = nullptr, *qb_d = nullptr, *h_n = nullptr;
-    uint2* h_m = nullptr;
-    float *occ = nullptr, *shadow = nullptr;
-    float4 *lvl = nullptr, *term = nullptr;
-    void release() {
-        void* ps[] = {qa_o, qa_d, qb_o, qb_d, h_n, h_m, occ, shadow, lvl, term};
-        for (void* p : ps) cudaFree(p);
-        *this = WaveStore();
-    }
-};
+FrameJob scene_job(const mm3e_scene* s, const unsigned char* tape, const mm3e_camera& cam, uint32_t w, uint32_t h,
+                   uint32_t wlog) {
+    FrameJob j{};
+    j.tape = tape ? tape : s->d_tape;
+    j.bloom_w = s->d_kernel;
+    fill_camera(j.cam, cam);
+    j.width = w ? w : s->low.width;
+    j.height = h ? h : s->low.height;
+    j.aa = s->low.aa;
+    j.spp = j.aa * j.aa;
+    j.tiles_x = tiles_x_of(j.width, wlog);
+    j.n_slots = (uint32_t)slots_of(j.width, j.height, wlog);
+    j.n_samples = j.n_slots * j.spp;
+    j.n_pixels = j.width * j.height;
+    j.n_lights = s->n_lights();
+    const mm3e_post& post = s->src.d.post;
+    j.bloom_radius = s->bloom_radius;
+    j.flags = (post.bloom && post.bloom_intensity > 0.0f) ? JF_BLOOM : 0u;
+    j.threshold = post.bloom_threshold;
+    j.intensity = post.bloom_intensity;
+    j.exposure = post.exposure;
+    j.format = MM3E_FB_RGBA8;
+    return j;
+}
 
-struct mm3e_scene {
-    mm3e_ctx* ctx = nullptr;
-    SceneCopy src;
-    LoweredScene low;
-    unsigned char* d_tape = nullptr;
-    size_t tape_cap = 0;
-    unsigned char* d_dyn_tape = nullptr;  // tape with dynamic spheres appended
-    size_t dyn_cap = 0;
-    std::vector<void*> d_payloads;        // same order as low.payloads
-    float* d_kernel = nullptr;            // bloom weights
-    uint32_t bloom_radius = 0;
-    float4 *d_hdr = nullptr, *d_bright = nullptr, *d_blur = nullptr, *d_out = nullptr;
-    void* h_stage = nullptr;              // pinned staging (w*h*16 bytes)
-    size_t pixels = 0;
-    WaveStore wave;                       // frame ray queues / hit records
-    uint32_t* d_counters = nullptr;       // 64 words: work counters, queue lengths, status (63)
+}  // namespace mm3e
 
-    ~mm3e_scene() {
-        if (ctx) cudaSetDevice(ctx->device);
-        cudaFree(d_tape);
-        cudaFree(d_dyn_tape);
-        for (void* p : d_payloads) cudaFree(p);
-        cudaFree(d_kernel);
-        cudaFree(d_hdr);
-        cudaFree(d_bright);
-        cudaFree(d_blur);
-        cudaFree(d_out);
-        cudaFree(d_counters);
-        wave.release();
-        if (h_stage) cudaFreeHost(h_stage);
-    }
-};
+uint32_t mm3e_scene::n_lights() const {
+    return low.blob.empty() ? 0u : reinterpret_cast<const TapeHeader*>(low.blob.data())->n_lights;
+}
+
+size_t mm3e_scene::device_bytes() const {
+    size_t b = tape_cap + dyn_cap + buf.bytes() + pixels * sizeof(float4);
+    for (const auto& p : low.payloads) b += p.bytes;
+    return b;
+}
+
+mm3e_scene::~mm3e_scene() {
+    if (ctx) cudaSetDevice(ctx->device);
+    cudaFree(d_tape);
+    cudaFree(d_dyn_tape);
+    for (void* p : d_payloads) cudaFree(p);
+    cudaFree(d_kernel);
+    cudaFree(d_out);
+    buf.release();
+    if (h_stage) cudaFreeHost(h_stage);
+}
 
 namespace {
 
@@ -204,73 +181,39 @@ int upload_tape(mm3e_scene* s, const LoweredScene& low, unsigned char** dst, siz
     return MM3E_OK;
 }
 
-// Samples of one beauty frame: 8x4 pixel tiles (padding included) times aa^2.
-size_t frame_samples(const LoweredScene& low) {
-    size_t tiles = (size_t)((low.width + 7) / 8) * ((low.height + 3) / 4) * 32;
-    return tiles * low.aa * low.aa;
-}
-
-int ensure_wave(mm3e_ctx* c, WaveStore& w, size_t cap, size_t lights, size_t levels) {
-    if (cap <= w.cap && lights <= w.lights && levels <= w.levels) return MM3E_OK;
-    w.release();
-    cap = cap ? cap : 1;
-    cudaError_t e = cudaSuccess;
-    bool ok = (w.qa_o = dmalloc<float4>(cap, e)) && (w.qa_d = dmalloc<float4>(cap, e)) &&
-              (w.qb_o = dmalloc<float4>(cap, e)) && (w.qb_d = dmalloc<float4>(cap, e)) &&
-              (w.h_n = dmalloc<float4>(cap, e)) && (w.h_m = dmalloc<uint2>(cap, e)) &&
-              (w.occ = dmalloc<float>(cap, e)) && (w.shadow = dmalloc<float>(cap * (lights ? lights : 1), e)) &&
-              (w.lvl = dmalloc<float4>(cap * 2 * (levels ? levels : 1), e)) && (w.term = dmalloc<float4>(cap, e));
-    if (!ok) {
-        w.release();
-        return cuda_fail(c, e, "ray queue allocation");
-    }
-    w.cap = cap;
-    w.lights = lights;
-    w.levels = levels;
-    return MM3E_OK;
-}
-
+// Frame buffers of the scene for the context's tile shape.
 int ensure_frame_buffers(mm3e_scene* s) {
     mm3e_ctx* c = s->ctx;
     cudaError_t e;
-    if (!s->d_counters) {
-        s->d_counters = dmalloc<uint32_t>(64, e);
-        if (!s->d_counters) return cuda_fail(c, e, "counter allocation");
-    }
+    uint32_t wlog = c->tune.tile_wlog;
     size_t n = (size_t)s->low.width * s->low.height;
-    if (n != s->pixels || (n && !s->d_hdr)) {
-        cudaFree(s->d_hdr);
-        cudaFree(s->d_bright);
-        cudaFree(s->d_blur);
+    size_t samples = slots_of(s->low.width, s->low.height, wlog) * s->low.aa * s->low.aa;
+    if (n != s->pixels || (n && !s->d_out)) {
         cudaFree(s->d_out);
         if (s->h_stage) cudaFreeHost(s->h_stage);
-        s->d_hdr = s->d_bright = s->d_blur = s->d_out = nullptr;
+        s->d_out = nullptr;
         s->h_stage = nullptr;
         s->pixels = n;
         if (n) {
-            s->d_hdr = dmalloc<float4>(n, e);
-            if (!s->d_hdr) return cuda_fail(c, e, "frame buffer allocation");
-            s->d_bright = dmalloc<float4>(n, e);
-            if (!s->d_bright) return cuda_fail(c, e, "frame buffer allocation");
-            s->d_blur = dmalloc<float4>(n, e);
-            if (!s->d_blur) return cuda_fail(c, e, "frame buffer allocation");
-            s->d_out = dmalloc<float4>(n, e);
-            if (!s->d_out) return cuda_fail(c, e, "frame buffer allocation");
+            e = cudaMalloc(reinterpret_cast<void**>(&s->d_out), n * sizeof(float4));
+            if (e != cudaSuccess) return cuda_fail(c, e, "frame buffer allocation");
             e = cudaMallocHost(&s->h_stage, n * sizeof(float4));
             if (e != cudaSuccess) return cuda_fail(c, e, "pinned staging allocation");
         }
     }
-    size_t lights = s->low.blob.empty() ? 0 : reinterpret_cast<const TapeHeader*>(s->low.blob.data())->n_lights;
-    return ensure_wave(c, s->wave, n ? frame_samples(s->low) : 0, lights, s->low.bounces);
+    e = s->buf.ensure(samples ? samples : 1, s->n_lights(), s->low.bounces + 1, n ? n : 1);
+    if (e != cudaSuccess) return cuda_fail(c, e, "pass buffer allocation");
+    s->buf_wlog = wlog;
+    return MM3E_OK;
 }
 
 int upload_post_kernel(mm3e_scene* s) {
     uint32_t r = s->src.d.post.bloom_radius;
     std::vector<float> k = gaussian_kernel(r);
     cudaFree(s->d_kernel);
-    cudaError_t e;
-    s->d_kernel = dmalloc<float>(k.size(), e);
-    if (!s->d_kernel) return cuda_fail(s->ctx, e, "bloom kernel allocation");
+    s->d_kernel = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&s->d_kernel), k.size() * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(s->ctx, e, "bloom kernel allocation");
     e = cudaMemcpy(s->d_kernel, k.data(), k.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(s->ctx, e, "bloom kernel upload");
     s->bloom_radius = (uint32_t)(k.size() / 2);
@@ -291,18 +234,9 @@ int relower(mm3e_scene* s) {
     return upload_post_kernel(s);
 }
 
-void fill_camera(CameraArgs& a, const mm3e_camera& c) {
-    std::memcpy(a.eye, c.eye, 12);
-    std::memcpy(a.fwd, c.forward, 12);
-    std::memcpy(a.right, c.right, 12);
-    std::memcpy(a.up, c.up, 12);
-    a.fov_scale = c.fov_scale;
-}
-
-int check_status(mm3e_scene* s) {
-    mm3e_ctx* c = s->ctx;
+int check_status(mm3e_ctx* c, const uint32_t* d_status) {
     uint32_t st = 0;
-    cudaError_t e = cudaMemcpyAsync(&st, s->d_counters + 63, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaMemcpyAsync(&st, d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "render");
     if (st & ST_TAPE_TIMEOUT) return fail(c, MM3E_ERR_TIMEOUT, "scene tape staging wait gave up");
@@ -310,25 +244,7 @@ int check_status(mm3e_scene* s) {
     return MM3E_OK;
 }
 
-WaveArgs base_args(mm3e_scene* s, const unsigned char* tape, uint32_t tape_bytes) {
-    WaveArgs a{};
-    a.tape = tape;
-    a.tape_bytes = tape_bytes;
-    a.status = s->d_counters + 63;
-    WaveStore& w = s->wave;
-    a.b.q_o = w.qa_o;
-    a.b.q_d = w.qa_d;
-    a.b.h_n = w.h_n;
-    a.b.h_m = w.h_m;
-    a.b.occ = w.occ;
-    a.b.shadow = w.shadow;
-    a.b.nq_o = w.qb_o;
-    a.b.nq_d = w.qb_d;
-    a.b.lvl = w.lvl;
-    a.b.term = w.term;
-    a.b.hdr = s->d_hdr;
-    return a;
-}
+int check_status(mm3e_scene* s) { return check_status(s->ctx, s->buf.counters + (N_COUNTERS - 1)); }
 
 #define CK(x)                                                   \
     do {                                                        \
@@ -336,64 +252,65 @@ WaveArgs base_args(mm3e_scene* s, const unsigned char* tape, uint32_t tape_bytes
         if (e_ != cudaSuccess) return cuda_fail(c, e_, #x);     \
     } while (0)
 
-// Beauty radiance of one frame into s->d_hdr: march / ao / shadow / shade per reflection
-// level, then resolve (lib.rs:908-947, 1223-1360).
-int render_beauty(mm3e_scene* s, const mm3e_camera* cam, const unsigned char* tape, uint32_t tape_bytes,
-                  uint32_t* launches) {
-    mm3e_ctx* c = s->ctx;
+// Single-job plan of one beauty frame of `s`.
+PassPlan scene_plan(mm3e_scene* s, const unsigned char* tape, uint32_t tape_bytes, const mm3e_camera& cam,
+                    uint32_t format, void* dout) {
     const TapeHeader* h = reinterpret_cast<const TapeHeader*>(s->low.blob.data());
-    uint32_t n = (uint32_t)frame_samples(s->low);
-    CK(cudaMemsetAsync(s->d_counters, 0, 64 * sizeof(uint32_t), c->stream));
-    WaveArgs a = base_args(s, tape, tape_bytes);
-    fill_camera(a.cam, *cam);
-    a.n_samples = n;
-    bool ao = (h->flags & SF_AO) && h->ao_samples > 0;
-    bool shadows = (h->flags & SF_SHADOWS) && h->shadow_steps > 0 && h->n_lights > 0;
-    for (uint32_t level = 0; level <= s->low.bounces; ++level) {
-        a.level = level;
-        a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
-        a.n_items = n;
-        a.n_items_dev = level == 0 ? nullptr : s->d_counters + 4 * (level - 1) + 2;
-        a.b.nq_count = s->d_counters + 4 * level + 2;
-        a.counter = s->d_counters + 4 * level;
-        CK(launch_march(a, c->stream, c->sm_count, launches));
-        if (ao) CK(launch_ao(a, c->stream, launches));
-        if (shadows) {
-            a.counter = s->d_counters + 4 * level + 1;
-            CK(launch_shadow(a, c->stream, c->sm_count, launches));
-        }
-        CK(launch_shade(a, c->stream, launches));
-        std::swap(a.b.q_o, a.b.nq_o);
-        std::swap(a.b.q_d, a.b.nq_d);
-    }
-    CK(launch_resolve(a, s->low.width, s->low.height, c->stream, launches));
-    return MM3E_OK;
+    PassPlan p;
+    p.job0 = scene_job(s, tape, cam, 0, 0, s->buf_wlog);
+    p.job0.format = format;
+    p.job0.out = dout;
+    p.tape_bytes = tape_bytes;
+    p.n_samples = p.job0.n_samples;
+    p.n_slots = p.job0.n_slots;
+    p.n_pixels = p.job0.n_pixels;
+    p.levels = s->low.bounces + 1;
+    p.lights_max = h->n_lights;
+    p.ao = (h->flags & SF_AO) && h->ao_samples > 0;
+    p.shadows = (h->flags & SF_SHADOWS) && h->shadow_steps > 0 && h->n_lights > 0;
+    p.bloom = (p.job0.flags & JF_BLOOM) != 0;
+    return p;
 }
 
-// Pixel-centre march (AOV / hits): hit records in the wave store, row-major slots.
+// Pixel-centre march of job 0 (AOV / hits): hit records in the pass buffers, row-major slots.
 int march_centers(mm3e_scene* s, const mm3e_camera* cam, const unsigned char* tape, uint32_t tape_bytes,
-                  bool want_ao, uint32_t* launches, WaveArgs& a) {
+                  bool want_ao, LaunchLog* log, WaveArgs& a) {
     mm3e_ctx* c = s->ctx;
     uint32_t n = s->low.width * s->low.height;
-    CK(cudaMemsetAsync(s->d_counters, 0, 64 * sizeof(uint32_t), c->stream));
-    a = base_args(s, tape, tape_bytes);
-    fill_camera(a.cam, *cam);
+    CK(cudaMemsetAsync(s->buf.counters, 0, N_COUNTERS * sizeof(uint32_t), c->stream));
+    a = WaveArgs{};
+    a.job0 = scene_job(s, tape, *cam, 0, 0, s->buf_wlog);
+    a.tape_bytes = tape_bytes;
+    a.cap = (uint32_t)s->buf.cap;
+    a.lights_max = s->n_lights();
+    a.tile_wlog = s->buf_wlog;
+    a.grid_cap = (uint32_t)c->sm_count * 16u;
+    a.status = s->buf.counters + (N_COUNTERS - 1);
+    a.b.q_o = s->buf.qa_o;
+    a.b.q_d = s->buf.qa_d;
+    a.b.h_n = s->buf.h_n;
+    a.b.h_m = s->buf.h_m;
+    a.b.occ = s->buf.occ;
     a.src = SRC_CENTER;
     a.n_items = n;
-    a.n_samples = n;
-    a.counter = s->d_counters;
-    CK(launch_march(a, c->stream, c->sm_count, launches));
-    if (want_ao) CK(launch_ao(a, c->stream, launches));
+    a.counter = s->buf.counters;
+    CK(launch_march(a, c->tune, c->stream, c->sm_count, log));
+    if (want_ao) CK(launch_ao(a, c->stream, log));
     return MM3E_OK;
 }
 
 // Render into device memory `dout` (w*h float4 or uchar4). Asynchronous on the ctx stream.
+// linear_only: beauty radiance into s->buf.hdr only (no post).
 int render_to_device(mm3e_scene* s, const mm3e_camera* cam, const mm3e_dyn_sphere* dyn, size_t n_dyn, uint32_t format,
-                     void* dout, bool linear_only, uint32_t* launches) {
+                     void* dout, bool linear_only, LaunchLog* log) {
     mm3e_ctx* c = s->ctx;
     const unsigned char* tape = s->d_tape;
     uint32_t tape_bytes = (uint32_t)s->low.blob.size();
     uint32_t mode = s->low.mode;
+    if (s->buf_wlog != c->tune.tile_wlog) {
+        int rc = ensure_frame_buffers(s);
+        if (rc) return rc;
+    }
     if (n_dyn > 0) {
         std::string err;
         LoweredScene low;
@@ -407,37 +324,28 @@ int render_to_device(mm3e_scene* s, const mm3e_camera* cam, const mm3e_dyn_spher
     uint32_t w = s->low.width, h = s->low.height;
     if ((size_t)w * h == 0) return MM3E_OK;
     if (mode == MM3E_MODE_BEAUTY || linear_only) {
-        int rc = render_beauty(s, cam, tape, tape_bytes, launches);
-        if (rc) return rc;
-        if (linear_only) return MM3E_OK;
-        PostArgs p{};
-        p.hdr = s->d_hdr;
-        p.bright = s->d_bright;
-        p.blur_h = s->d_blur;
-        p.kernel_w = s->d_kernel;
-        p.radius = s->bloom_radius;
-        p.width = w;
-        p.height = h;
-        const mm3e_post& post = s->src.d.post;
-        p.bloom = post.bloom && post.bloom_intensity > 0.0f;
-        p.threshold = post.bloom_threshold;
-        p.intensity = post.bloom_intensity;
-        p.exposure = post.exposure;
-        p.format = (int)format;
-        p.out = dout;
-        CK(launch_post(p, c->stream, launches));
+        PassPlan p = scene_plan(s, tape, tape_bytes, *cam, format, dout);
+        if (n_dyn > 0) {  // dynamic spheres add no lights; AO / shadow flags are the scene's
+            p.job0.n_lights = p.lights_max;
+        }
+        p.post = !linear_only;
+        CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, log));
         return MM3E_OK;
     }
     const TapeHeader* th = reinterpret_cast<const TapeHeader*>(s->low.blob.data());
     WaveArgs a;
-    int rc = march_centers(s, cam, tape, tape_bytes, mode == MM3E_MODE_AO && th->ao_samples > 0, launches, a);
+    int rc = march_centers(s, cam, tape, tape_bytes, mode == MM3E_MODE_AO && th->ao_samples > 0, log, a);
     if (rc) return rc;
     a.aov_mode = mode;
-    float4* out = format == MM3E_FB_RGBA_F32 ? static_cast<float4*>(dout) : s->d_hdr;
-    CK(launch_aov(a, w, h, out, c->stream, launches));
-    if (format == MM3E_FB_RGBA8) CK(launch_pack_rgba8(s->d_hdr, static_cast<uchar4*>(dout), (size_t)w * h, c->stream, launches));
+    float4* out = format == MM3E_FB_RGBA_F32 ? static_cast<float4*>(dout) : s->buf.hdr;
+    CK(launch_aov(a, out, c->stream, log));
+    if (format == MM3E_FB_RGBA8) CK(launch_pack_rgba8(s->buf.hdr, static_cast<uchar4*>(dout), (size_t)w * h, c->stream, log));
     return MM3E_OK;
 }
+
+}  // namespace
+
+namespace {
 
 bool finite3(const float* a) { return std::isfinite(a[0]) && std::isfinite(a[1]) && std::isfinite(a[2]); }
 
@@ -595,7 +503,6 @@ int mm3e_ctx_create(int device, mm3e_ctx** out) {
     cudaEventCreate(&c->ev1);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&c->clock_khz, cudaDevAttrClockRate, device);
-    if ((e = cudaMalloc(&c->d_counter, 4 * sizeof(uint32_t))) != cudaSuccess) return MM3E_ERR_NO_MEMORY;
     *out = c.release();
     return MM3E_OK;
 }
@@ -604,10 +511,10 @@ void mm3e_ctx_destroy(mm3e_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->batch.reset();
     std::set<mm3e_scene*> live;
     live.swap(ctx->scenes);
     for (mm3e_scene* s : live) delete s;  // scenes left alive by the caller
-    cudaFree(ctx->d_counter);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -637,6 +544,57 @@ int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz) {
     return MM3E_OK;
 }
 
+int mm3e_ctx_set_tuning(mm3e_ctx* ctx, const mm3e_tuning* t) {
+    if (!ctx || !t) return MM3E_ERR_INVALID;
+    if (t->block != 128 && t->block != 256) return fail(ctx, MM3E_ERR_INVALID, "block must be 128 or 256");
+    if (t->tile_wlog > 5) return fail(ctx, MM3E_ERR_INVALID, "tile_wlog must be 0..5");
+    if (t->unroll != 1 && t->unroll != 2) return fail(ctx, MM3E_ERR_INVALID, "unroll must be 1 or 2");
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);  // frames in flight keep their buffers
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "set tuning");
+    ctx->tune.block = t->block;
+    ctx->tune.tile_wlog = t->tile_wlog;
+    ctx->tune.unroll = t->unroll;
+    return MM3E_OK;
+}
+
+int mm3e_ctx_get_tuning(mm3e_ctx* ctx, mm3e_tuning* t) {
+    if (!ctx || !t) return MM3E_ERR_INVALID;
+    t->block = ctx->tune.block;
+    t->tile_wlog = ctx->tune.tile_wlog;
+    t->unroll = ctx->tune.unroll;
+    return MM3E_OK;
+}
+
+int mm3e_ctx_set_profiling(mm3e_ctx* ctx, int enable) {
+    if (!ctx) return MM3E_ERR_INVALID;
+    ctx->prof.on = enable != 0;
+    return MM3E_OK;
+}
+
+int mm3e_ctx_kernel_times(mm3e_ctx* ctx, mm3e_kernel_time* out, uint32_t cap, uint32_t* n_out) {
+    if (!ctx) return MM3E_ERR_INVALID;
+    static const char* names[KK_COUNT] = {"march", "ao", "shadow", "shade", "resolve", "post", "aov", "gi", "other"};
+    cudaError_t e = ctx->prof.collect(ctx->kk_ms, ctx->kk_launches);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel times");
+    uint32_t n = 0;
+    for (uint32_t k = 0; k < KK_COUNT; ++k) {
+        if (!ctx->kk_launches[k]) continue;
+        if (out && n < cap) {
+            std::memset(&out[n], 0, sizeof(out[n]));
+            std::strncpy(out[n].name, names[k], sizeof(out[n].name) - 1);
+            out[n].launches = ctx->kk_launches[k];
+            out[n].ms = ctx->kk_ms[k];
+        }
+        ++n;
+    }
+    for (uint32_t k = 0; k < KK_COUNT; ++k) {
+        ctx->kk_ms[k] = 0.0;
+        ctx->kk_launches[k] = 0;
+    }
+    if (n_out) *n_out = n;
+    return MM3E_OK;
+}
+
 int mm3e_scene_compile(mm3e_ctx* ctx, const mm3e_scene_desc* desc, mm3e_scene** out) {
     if (!ctx || !desc || !out) return fail(ctx, MM3E_ERR_INVALID, "null argument");
     *out = nullptr;
@@ -663,6 +621,12 @@ void mm3e_scene_destroy(mm3e_scene* scene) {
     delete scene;
 }
 
+int mm3e_scene_device_bytes(mm3e_scene* scene, size_t* out_bytes) {
+    if (!scene || !out_bytes) return MM3E_ERR_INVALID;
+    *out_bytes = scene->device_bytes();
+    return MM3E_OK;
+}
+
 int mm3e_render(mm3e_scene* s, const mm3e_camera* camera, const mm3e_dyn_sphere* dyn, size_t n_dyn, uint32_t format,
                 void* host_out, size_t out_bytes, mm3e_render_stats* stats) {
     if (!s || !camera) return MM3E_ERR_INVALID;
@@ -677,12 +641,10 @@ int mm3e_render(mm3e_scene* s, const mm3e_camera* camera, const mm3e_dyn_sphere*
     int rc = validate_dynamic(s->src.d, dyn, n_dyn, err);
     if (rc) return fail(c, rc, err);
     cudaSetDevice(c->device);
-    uint32_t launches = 0;
+    LaunchLog log = c->prof.log();
     cudaEventRecord(c->ev0, c->stream);
-    rc = render_to_device(s, camera, dyn, n_dyn, format, s->d_out == nullptr ? nullptr : (void*)s->d_out, false,
-                          &launches);
+    rc = render_to_device(s, camera, dyn, n_dyn, format, (void*)s->d_out, false, &log);
     if (rc) return rc;
-    // AOV RGBA f32 writes straight into d_out; beauty post writes into d_out too.
     cudaEventRecord(c->ev1, c->stream);
     if (n) {
         cudaError_t e = cudaMemcpyAsync(s->h_stage, s->d_out, n * px, cudaMemcpyDeviceToHost, c->stream);
@@ -698,7 +660,7 @@ int mm3e_render(mm3e_scene* s, const mm3e_camera* camera, const mm3e_dyn_sphere*
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->h2d_bytes = 0;
         stats->d2h_bytes = n * px;
-        stats->kernel_launches = launches;
+        stats->kernel_launches = log.launches;
     }
     return MM3E_OK;
 }
@@ -709,11 +671,11 @@ int mm3e_render_linear(mm3e_scene* s, const mm3e_camera* camera, float* host_rgb
     size_t n = (size_t)s->low.width * s->low.height;
     if (n && (!host_rgb || n_floats < 3 * n)) return fail(c, MM3E_ERR_INVALID, "output buffer too small");
     cudaSetDevice(c->device);
-    uint32_t launches = 0;
-    int rc = render_to_device(s, camera, nullptr, 0, MM3E_FB_RGBA_F32, nullptr, true, &launches);
+    LaunchLog log = c->prof.log();
+    int rc = render_to_device(s, camera, nullptr, 0, MM3E_FB_RGBA_F32, nullptr, true, &log);
     if (rc) return rc;
     if (n) {
-        cudaError_t e = cudaMemcpyAsync(s->h_stage, s->d_hdr, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
+        cudaError_t e = cudaMemcpyAsync(s->h_stage, s->buf.hdr, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "HDR download");
     }
     rc = check_status(s);
@@ -735,15 +697,20 @@ int mm3e_render_device(mm3e_scene* s, const mm3e_camera* camera, uint32_t format
     size_t px = format == MM3E_FB_RGBA8 ? 4 : 16;
     if (n && (!device_out || out_bytes < n * px)) return fail(c, MM3E_ERR_INVALID, "output buffer too small");
     cudaSetDevice(c->device);
+    LaunchLog log = c->prof.log();
     if (format == MM3E_FB_LINEAR_F32) {
         if (s->low.mode != MM3E_MODE_BEAUTY) return fail(c, MM3E_ERR_INVALID, "linear output needs beauty mode");
-        float4* keep = s->d_hdr;
-        s->d_hdr = static_cast<float4*>(device_out);
-        int rc = render_to_device(s, camera, nullptr, 0, format, device_out, true, nullptr);
-        s->d_hdr = keep;
+        if (s->buf_wlog != c->tune.tile_wlog) {
+            int rc = ensure_frame_buffers(s);
+            if (rc) return rc;
+        }
+        float4* keep = s->buf.hdr;
+        s->buf.hdr = static_cast<float4*>(device_out);
+        int rc = render_to_device(s, camera, nullptr, 0, format, device_out, true, &log);
+        s->buf.hdr = keep;
         return rc;
     }
-    return render_to_device(s, camera, nullptr, 0, format, device_out, false, nullptr);
+    return render_to_device(s, camera, nullptr, 0, format, device_out, false, &log);
 }
 
 int mm3e_bake_gi(mm3e_scene* s, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t samples) {
@@ -756,32 +723,34 @@ int mm3e_bake_gi(mm3e_scene* s, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t 
     uint64_t items = probes * 6 * g.dirs_per_face;
     if (items >= 0x7FFFFFFFull) return fail(c, MM3E_ERR_INVALID, "GI probe grid too large");
     cudaError_t e = cudaSuccess;
-    WaveStore w;
-    int rc = ensure_wave(c, w, items, 0, 0);
-    if (rc) return rc;
-    float4* d_dirs = dmalloc<float4>(g.dirs.size() / 4, e);
-    float4* d_rad = d_dirs ? dmalloc<float4>(items, e) : nullptr;
-    float4* d_cubes = d_rad ? dmalloc<float4>(probes * 6, e) : nullptr;
+    PassBuffers w;
+    e = w.ensure(items, 0, 1, 1);
+    if (e != cudaSuccess) return cuda_fail(c, e, "GI bake allocation");
+    float4 *d_dirs = nullptr, *d_rad = nullptr, *d_cubes = nullptr;
+    e = cudaMalloc(reinterpret_cast<void**>(&d_dirs), g.dirs.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_rad), items * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_cubes), probes * 6 * sizeof(float4));
     auto cleanup = [&]() {
         cudaFree(d_dirs);
         cudaFree(d_rad);
         cudaFree(d_cubes);
         w.release();
     };
-    if (!d_cubes) {
+    if (e != cudaSuccess) {
         cleanup();
         return cuda_fail(c, e, "GI bake allocation");
     }
     std::vector<float> cubes4(probes * 24);
     e = cudaMemcpyAsync(d_dirs, g.dirs.data(), g.dirs.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counters, 0, 64 * sizeof(uint32_t), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, N_COUNTERS * sizeof(uint32_t), c->stream);
     WaveArgs a{};
-    a.tape = s->d_tape;
+    a.job0.tape = s->d_tape;
     a.tape_bytes = (uint32_t)s->low.blob.size();
-    a.status = s->d_counters + 63;
-    a.counter = s->d_counters;
+    a.status = w.counters + (N_COUNTERS - 1);
+    a.counter = w.counters;
     a.src = SRC_GATHER;
     a.n_items = (uint32_t)items;
+    a.cap = (uint32_t)items;
     a.b.q_o = w.qa_o;
     a.b.q_d = w.qa_d;
     a.b.h_n = w.h_n;
@@ -793,12 +762,13 @@ int mm3e_bake_gi(mm3e_scene* s, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t 
     a.gi_nz = g.nz;
     a.dirs_per_face = g.dirs_per_face;
     a.gather_dirs = d_dirs;
-    if (e == cudaSuccess) e = launch_march(a, c->stream, c->sm_count, nullptr);
-    if (e == cudaSuccess) e = launch_gather_shade(a, d_rad, c->stream, nullptr);
-    if (e == cudaSuccess) e = launch_gi_reduce(d_rad, d_dirs, g.dirs_per_face, (uint32_t)probes, d_cubes, c->stream, nullptr);
+    LaunchLog log = c->prof.log();
+    if (e == cudaSuccess) e = launch_march(a, c->tune, c->stream, c->sm_count, &log);
+    if (e == cudaSuccess) e = launch_gather_shade(a, d_rad, c->stream, &log);
+    if (e == cudaSuccess) e = launch_gi_reduce(d_rad, d_dirs, g.dirs_per_face, (uint32_t)probes, d_cubes, c->stream, &log);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(cubes4.data(), d_cubes, cubes4.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
-    rc = e == cudaSuccess ? check_status(s) : cuda_fail(c, e, "GI bake");
+    int rc = e == cudaSuccess ? check_status(c, w.counters + (N_COUNTERS - 1)) : cuda_fail(c, e, "GI bake");
     cleanup();
     if (rc) return rc;
     SceneCopy& sc = s->src;
@@ -834,16 +804,17 @@ int mm3e_scene_get_gi(mm3e_scene* s, float min[3], float size[3], uint32_t dims[
     return MM3E_OK;
 }
 
+}  // extern "C"
+
 // Copy hit records (normal xyz + t, material/NIL + steps) out and split them.
-static int download_hits(mm3e_scene* s, const WaveStore& w, size_t n, float* t, uint32_t* mat, uint32_t* steps,
+static int download_hits(mm3e_ctx* c, const PassBuffers& w, size_t n, float* t, uint32_t* mat, uint32_t* steps,
                          float* normal3) {
-    mm3e_ctx* c = s->ctx;
     std::vector<float4> hn(n);
     std::vector<uint2> hm(n);
     cudaError_t e = cudaMemcpyAsync(hn.data(), w.h_n, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hm.data(), w.h_m, n * sizeof(uint2), cudaMemcpyDeviceToHost, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "hits download");
-    int rc = check_status(s);
+    int rc = check_status(c, w.counters + (N_COUNTERS - 1));
     if (rc) return rc;
     for (size_t i = 0; i < n; ++i) {
         t[i] = hn[i].w;
@@ -858,6 +829,8 @@ static int download_hits(mm3e_scene* s, const WaveStore& w, size_t n, float* t, 
     return MM3E_OK;
 }
 
+extern "C" {
+
 int mm3e_render_hits(mm3e_scene* s, const mm3e_camera* camera, float* t, uint32_t* mat, uint32_t* steps,
                      float* normal3) {
     if (!s || !camera || !t || !mat) return MM3E_ERR_INVALID;
@@ -866,9 +839,10 @@ int mm3e_render_hits(mm3e_scene* s, const mm3e_camera* camera, float* t, uint32_
     size_t n = (size_t)s->low.width * s->low.height;
     if (n == 0) return MM3E_OK;
     WaveArgs a;
-    int rc = march_centers(s, camera, s->d_tape, (uint32_t)s->low.blob.size(), false, nullptr, a);
+    LaunchLog log = c->prof.log();
+    int rc = march_centers(s, camera, s->d_tape, (uint32_t)s->low.blob.size(), false, &log, a);
     if (rc) return rc;
-    return download_hits(s, s->wave, n, t, mat, steps, normal3);
+    return download_hits(c, s->buf, n, t, mat, steps, normal3);
 }
 
 int mm3e_march_rays(mm3e_scene* s, const float* rays6, size_t n, float* t, uint32_t* mat, uint32_t* steps) {
@@ -877,30 +851,32 @@ int mm3e_march_rays(mm3e_scene* s, const float* rays6, size_t n, float* t, uint3
     if (n >= 0x7FFFFFFFull) return fail(c, MM3E_ERR_INVALID, "too many rays");
     if (n == 0) return MM3E_OK;
     cudaSetDevice(c->device);
-    WaveStore w;
-    int rc = ensure_wave(c, w, n, 0, 0);
-    if (rc) return rc;
+    PassBuffers w;
+    cudaError_t e = w.ensure(n, 0, 1, 1);
+    if (e != cudaSuccess) return cuda_fail(c, e, "ray buffer allocation");
     std::vector<float4> o(n), d(n);
     for (size_t i = 0; i < n; ++i) {
         o[i] = make_float4(rays6[6 * i], rays6[6 * i + 1], rays6[6 * i + 2], 0.0f);
         d[i] = make_float4(rays6[6 * i + 3], rays6[6 * i + 4], rays6[6 * i + 5], 0.0f);
     }
-    cudaError_t e = cudaMemcpyAsync(w.qa_o, o.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream);
+    e = cudaMemcpyAsync(w.qa_o, o.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(w.qa_d, d.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counters, 0, 64 * sizeof(uint32_t), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.counters, 0, N_COUNTERS * sizeof(uint32_t), c->stream);
     WaveArgs a{};
-    a.tape = s->d_tape;
+    a.job0.tape = s->d_tape;
     a.tape_bytes = (uint32_t)s->low.blob.size();
-    a.status = s->d_counters + 63;
-    a.counter = s->d_counters;
+    a.status = w.counters + (N_COUNTERS - 1);
+    a.counter = w.counters;
     a.src = SRC_QUEUE;
     a.n_items = (uint32_t)n;
+    a.cap = (uint32_t)n;
     a.b.q_o = w.qa_o;
     a.b.q_d = w.qa_d;
     a.b.h_n = w.h_n;
     a.b.h_m = w.h_m;
-    if (e == cudaSuccess) e = launch_march(a, c->stream, c->sm_count, nullptr);
-    rc = e == cudaSuccess ? download_hits(s, w, n, t, mat, steps, nullptr) : cuda_fail(c, e, "march rays");
+    LaunchLog log = c->prof.log();
+    if (e == cudaSuccess) e = launch_march(a, c->tune, c->stream, c->sm_count, &log);
+    int rc = e == cudaSuccess ? download_hits(c, w, n, t, mat, steps, nullptr) : cuda_fail(c, e, "march rays");
     w.release();
     return rc;
 }
@@ -911,17 +887,20 @@ int mm3e_field(mm3e_scene* s, const float* points3, size_t n, float* dist, uint3
     if (n == 0) return MM3E_OK;
     if (n >= 0xFFFFFFFFull) return fail(c, MM3E_ERR_INVALID, "too many points");
     cudaSetDevice(c->device);
-    cudaError_t e;
-    float* d_p = dmalloc<float>(3 * n, e);
-    float* d_d = d_p ? dmalloc<float>(n, e) : nullptr;
-    uint32_t* d_m = d_d ? dmalloc<uint32_t>(n, e) : nullptr;
-    if (!d_m) {
+    float *d_p = nullptr, *d_d = nullptr;
+    uint32_t* d_m = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&d_p), 12 * n);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_d), 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_m), 4 * n);
+    if (e != cudaSuccess) {
         cudaFree(d_p);
         cudaFree(d_d);
+        cudaFree(d_m);
         return cuda_fail(c, e, "field allocation");
     }
-    cudaMemcpyAsync(d_p, points3, 12 * n, cudaMemcpyHostToDevice, c->stream);
-    e = launch_field(s->d_tape, (uint32_t)s->low.blob.size(), d_p, (uint32_t)n, d_d, d_m, c->stream, nullptr);
+    LaunchLog log = c->prof.log();
+    e = cudaMemcpyAsync(d_p, points3, 12 * n, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_field(s->d_tape, d_p, (uint32_t)n, d_d, d_m, c->stream, &log);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dist, d_d, 4 * n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(mat, d_m, 4 * n, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

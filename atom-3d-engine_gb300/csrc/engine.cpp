@@ -1,0 +1,195 @@
+// engine.cpp — pass-sequence driver, pass buffers and the kernel-time profiler.
+#include "engine.h"
+
+#include <utility>
+
+namespace mm3e {
+
+namespace {
+template <class T> cudaError_t grow(T** p, size_t n) {
+    return cudaMalloc(reinterpret_cast<void**>(p), (n ? n : 1) * sizeof(T) + 16);
+}
+}  // namespace
+
+void PassBuffers::release() {
+    void* ps[] = {qa_o, qa_d, qb_o, qb_d, h_n, h_m, occ, shadow, lvl, term, hdr, bright, blur, counters};
+    for (void* p : ps) cudaFree(p);
+    *this = PassBuffers();
+}
+
+size_t PassBuffers::bytes_for(size_t cap, size_t lights, size_t levels, size_t pixels) {
+    size_t l = lights ? lights : 1, v = levels ? levels : 1;
+    return cap * (5 * sizeof(float4) + sizeof(uint2) + sizeof(float) + l * sizeof(float) + 2 * v * sizeof(float4) +
+                  sizeof(float4)) +
+           pixels * 3 * sizeof(float4) + N_COUNTERS * sizeof(uint32_t);
+}
+
+size_t PassBuffers::bytes() const { return cap ? bytes_for(cap, lights, levels, pixels) : 0; }
+
+cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need_levels, size_t need_pixels) {
+    if (counters && need_cap <= cap && need_lights <= lights && need_levels <= levels && need_pixels <= pixels)
+        return cudaSuccess;
+    size_t c = need_cap > cap ? need_cap : cap;
+    size_t l = need_lights > lights ? need_lights : lights;
+    size_t v = need_levels > levels ? need_levels : levels;
+    size_t px = need_pixels > pixels ? need_pixels : pixels;
+    release();
+    c = c ? c : 1;
+    cudaError_t e;
+    if ((e = grow(&qa_o, c)) || (e = grow(&qa_d, c)) || (e = grow(&qb_o, c)) || (e = grow(&qb_d, c)) ||
+        (e = grow(&h_n, c)) || (e = grow(&h_m, c)) || (e = grow(&occ, c)) || (e = grow(&shadow, c * (l ? l : 1))) ||
+        (e = grow(&lvl, c * 2 * (v ? v : 1))) || (e = grow(&term, c)) || (e = grow(&hdr, px)) ||
+        (e = grow(&bright, px)) || (e = grow(&blur, px)) || (e = grow(&counters, (size_t)N_COUNTERS))) {
+        release();
+        return e;
+    }
+    if ((e = cudaMemset(counters, 0, N_COUNTERS * sizeof(uint32_t))) != cudaSuccess) {
+        release();
+        return e;
+    }
+    cap = c;
+    lights = l;
+    levels = v;
+    pixels = px;
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------------------
+Profiler::~Profiler() {
+    for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+}
+
+cudaEvent_t Profiler::event() {
+    if (used_ == pool_.size()) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        pool_.push_back(e);
+    }
+    return pool_[used_++];
+}
+
+void Profiler::begin(uint32_t kind, cudaStream_t s) {
+    (void)kind;
+    cudaEvent_t e = event();
+    if (e) cudaEventRecord(e, s);
+    open_.push_back(e);
+}
+
+void Profiler::end(uint32_t kind, cudaStream_t s) {
+    if (open_.empty()) return;
+    cudaEvent_t a = open_.back();
+    open_.pop_back();
+    cudaEvent_t b = event();
+    if (!a || !b) return;
+    cudaEventRecord(b, s);
+    recs_.push_back(Rec{kind, a, b});
+}
+
+cudaError_t Profiler::collect(double* ms, uint32_t* launches) {
+    cudaError_t err = cudaSuccess;
+    for (const Rec& r : recs_) {
+        cudaError_t e = cudaEventSynchronize(r.b);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.a, r.b);
+        if (e != cudaSuccess) {
+            err = e;
+            continue;
+        }
+        if (r.kind < KK_COUNT) {
+            ms[r.kind] += t;
+            launches[r.kind] += 1;
+        }
+    }
+    recs_.clear();
+    open_.clear();
+    used_ = 0;
+    return err;
+}
+
+namespace {
+void prof_begin(void* p, uint32_t k, cudaStream_t s) { static_cast<Profiler*>(p)->begin(k, s); }
+void prof_end(void* p, uint32_t k, cudaStream_t s) { static_cast<Profiler*>(p)->end(k, s); }
+}  // namespace
+
+LaunchLog Profiler::log() {
+    LaunchLog l;
+    if (on) {
+        l.recorder = this;
+        l.begin = prof_begin;
+        l.end = prof_end;
+    }
+    return l;
+}
+
+// ---------------------------------------------------------------------------------------
+namespace {
+WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tune, int sm_count) {
+    WaveArgs a{};
+    a.job0 = plan.job0;
+    a.jobs = plan.jobs;
+    a.totals = plan.totals;
+    a.n_jobs = 1;
+    a.tape_bytes = plan.tape_bytes;
+    a.cap = (uint32_t)buf.cap;
+    a.lights_max = plan.lights_max;
+    a.tile_wlog = tune.tile_wlog;
+    a.grid_cap = (uint32_t)sm_count * 16u;
+    a.status = buf.counters + (N_COUNTERS - 1);
+    a.b.q_o = buf.qa_o;
+    a.b.q_d = buf.qa_d;
+    a.b.h_n = buf.h_n;
+    a.b.h_m = buf.h_m;
+    a.b.occ = buf.occ;
+    a.b.shadow = buf.shadow;
+    a.b.nq_o = buf.qb_o;
+    a.b.nq_d = buf.qb_d;
+    a.b.lvl = buf.lvl;
+    a.b.term = buf.term;
+    a.b.hdr = buf.hdr;
+    return a;
+}
+}  // namespace
+
+cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams& tune, cudaStream_t s, int sm_count,
+                       LaunchLog* log) {
+    cudaError_t e = cudaMemsetAsync(buf.counters, 0, (N_COUNTERS - (plan.clear_status ? 0 : 1)) * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    WaveArgs a = wave_args(plan, buf, tune, sm_count);
+    for (uint32_t level = 0; level < plan.levels; ++level) {
+        a.level = level;
+        a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
+        a.n_items = plan.n_samples;
+        a.n_items_dev = level == 0 ? (plan.jobs ? &plan.totals->n_samples : nullptr) : buf.counters + 4 * (level - 1) + 2;
+        a.b.nq_count = buf.counters + 4 * level + 2;
+        a.counter = buf.counters + 4 * level;
+        if ((e = launch_march(a, tune, s, sm_count, log)) != cudaSuccess) return e;
+        if (plan.ao && (e = launch_ao(a, s, log)) != cudaSuccess) return e;
+        if (plan.shadows && plan.lights_max > 0) {
+            a.counter = buf.counters + 4 * level + 1;
+            if ((e = launch_shadow(a, tune, s, sm_count, log)) != cudaSuccess) return e;
+        }
+        if ((e = launch_shade(a, s, log)) != cudaSuccess) return e;
+        std::swap(a.b.q_o, a.b.nq_o);
+        std::swap(a.b.q_d, a.b.nq_d);
+    }
+    if ((e = launch_resolve(a, plan.n_slots, s, log)) != cudaSuccess) return e;
+    if (!plan.post) return cudaSuccess;
+    return run_post(plan, buf, s, sm_count, log);
+}
+
+cudaError_t run_post(const PassPlan& plan, PassBuffers& buf, cudaStream_t s, int sm_count, LaunchLog* log) {
+    PostArgs p{};
+    p.job0 = plan.job0;
+    p.jobs = plan.jobs;
+    p.totals = plan.totals;
+    p.n_jobs = 1;
+    p.n_pixels = plan.n_pixels;
+    p.any_bloom = plan.bloom ? 1 : 0;
+    p.grid_cap = (uint32_t)sm_count * 16u;
+    p.hdr = buf.hdr;
+    p.bright = buf.bright;
+    p.blur_h = buf.blur;
+    return launch_post(p, s, log);
+}
+
+}  // namespace mm3e

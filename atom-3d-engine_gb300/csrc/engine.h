@@ -1,0 +1,93 @@
+// engine.h — pass sequences over frame jobs.
+//
+// One driver runs the beauty passes (march / AO / shadow / shade per reflection level, then
+// resolve and post) for a set of frame jobs; the plain per-frame call runs it for one job
+// with host-known sizes, the batched launch and the request server run it for a device job
+// table with device-side sizes (so the same sequence can be captured once in a CUDA graph
+// and replayed for any table that fits its buffers).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "kernels.h"
+
+namespace mm3e {
+
+inline uint32_t tile_w_of(uint32_t wlog) { return 1u << wlog; }
+inline uint32_t tile_h_of(uint32_t wlog) { return 32u >> wlog; }
+inline uint32_t tiles_x_of(uint32_t w, uint32_t wlog) { return (w + tile_w_of(wlog) - 1) / tile_w_of(wlog); }
+// Pixel slots of a w x h frame in 32-pixel tiles (padding included).
+inline uint64_t slots_of(uint32_t w, uint32_t h, uint32_t wlog) {
+    return (uint64_t)tiles_x_of(w, wlog) * ((h + tile_h_of(wlog) - 1) / tile_h_of(wlog)) * 32u;
+}
+
+constexpr int N_COUNTERS = 64;  // [4L] march, [4L+1] shadow, [4L+2] next queue length; [63] status
+
+// Device buffers of a pass sequence: ray queues and per-sample records for `cap` samples,
+// HDR / bloom arrays for `pixels` output pixels, and the work counters.
+struct PassBuffers {
+    size_t cap = 0, lights = 0, levels = 0, pixels = 0;
+    float4 *qa_o = nullptr, *qa_d = nullptr, *qb_o = nullptr, *qb_d = nullptr, *h_n = nullptr;
+    uint2* h_m = nullptr;
+    float *occ = nullptr, *shadow = nullptr;
+    float4 *lvl = nullptr, *term = nullptr;
+    float4 *hdr = nullptr, *bright = nullptr, *blur = nullptr;
+    uint32_t* counters = nullptr;
+    void release();
+    // Grows the buffers to hold at least the given sizes (contents are not kept).
+    cudaError_t ensure(size_t cap, size_t lights, size_t levels, size_t pixels);
+    size_t bytes() const;
+    static size_t bytes_for(size_t cap, size_t lights, size_t levels, size_t pixels);
+};
+
+// Per-kernel-kind device time, from CUDA events around each pass (off by default).
+class Profiler {
+  public:
+    ~Profiler();
+    bool on = false;
+    void begin(uint32_t kind, cudaStream_t s);
+    void end(uint32_t kind, cudaStream_t s);
+    // Waits for the recorded passes and adds their times into ms / launches; clears.
+    cudaError_t collect(double* ms, uint32_t* launches);
+    LaunchLog log();  // a launch log that records into this profiler when `on`
+
+  private:
+    cudaEvent_t event();
+    std::vector<cudaEvent_t> pool_;
+    size_t used_ = 0;
+    struct Rec {
+        uint32_t kind;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs_;
+    std::vector<cudaEvent_t> open_;
+};
+
+// A beauty pass sequence: either one job inline (host sizes) or a device job table (sizes
+// read by the kernels, buffers sized by the capacities below).
+struct PassPlan {
+    FrameJob job0{};
+    uint32_t tape_bytes = 0;        // job0's tape (shared-memory staging)
+    const FrameJob* jobs = nullptr; // device table, or null
+    const JobTotals* totals = nullptr;
+    uint32_t n_samples = 0;         // samples / slots / pixels (host sizes, or capacities)
+    uint32_t n_slots = 0;
+    uint32_t n_pixels = 0;
+    uint32_t levels = 1;            // bounces + 1
+    uint32_t lights_max = 0;
+    bool ao = false, shadows = false, bloom = false, post = true;
+    bool clear_status = true;       // also clear the status word with the work counters
+};
+
+// Enqueues the passes on `s`: counters cleared, march / AO / shadow / shade per level,
+// resolve into buf.hdr, then post into each job's `out` when plan.post. Asynchronous.
+cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams& tune, cudaStream_t s, int sm_count,
+                       LaunchLog* log);
+
+// Post stack only (hdr already in buf.hdr).
+cudaError_t run_post(const PassPlan& plan, PassBuffers& buf, cudaStream_t s, int sm_count, LaunchLog* log);
+
+}  // namespace mm3e

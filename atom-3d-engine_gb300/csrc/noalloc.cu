@@ -96,17 +96,18 @@ int noalloc_march_rays(const unsigned char* tape, uint32_t tape_bytes, int devic
     }
     if (e == cudaSuccess) {
         WaveArgs a{};
-        a.tape = tape;
+        a.job0.tape = tape;
         a.tape_bytes = tape_bytes;
         a.status = s->counters + 63;
         a.counter = s->counters;
         a.src = SRC_QUEUE;
         a.n_items = nn;
+        a.cap = nn;
         a.b.q_o = s->q_o;
         a.b.q_d = s->q_d;
         a.b.h_n = s->h_n;
         a.b.h_m = s->h_m;
-        e = launch_march(a, stream, sm_count, nullptr);
+        e = launch_march(a, TuneParams{}, stream, sm_count, nullptr);
     }
     if (e == cudaSuccess) {
         k_split_hits<<<blocks, 128, 0, stream>>>(s->h_n, s->h_m, nn, d_t, d_mat, d_steps);

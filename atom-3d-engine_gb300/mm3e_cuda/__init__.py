@@ -66,6 +66,61 @@ class Context:
         self.check(lib().mm3e_ctx_device_info(self._ptr, C.byref(sm), C.byref(clk)))
         return {"sm_count": sm.value, "clock_khz": clk.value}
 
+    # ---- launch shape, profiling -------------------------------------------------------------
+    def set_tuning(self, block=128, tile_wlog=3, unroll=1):
+        self.check(lib().mm3e_ctx_set_tuning(self._ptr, C.byref(abi.Tuning(block, tile_wlog, unroll))))
+
+    def get_tuning(self):
+        t = abi.Tuning()
+        self.check(lib().mm3e_ctx_get_tuning(self._ptr, C.byref(t)))
+        return {"block": t.block, "tile_wlog": t.tile_wlog, "unroll": t.unroll}
+
+    def set_profiling(self, on=True):
+        self.check(lib().mm3e_ctx_set_profiling(self._ptr, 1 if on else 0))
+
+    def kernel_times(self):
+        """{kind: (launches, ms)} of the passes run since the last call (profiling on)."""
+        arr = (abi.KernelTime * 16)()
+        n = C.c_uint32()
+        self.check(lib().mm3e_ctx_kernel_times(self._ptr, arr, 16, C.byref(n)))
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].ms) for i in range(min(n.value, 16))}
+
+    # ---- batched rendering ---------------------------------------------------------------------
+    def configure_batch(self, max_samples=0, use_graphs=True):
+        self.check(lib().mm3e_batch_configure(self._ptr, C.byref(abi.BatchConfig(max_samples, 1 if use_graphs else 0))))
+
+    @staticmethod
+    def make_jobs(items):
+        """items: (CompiledScene, camera, width, height, format, device_ptr or None, host ndarray or None)."""
+        jobs = (abi.Job * len(items))()
+        for i, (sc, cam, w, h, fmt, dptr, host) in enumerate(items):
+            j = jobs[i]
+            j.scene = sc._ptr
+            j.camera = cam
+            j.width, j.height, j.format = w, h, fmt
+            px = 4 if fmt == abi.FB_RGBA8 else 16
+            j.out_bytes = (w or sc.width) * (h or sc.height) * px
+            if dptr:
+                j.device_out = dptr
+            else:
+                j.host_out = host.ctypes.data
+        return jobs
+
+    def render_batch(self, jobs, n=None):
+        """Render a ctypes Job array (see make_jobs); returns the batch stats as a dict."""
+        st = abi.BatchStats()
+        self.check(lib().mm3e_render_batch(self._ptr, jobs, len(jobs) if n is None else n, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in abi.BatchStats._fields_}
+
+    def autotune(self, jobs, repeats=1):
+        best = abi.Tuning()
+        rep = (abi.TuneEntry * 64)()
+        n = C.c_uint32()
+        self.check(lib().mm3e_autotune(self._ptr, jobs, len(jobs), repeats, C.byref(best), rep, 64, C.byref(n)))
+        table = [({"block": rep[i].tuning.block, "tile_wlog": rep[i].tuning.tile_wlog,
+                   "unroll": rep[i].tuning.unroll}, rep[i].device_ms) for i in range(n.value)]
+        return {"block": best.block, "tile_wlog": best.tile_wlog, "unroll": best.unroll}, table
+
     def close(self):
         """Destroy the context; scenes compiled on it are destroyed first."""
         if self._ptr:
@@ -115,6 +170,11 @@ class CompiledScene:
             self.close()
         except Exception:
             pass
+
+    def device_bytes(self):
+        n = C.c_size_t()
+        self.ctx.check(lib().mm3e_scene_device_bytes(self._ptr, C.byref(n)))
+        return n.value
 
     def render(self, camera, dyn_spheres=(), fmt=abi.FB_RGBA_F32, stats=False):
         """Framebuffer of the frame: (h, w, 4) f32 RGBA, or (h, w, 4) u8 for FB_RGBA8."""

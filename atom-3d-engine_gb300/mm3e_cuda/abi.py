@@ -1,7 +1,7 @@
 """ctypes mirror of include/mm3e_cuda.h (the C ABI of the GB300 SDF render path)."""
 import ctypes as C
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 OK = 0
 ERR_INVALID = -1
@@ -96,6 +96,34 @@ class RenderStats(C.Structure):
                 ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("block", C.c_uint32), ("tile_wlog", C.c_uint32), ("unroll", C.c_uint32)]
+
+
+class KernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 16), ("launches", C.c_uint32), ("ms", C.c_double)]
+
+
+class Job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("format", C.c_uint32), ("device_out", C.c_void_p), ("host_out", C.c_void_p),
+                ("out_bytes", C.c_size_t)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("max_samples", C.c_uint64), ("use_graphs", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("device_ms", C.c_double), ("total_ms", C.c_double), ("sequences", C.c_uint32),
+                ("kernel_launches", C.c_uint32), ("graph_launches", C.c_uint32), ("samples", C.c_uint64),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("tuning", Tuning), ("device_ms", C.c_double)]
+
+
 # Every symbol include/mm3e_cuda.h declares (checked by the CPU test suite).
 EXPORTED_SYMBOLS = [
     "mm3e_abi_version", "mm3e_camera_look_at", "mm3e_orbit_camera", "mm3e_mat3_from_euler", "mm3e_quat_to_mat3",
@@ -104,4 +132,6 @@ EXPORTED_SYMBOLS = [
     "mm3e_scene_compile", "mm3e_scene_destroy", "mm3e_render", "mm3e_render_linear", "mm3e_render_device",
     "mm3e_bake_gi", "mm3e_scene_get_gi", "mm3e_render_hits", "mm3e_march_rays", "mm3e_field",
     "mm3e_march_rays_noalloc",
+    "mm3e_ctx_set_tuning", "mm3e_ctx_get_tuning", "mm3e_ctx_set_profiling", "mm3e_ctx_kernel_times",
+    "mm3e_scene_device_bytes", "mm3e_batch_configure", "mm3e_render_batch", "mm3e_autotune",
 ]

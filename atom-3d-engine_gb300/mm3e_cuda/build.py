@@ -23,8 +23,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["wavefront.cu", "noalloc.cu"]
-CPP_SOURCES = ["lower.cpp", "capi.cpp"]
-HEADERS = ["tape.h", "lower.h", "kernels.h", "device_math.cuh", "noalloc.h"]
+CPP_SOURCES = ["lower.cpp", "capi.cpp", "engine.cpp", "batch.cpp"]
+HEADERS = ["tape.h", "lower.h", "kernels.h", "device_math.cuh", "noalloc.h", "engine.h", "capi_internal.h", "batch.h"]
 
 
 def _cudart_dir():

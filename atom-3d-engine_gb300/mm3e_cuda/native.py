@@ -63,6 +63,15 @@ def _declare_extra(lib):
         "mm3e_field": (C.c_int, [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float), P(C.c_uint32)]),
         "mm3e_march_rays_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p,
                                               C.c_void_p]),
+        "mm3e_ctx_set_tuning": (C.c_int, [C.c_void_p, P(abi.Tuning)]),
+        "mm3e_ctx_get_tuning": (C.c_int, [C.c_void_p, P(abi.Tuning)]),
+        "mm3e_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+        "mm3e_ctx_kernel_times": (C.c_int, [C.c_void_p, P(abi.KernelTime), C.c_uint32, P(C.c_uint32)]),
+        "mm3e_scene_device_bytes": (C.c_int, [C.c_void_p, P(C.c_size_t)]),
+        "mm3e_batch_configure": (C.c_int, [C.c_void_p, P(abi.BatchConfig)]),
+        "mm3e_render_batch": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, P(abi.BatchStats)]),
+        "mm3e_autotune": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, C.c_uint32, P(abi.Tuning),
+                                    P(abi.TuneEntry), C.c_uint32, P(C.c_uint32)]),
     }
     for name, (res, args) in extra.items():
         fn = getattr(lib, name, None)

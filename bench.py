@@ -10,9 +10,11 @@ scene tape to a device RGBA8 framebuffer (render kernel + post kernels).
              L2 flushed between timed frames by writing a 256 MB buffer)
   e2e        frames/s through the public C ABI call mm3e_render with a host framebuffer:
              per frame the camera goes host->device and the RGBA8 frame device->host
-  roofline   FP32-pipe roofline of the dominant kernel (the tape interpreter): algorithmic
-             f32 operations per frame (oracle operation count, committed fixture) / its
-             event-timed launch duration, against SMs x 128 lanes x 2 x max SM clock
+  roofline   FP32-pipe roofline of the dominant kernel (the march tape interpreter): the
+             algorithmic f32 operations of its phase per frame (oracle operation count split by
+             kernel, committed fixture) / its CUDA-event-timed device time per frame (events
+             around every pass, a second run of the same frames), against SMs x 128 lanes x 2 x
+             max SM clock
   cpu_baseline  the CPU restatement of the reference render path on all host cores, timed on
              a bounded row sample (rows scaled to a full frame) plus its single-thread post pass
 
@@ -35,13 +37,18 @@ sys.path.insert(0, os.path.join(ROOT, "atom-3d-engine_gb300"))
 COUNTS_FIXTURE = os.path.join(ROOT, "tests", "golden", "workload_counts.json")
 
 
-def workloads():
+def workloads(size=None):
+    """Workload name -> () -> (Scene, Camera). `size` (w, h) overrides the resolution (small
+    cases for profiler captures)."""
     from mm3e_cuda import scenes
 
+    def sz(w, h):
+        return size if size else (w, h)
+
     return {
-        "gallery_1080p": lambda: scenes.gallery_scene(1920, 1080),
-        "spheres_540p": lambda: scenes.spheres_scene(960, 540),
-        "hero_540p_aa2": lambda: scenes.hero_scene(960, 540, 2, 2),
+        "gallery_1080p": lambda: scenes.gallery_scene(*sz(1920, 1080)),
+        "spheres_540p": lambda: scenes.spheres_scene(*sz(960, 540)),
+        "hero_540p_aa2": lambda: scenes.hero_scene(*sz(960, 540), 2, 2),
     }
 
 
@@ -54,7 +61,30 @@ def parse():
     ap.add_argument("--workload", default="gallery_1080p")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="only render this many frames of the workload (no timing, no JSON line): the "
+                         "command profilers run")
+    ap.add_argument("--size", default=None, help="WxH resolution override (with --profile-frames)")
     return ap.parse_args()
+
+
+def run_profile_frames(args):
+    """Renders N frames of the workload through mm3e_render_device and exits (for ncu)."""
+    import torch
+
+    import mm3e_cuda
+    from mm3e_cuda import abi
+
+    size = tuple(int(v) for v in args.size.lower().split("x")) if args.size else None
+    scene, cam = workloads(size)[args.workload]()
+    ctx = mm3e_cuda.Context(0)
+    compiled = mm3e_cuda.CompiledScene(ctx, scene)
+    out = torch.empty(scene.width * scene.height * 4, dtype=torch.uint8, device="cuda")
+    for _ in range(args.profile_frames):
+        compiled.render_device(cam, abi.FB_RGBA8, out.data_ptr(), out.numel())
+    ctx.sync()
+    print(f"rendered {args.profile_frames} frame(s) of {args.workload} at {scene.width}x{scene.height}")
+    ctx.close()
 
 
 def load_counts(workload):
@@ -195,9 +225,6 @@ def run_ours(args):
     def frame():
         compiled.render_device(cam, abi.FB_RGBA8, out8.data_ptr(), out8.numel())
 
-    def interp_only():
-        compiled.render_device(cam, abi.FB_LINEAR_F32, hdr.data_ptr(), hdr.numel() * 4)
-
     def timed(fn, k):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
         with torch.cuda.stream(stream):
@@ -211,7 +238,6 @@ def run_ours(args):
 
     for _ in range(max(3, args.warmup)):
         frame()
-        interp_only()
     stream.synchronize()
     if dist:
         tdist.barrier()
@@ -222,7 +248,12 @@ def run_ours(args):
     frame_ms = timed(frame, args.steps)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    interp_ms = timed(interp_only, args.steps)
+    # per-kernel device time: the same frames again with CUDA events around every pass
+    ctx.set_profiling(True)
+    ctx.kernel_times()
+    prof_ms = timed(frame, args.steps)
+    kt = ctx.kernel_times()
+    ctx.set_profiling(False)
 
     # e2e: the public call with a host framebuffer (camera in, RGBA8 frame out, every frame)
     host = np.empty((h, w, 4), np.uint8)
@@ -245,23 +276,32 @@ def run_ours(args):
 
     value = world * 1000.0 / mean_ms
     counts = load_counts(args.workload)
-    interp_avg_s = sum(interp_ms) / len(interp_ms) / 1000.0
     sm = info["sm_count"]
     max_mhz = clocks.get("sm_max_mhz") or 2070.0
     peak = sm * 128 * 2 * max_mhz * 1e6 / 1e12
+    prof_total = sum(ms for _, ms in kt.values())
+    kernels = {k: {"launches_per_frame": n / args.steps, "ms_per_frame": ms / args.steps,
+                   "share": ms / prof_total if prof_total else None} for k, (n, ms) in kt.items()}
+    dom = max(kt, key=lambda k: kt[k][1]) if kt else "march"
+    dom_s = kt[dom][1] / args.steps / 1000.0 if kt else None
     roofline = {"bound": "fp32", "unit": "TFLOP/s", "peak": peak,
                 "peak_basis": f"{sm} SMs x 128 FP32 lanes x 2 (FMA) x {max_mhz:.0f} MHz max SM clock "
                               "(nominal; MEASURED_PEAKS.json holds no FP32 figure)",
-                "traffic": None, "kernel": "k_uber (tape interpreter)", "kernel_ms": interp_avg_s * 1000.0}
+                "kernel": f"k_{dom}", "kernel_ms_per_frame": None if dom_s is None else dom_s * 1000.0,
+                "kernels": kernels, "traffic": None,
+                "profiled_frame_ms": sum(prof_ms) / len(prof_ms)}
     mrays = None
     if counts:
         r = counts["render"]
-        roofline["achieved"] = r["fp32"] / interp_avg_s / 1e12
-        roofline["frac"] = roofline["achieved"] / peak
-        if clocks.get("sm_mhz"):
-            roofline["frac_at_run_clock"] = roofline["achieved"] / (sm * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
-        roofline["algorithmic_fp32_per_launch"] = r["fp32"]
-        roofline["field_evals_per_launch"] = r["field_evals"]
+        phase = counts.get(dom) or r
+        if dom_s:
+            roofline["achieved"] = phase["fp32"] / dom_s / 1e12
+            roofline["frac"] = roofline["achieved"] / peak
+            if clocks.get("sm_mhz"):
+                roofline["frac_at_run_clock"] = roofline["achieved"] / (sm * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
+        roofline["algorithmic_fp32_per_frame"] = phase["fp32"]
+        roofline["field_evals_per_frame"] = phase["field_evals"]
+        roofline["frame_fp32_per_s"] = (r["fp32"] + counts["post"]["fp32"]) * value / 1e12
         rays = r["primary_rays"] + r["reflection_rays"] + r["shadow_rays"]
         mrays = rays * value / 1e6
     cpu = None
@@ -290,7 +330,9 @@ def run_ours(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile_frames:
+        run_profile_frames(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define MM3E_ABI_VERSION 1
+#define MM3E_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------------------- */
 enum {
@@ -288,10 +288,33 @@ int mm3e_ctx_set_stream(mm3e_ctx* ctx, void* cuda_stream);
 /* SM count and clock of the context's device (for roofline reporting). */
 int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
 
+/* Launch shape of the march and soft-shadow passes: threads per CTA (128 or 256), pixel tile
+ * of 32 pixels 2^tile_wlog wide (tile_wlog 0..5; 3 = 8x4), and field samples per lane between
+ * work refills (unroll 1 or 2). Results do not depend on it. mm3e_autotune picks one. */
+typedef struct mm3e_tuning {
+    uint32_t block, tile_wlog, unroll;
+} mm3e_tuning;
+int mm3e_ctx_set_tuning(mm3e_ctx* ctx, const mm3e_tuning* t);
+int mm3e_ctx_get_tuning(mm3e_ctx* ctx, mm3e_tuning* t);
+
+/* Per-kernel device time: when enabled, every pass is bracketed with CUDA events on the
+ * context's stream (batched pass sequences then run without CUDA graphs).
+ * mm3e_ctx_kernel_times waits for the recorded passes, writes one entry per kernel kind that
+ * ran (march, ao, shadow, shade, resolve, post, aov, gi, other) and clears the totals. */
+typedef struct mm3e_kernel_time {
+    char name[16];
+    uint32_t launches;
+    double ms;
+} mm3e_kernel_time;
+int mm3e_ctx_set_profiling(mm3e_ctx* ctx, int enable);
+int mm3e_ctx_kernel_times(mm3e_ctx* ctx, mm3e_kernel_time* out, uint32_t cap, uint32_t* n_out);
+
 /* ---- scenes ------------------------------------------------------------------------------- */
 /* Validates and lowers `desc` into a device-resident scene tape; `desc` may be freed after. */
 int mm3e_scene_compile(mm3e_ctx* ctx, const mm3e_scene_desc* desc, mm3e_scene** out);
 void mm3e_scene_destroy(mm3e_scene* scene);
+/* Device memory the compiled scene holds (tape, payloads, pass and frame buffers). */
+int mm3e_scene_device_bytes(mm3e_scene* scene, size_t* out_bytes);
 
 /* Render one frame of `scene` (scene->width x height, scene->mode) into host memory.
  * `dyn`/`n_dyn` append dynamic spheres exactly as CpuParallelScene::try_render does.
@@ -326,6 +349,52 @@ int mm3e_render_hits(mm3e_scene* scene, const mm3e_camera* camera, float* t, uin
 int mm3e_march_rays(mm3e_scene* scene, const float* rays6, size_t n, float* t, uint32_t* mat, uint32_t* steps);
 /* World field (accelerated plan) at `n` points: Scene::field (lib.rs:715-717). */
 int mm3e_field(mm3e_scene* scene, const float* points3, size_t n, float* dist, uint32_t* mat);
+
+/* ---- batched rendering ---------------------------------------------------------------------- */
+/* One frame of a batch: a compiled beauty-mode scene, a camera and an output. width/height 0
+ * render at the scene's own size; otherwise the scene is rendered at width x height (the
+ * reference renders any Scene at the size its caller sets). The frame goes to device_out
+ * (device memory) or, when that is NULL, to host_out. */
+typedef struct mm3e_job {
+    mm3e_scene* scene;
+    mm3e_camera camera;
+    uint32_t width, height;
+    uint32_t format;     /* MM3E_FB_RGBA8 or MM3E_FB_RGBA_F32 */
+    void* device_out;
+    void* host_out;
+    size_t out_bytes;
+} mm3e_job;
+
+typedef struct mm3e_batch_config {
+    uint64_t max_samples; /* samples (pixels x aa^2, tiles padded) per pass sequence; 0 = 2^24 */
+    uint32_t use_graphs;  /* 1: replay each pass-sequence shape from a captured CUDA graph */
+} mm3e_batch_config;
+
+typedef struct mm3e_batch_stats {
+    double device_ms;         /* CUDA events around the whole batch on the context's stream */
+    double total_ms;          /* host wall time of the call */
+    uint32_t sequences;       /* pass sequences (waves) run */
+    uint32_t kernel_launches; /* kernels launched, graph kernel nodes included */
+    uint32_t graph_launches;
+    uint64_t samples;
+    uint64_t h2d_bytes, d2h_bytes;
+} mm3e_batch_stats;
+
+int mm3e_batch_configure(mm3e_ctx* ctx, const mm3e_batch_config* cfg);
+/* Renders every job; frames are identical to mm3e_render / mm3e_render_device of the same scene
+ * and camera at the same size. Jobs are packed in order into pass sequences of at most
+ * max_samples samples; each pass of a sequence is one launch over all its jobs. Blocking. */
+int mm3e_render_batch(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats);
+
+/* Times every launch shape (block 128/256 x tile_wlog 2/3/4 x unroll 1/2) on `jobs` (each
+ * rendered `repeats` times after a warm-up), keeps the fastest as the context's tuning and
+ * reports the timings. */
+typedef struct mm3e_tune_entry {
+    mm3e_tuning tuning;
+    double device_ms;
+} mm3e_tune_entry;
+int mm3e_autotune(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, uint32_t repeats, mm3e_tuning* best,
+                  mm3e_tune_entry* report, uint32_t report_cap, uint32_t* n_report);
 
 /* ---- allocation-free ray queries --------------------------------------------------------- */
 /* No counterpart in the reference: an addition for callers that cannot allocate device memory

@@ -201,20 +201,31 @@ int oracle_field(const mm3e_scene_desc* d, const float* pts3, size_t n, int line
     return 0;
 }
 
-// Operation counts for one full frame, f32 semantics: 14 values for the render phase
-// (tape interpretation + shading) followed by 14 for the post phase (bloom + tone map):
+namespace {
+void put_counts(const OpCounts& t, uint64_t* out) {
+    uint64_t v[14] = {t.fp32(), t.add, t.mul, t.cmp, t.minmax, t.div, t.sqrt, t.trans, t.field_evals, t.dual_evals,
+                      t.primary_rays, t.reflection_rays, t.shadow_rays, t.gi_rays};
+    std::memcpy(out, v, sizeof(v));
+}
+}  // namespace
+
+// Operation counts for one full frame, f32 semantics, 14 values per block:
 // [fp32, add, mul, cmp, minmax, div, sqrt, trans, field_evals, dual_evals,
-//  primary_rays, reflection_rays, shadow_rays, gi_rays]
-int oracle_count_frame(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, uint64_t* counts) {
+//  primary_rays, reflection_rays, shadow_rays, gi_rays].
+// Blocks: 0 render phase (tape interpretation + shading), 1 post phase (bloom + tone map),
+// then, when `n_blocks` is 6, the render phase split by kernel: 2 march (+ hit normal), 3 AO,
+// 4 soft shadow, 5 shading (camera rays, BRDF / IBL / GI / fog, reflection set-up).
+int oracle_count_frame_blocks(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, uint64_t* counts,
+                              int n_blocks) {
     Scene<CountF> s = scene_from_desc<CountF>(*d);
     Camera<CountF> c = cam_from<CountF>(*cam);
     size_t n = (size_t)s.width * s.height;
     std::vector<V3<CountF>> hdr(n);
-    OpCounts render, post;
+    OpCounts render, post, phase[PH_COUNT];
     std::mutex mu;
     bool dual_safe = scene_dual_safe(s);
     for_row_bands(0, s.height, threads, [&](uint32_t a, uint32_t b, size_t) {
-        op_counts() = OpCounts();
+        reset_counts();
         World<CountF> w(s);
         for (uint32_t y = a; y < b; ++y)
             for (uint32_t x = 0; x < s.width; ++x) {
@@ -222,22 +233,26 @@ int oracle_count_frame(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigne
                 else (void)aov_pixel(s, w, c, x, y, dual_safe);
             }
         std::lock_guard<std::mutex> lk(mu);
-        render.merge(op_counts());
+        for (int i = 0; i < PH_COUNT; ++i) {
+            render.merge(phase_counts()[i]);
+            phase[i].merge(phase_counts()[i]);
+        }
     });
     if (s.mode == MM3E_MODE_BEAUTY) {
-        op_counts() = OpCounts();
+        reset_counts();
         std::vector<float> rgba(4 * n);
         post_resolve(hdr, s.width, s.height, s.post, rgba.data());
-        post.merge(op_counts());
+        for (int i = 0; i < PH_COUNT; ++i) post.merge(phase_counts()[i]);
     }
-    const OpCounts* phases[2] = {&render, &post};
-    for (int ph = 0; ph < 2; ++ph) {
-        const OpCounts& t = *phases[ph];
-        uint64_t v[14] = {t.fp32(), t.add, t.mul, t.cmp, t.minmax, t.div, t.sqrt, t.trans, t.field_evals, t.dual_evals,
-                          t.primary_rays, t.reflection_rays, t.shadow_rays, t.gi_rays};
-        std::memcpy(counts + 14 * ph, v, sizeof(v));
-    }
+    put_counts(render, counts);
+    if (n_blocks > 1) put_counts(post, counts + 14);
+    for (int i = 0; i < PH_COUNT && i + 2 < n_blocks; ++i) put_counts(phase[i], counts + 14 * (i + 2));
     return 0;
+}
+
+// Render + post blocks only (28 values).
+int oracle_count_frame(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, uint64_t* counts) {
+    return oracle_count_frame_blocks(d, cam, threads, counts, 2);
 }
 
 // Scene::bake_gi (lib.rs:665-682). cubes: nx*ny*nz*18 floats. Returns 1 if baked, 0 if the

@@ -6,7 +6,9 @@
 //   fp32  = add + sub + mul + min/max + compare-select   (an FMA on the GPU retires two of these)
 //   div, sqrt and transcendentals (sin/cos/tan/exp/pow/acos) are counted separately and are not
 //   part of the FP32-pipe numerator.
-// Counters are thread-local; the render driver sums them over worker threads.
+// Counters are thread-local; the render driver sums them over worker threads. They are kept per
+// render phase (PH_MARCH: primary/reflection march + hit normal, PH_AO, PH_SHADOW, PH_SHADE:
+// everything else), matching the kernels the CUDA path splits a frame into.
 #pragma once
 #include <cstdint>
 
@@ -27,9 +29,18 @@ struct OpCounts {
     uint64_t fp32() const { return add + mul + cmp + minmax; }
 };
 
-inline OpCounts& op_counts() {
-    static thread_local OpCounts c;
+inline OpCounts* phase_counts() {
+    static thread_local OpCounts c[PH_COUNT];
     return c;
+}
+inline int& current_phase() {
+    static thread_local int ph = PH_SHADE;
+    return ph;
+}
+inline OpCounts& op_counts() { return phase_counts()[current_phase()]; }
+inline void reset_counts() {
+    for (int i = 0; i < PH_COUNT; ++i) phase_counts()[i] = OpCounts();
+    current_phase() = PH_SHADE;
 }
 
 struct CountF {
@@ -66,6 +77,11 @@ template <> struct Hooks<CountF> {
     static void reflection_ray() { op_counts().reflection_rays++; }
     static void shadow_ray() { op_counts().shadow_rays++; }
     static void gi_ray() { op_counts().gi_rays++; }
+    static int phase(int ph) {
+        int prev = current_phase();
+        current_phase() = ph;
+        return prev;
+    }
 };
 
 template <> struct Lit<CountF> { static CountF get(float f, double) { return CountF(f); } };

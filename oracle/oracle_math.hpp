@@ -98,14 +98,25 @@ template <class T> inline uint64_t o_to_usize(T x) {
 
 template <class T> inline T o_inf() { return T(std::numeric_limits<float>::infinity()); }
 
+// Render phases the counting instantiation attributes work to.
+enum : int { PH_MARCH = 0, PH_AO = 1, PH_SHADOW = 2, PH_SHADE = 3, PH_COUNT = 4 };
+
 // Event hooks for the counting instantiation (no-ops for float / double).
 template <class T> struct Hooks {
+    static int phase(int) { return PH_SHADE; }
     static void field_eval() {}
     static void dual_eval() {}
     static void primary_ray() {}
     static void reflection_ray() {}
     static void shadow_ray() {}
     static void gi_ray() {}
+};
+
+// Attributes the work of a scope to a render phase (counting instantiation only).
+template <class T> struct PhaseScope {
+    int prev;
+    explicit PhaseScope(int ph) : prev(Hooks<T>::phase(ph)) {}
+    ~PhaseScope() { Hooks<T>::phase(prev); }
 };
 
 }  // namespace oracle

@@ -41,6 +41,7 @@ def lib():
         l.oracle_aces.argtypes = [P(C.c_float), P(C.c_float)]
         l.oracle_field.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_int, P(C.c_float), P(C.c_uint32)]
         l.oracle_count_frame.argtypes = [vp, vp, C.c_uint, P(C.c_uint64)]
+        l.oracle_count_frame_blocks.argtypes = [vp, vp, C.c_uint, P(C.c_uint64), C.c_int]
         l.oracle_bake_gi.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint, P(C.c_float),
                                      P(C.c_float), P(C.c_uint32), P(C.c_float)]
         l.oracle_gi_sample.argtypes = [vp, P(C.c_float), P(C.c_float), C.c_size_t, P(C.c_float)]
@@ -171,12 +172,17 @@ COUNT_KEYS = ["fp32", "add", "mul", "cmp", "minmax", "div", "sqrt", "trans", "fi
               "primary_rays", "reflection_rays", "shadow_rays", "gi_rays"]
 
 
+COUNT_BLOCKS = ("render", "post", "march", "ao", "shadow", "shade")
+
+
 def count_frame(handle, cam, threads=None):
-    """Algorithmic work of one frame: {"render": {...}, "post": {...}} (f32 op counts, rays)."""
-    out = (C.c_uint64 * 28)()
-    lib().oracle_count_frame(C.addressof(handle.desc), C.addressof(cam), threads or threads_default(), out)
+    """Algorithmic work of one frame (f32 op counts, rays): {"render", "post"} plus the render
+    phase split by kernel ("march" incl. hit normals, "ao", "shadow", "shade")."""
+    out = (C.c_uint64 * (14 * len(COUNT_BLOCKS)))()
+    lib().oracle_count_frame_blocks(C.addressof(handle.desc), C.addressof(cam), threads or threads_default(), out,
+                                    len(COUNT_BLOCKS))
     vals = [int(v) for v in out]
-    return {"render": dict(zip(COUNT_KEYS, vals[:14])), "post": dict(zip(COUNT_KEYS, vals[14:]))}
+    return {name: dict(zip(COUNT_KEYS, vals[14 * i:14 * i + 14])) for i, name in enumerate(COUNT_BLOCKS)}
 
 
 def bake_gi(handle, dims, samples, threads=None):

@@ -649,6 +649,7 @@ template <class T> struct World {
 // lib.rs render path
 // ------------------------------------------------------------------------------------------
 template <class T> inline Hit<T> march_scene(const Scene<T>& s, const World<T>& w, bool dual_safe, const Ray<T>& ray) {
+    PhaseScope<T> ph(PH_MARCH);
     if (dual_safe) return s.marcher.march_with(w, [&](V3<T> p) { return normal_dual(s, p); }, ray);
     return s.marcher.march_with(w, [&](V3<T> p) { return s.marcher.normal(w, p); }, ray);
 }
@@ -710,7 +711,11 @@ inline V3<T> shade_hit(const Scene<T>& s, const World<T>& w, const Hit<T>& hit, 
     V3<T> albedo = m.albedo;
     V3<T> normal = hit.normal;
     V3<T> view = scale(ray.dir, T(-1));
-    T occ = s.ao ? s.marcher.ambient_occlusion(w, hit.pos, hit.normal) : T(1);
+    T occ = T(1);
+    if (s.ao) {
+        PhaseScope<T> ph(PH_AO);
+        occ = s.marcher.ambient_occlusion(w, hit.pos, hit.normal);
+    }
     V3<T> gi = s.gi ? s.gi->sample(hit.pos, normal) : zero3<T>();
     V3<T> ambient_irr = ibl_irradiance(s, normal) + gi + s.ambient;
     V3<T> radiance = scale(cmul(albedo, ambient_irr), occ);
@@ -724,6 +729,7 @@ inline V3<T> shade_hit(const Scene<T>& s, const World<T>& w, const Hit<T>& hit, 
             T max_t = o_min(l_dist, s.marcher.max_dist);
             T lift = o_max(s.marcher.normal_h * T(2), OL(0.01));
             Hooks<T>::shadow_ray();
+            PhaseScope<T> ph(PH_SHADOW);
             shadow = s.marcher.soft_shadow(w, hit.pos + scale(hit.normal, lift), l_dir, max_t, light.shadow_k(l_dist));
         }
         if (shadow <= T(0)) continue;

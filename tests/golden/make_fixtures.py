@@ -4,7 +4,8 @@
 
 * workload_counts.json  algorithmic work per frame of the benchmark workloads (the oracle's
                         counting instantiation: f32 ops, field evaluations, rays), render and
-                        post phases separately; bench.py reads it for Mrays/s and the roofline.
+                        post phases and the render phase split by kernel (march, ao, shadow,
+                        shade); bench.py reads it for Mrays/s and the roofline.
 * oracle_frames.npz     small RGB8 frames of the parity scenes rendered by the oracle; the CPU
                         suite checks the oracle still reproduces them bit-exactly and the GPU
                         suite compares the CUDA path against them.
@@ -76,7 +77,6 @@ def frames():
 
 
 def reference_images():
-    sys.path.insert(0, os.path.join(ROOT, "_work"))
     res = {}
     if not os.path.isdir(REFERENCE):
         return res
@@ -106,6 +106,8 @@ if __name__ == "__main__":
     sys.path.insert(0, HERE)
     with open(os.path.join(HERE, "workload_counts.json"), "w") as f:
         json.dump(counts(), f, indent=1)
+    if "--counts-only" in sys.argv:
+        sys.exit(0)
     np.savez_compressed(os.path.join(HERE, "oracle_frames.npz"), **frames())
     ri = reference_images()
     if ri:
