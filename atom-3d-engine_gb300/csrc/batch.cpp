@@ -7,27 +7,33 @@
 
 namespace mm3e {
 
+int status_error(mm3e_ctx* c, uint32_t st);
+
 namespace {
 constexpr uint32_t WAVE_JOBS_MAX = 4096;
 
-int check_wave_status(mm3e_ctx* c, const uint32_t* d_status) {
+int check_wave_status(mm3e_ctx* c, cudaStream_t s, const uint32_t* d_status) {
     uint32_t st = 0;
-    cudaError_t e = cudaMemcpyAsync(&st, d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaError_t e = cudaMemcpyAsync(&st, d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(c, e, "batch render");
+    return status_error(c, st);
+}
+}  // namespace
+
+int status_error(mm3e_ctx* c, uint32_t st) {
     if (st & ST_TAPE_TIMEOUT) return fail(c, MM3E_ERR_TIMEOUT, "scene tape staging wait gave up");
     if (st & ST_TAPE_CORRUPT) return fail(c, MM3E_ERR_CUDA, "scene tape corrupt after staging");
     return MM3E_OK;
 }
-}  // namespace
 
-BatchEngine::BatchEngine(mm3e_ctx* c) : c_(c) {
+BatchEngine::BatchEngine(mm3e_ctx* c, cudaStream_t stream) : c_(c), s_(stream) {
     for (Ring& r : ring_) cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming);
 }
 
 BatchEngine::~BatchEngine() {
     cudaSetDevice(c_->device);
-    cudaStreamSynchronize(c_->stream);
+    cudaStreamSynchronize(stream());
     for (auto& g : graphs_) cudaGraphExecDestroy(g.second.exec);
     buf_.release();
     cudaFree(d_jobs_);
@@ -47,10 +53,15 @@ size_t BatchEngine::device_bytes() const {
     return b;
 }
 
+int BatchEngine::reserve(uint64_t samples, uint32_t lights, uint32_t levels) {
+    cudaError_t e = buf_.ensure(samples, lights, levels, samples);
+    return e == cudaSuccess ? MM3E_OK : cuda_fail(c_, e, "batch buffer allocation");
+}
+
 int BatchEngine::configure(const mm3e_batch_config& cfg) {
     uint64_t cap = cfg.max_samples ? cfg.max_samples : (1ull << 24);
     if (cap > 0x7FFFFFFFull) return fail(c_, MM3E_ERR_INVALID, "max_samples too large");
-    cudaError_t e = cudaStreamSynchronize(c_->stream);
+    cudaError_t e = cudaStreamSynchronize(stream());
     if (e != cudaSuccess) return cuda_fail(c_, e, "batch configure");
     max_samples_ = cap;
     use_graphs_ = cfg.use_graphs != 0;
@@ -61,7 +72,7 @@ int BatchEngine::ensure(uint64_t samples, uint64_t pixels, uint32_t lights, uint
                         uint32_t jobs, int ring) {
     bool regrow = samples > buf_.cap || pixels > buf_.pixels || lights > buf_.lights || levels > buf_.levels;
     if (regrow) {
-        cudaStreamSynchronize(c_->stream);
+        cudaStreamSynchronize(stream());
         for (auto& g : graphs_) cudaGraphExecDestroy(g.second.exec);
         graphs_.clear();
         // grow geometrically up to the configured capacity (the captured graphs are redone)
@@ -71,7 +82,7 @@ int BatchEngine::ensure(uint64_t samples, uint64_t pixels, uint32_t lights, uint
         if (e != cudaSuccess) return cuda_fail(c_, e, "batch buffer allocation");
     }
     if (jobs > job_cap_) {
-        cudaStreamSynchronize(c_->stream);
+        cudaStreamSynchronize(stream());
         cudaFree(d_jobs_);
         cudaFree(d_totals_);
         d_jobs_ = nullptr;
@@ -100,7 +111,7 @@ int BatchEngine::ensure(uint64_t samples, uint64_t pixels, uint32_t lights, uint
     {
         Ring& r = ring_[ring];  // the other ring may still hold frames to copy out
         if (stage_bytes > r.stage_cap) {
-            cudaStreamSynchronize(c_->stream);
+            cudaStreamSynchronize(stream());
             cudaFreeHost(r.h_stage);
             cudaFree(r.d_stage);
             r.h_stage = nullptr;
@@ -136,7 +147,7 @@ cudaError_t BatchEngine::launch_sequence(const WaveShape& shape, uint32_t* launc
     *used_graph = false;
     if (!use_graphs_ || c_->prof.on) {
         LaunchLog log = c_->prof.log();
-        cudaError_t e = run_beauty(p, buf_, t, c_->stream, c_->sm_count, &log);
+        cudaError_t e = run_beauty(p, buf_, t, stream(), c_->sm_count, &log);
         *launches += log.launches;
         return e;
     }
@@ -164,7 +175,7 @@ cudaError_t BatchEngine::launch_sequence(const WaveShape& shape, uint32_t* launc
     }
     *launches += it->second.launches;
     *used_graph = true;
-    return cudaGraphLaunch(it->second.exec, c_->stream);
+    return cudaGraphLaunch(it->second.exec, stream());
 }
 
 // Copy the host-output frames of a finished ring to their caller buffers.
@@ -195,7 +206,7 @@ int BatchEngine::run_wave(std::vector<PackedJob>& wave, const WaveShape& shape, 
         r.h_jobs[i] = pj.fj;
     }
     *r.h_totals = JobTotals{(uint32_t)wave.size(), (uint32_t)samples, (uint32_t)slots, (uint32_t)pixels};
-    cudaStream_t s = c_->stream;
+    cudaStream_t s = stream();
     cudaError_t e = cudaMemcpyAsync(d_jobs_, r.h_jobs, wave.size() * sizeof(FrameJob), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_totals_, r.h_totals, sizeof(JobTotals), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_fail(c_, e, "batch job table upload");
@@ -226,9 +237,7 @@ int BatchEngine::run_wave(std::vector<PackedJob>& wave, const WaveShape& shape, 
     return MM3E_OK;
 }
 
-int BatchEngine::render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats) {
-    auto t0 = std::chrono::steady_clock::now();
-    mm3e_batch_stats st{};
+int BatchEngine::launch_jobs(const mm3e_job* jobs, size_t n, mm3e_batch_stats& st, bool allow_host) {
     if (n && !jobs) return fail(c_, MM3E_ERR_INVALID, "null job array");
     const uint32_t wlog = c_->tune.tile_wlog;
     // validate and size every job first
@@ -248,7 +257,7 @@ int BatchEngine::render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats)
             return fail(c_, MM3E_ERR_INVALID, "job " + std::to_string(i) + ": dimensions must be 1..=16384");
         size_t px = j.format == MM3E_FB_RGBA8 ? 4 : 16;
         size_t bytes = (size_t)w * h * px;
-        void* out = j.device_out ? j.device_out : j.host_out;
+        void* out = j.device_out ? j.device_out : (allow_host ? j.host_out : nullptr);
         if (!out || j.out_bytes < bytes)
             return fail(c_, MM3E_ERR_INVALID, "job " + std::to_string(i) + ": output buffer too small");
         PackedJob& pj = packed[i];
@@ -262,14 +271,13 @@ int BatchEngine::render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats)
     if (largest > 0x7FFFFFFFull) return fail(c_, MM3E_ERR_INVALID, "job too large");
     uint64_t cap = std::max<uint64_t>(max_samples_, largest);
     cudaSetDevice(c_->device);
-    cudaEventRecord(c_->ev0, c_->stream);
     std::vector<PackedJob> wave;
     WaveShape shape;
     uint64_t samples = 0, slots = 0, pixels = 0;
     size_t stage = 0;
     int ring = 0;
     if (buf_.counters) {  // status word of the previous call
-        cudaError_t e = cudaMemsetAsync(buf_.counters + (N_COUNTERS - 1), 0, sizeof(uint32_t), c_->stream);
+        cudaError_t e = cudaMemsetAsync(buf_.counters + (N_COUNTERS - 1), 0, sizeof(uint32_t), stream());
         if (e != cudaSuccess) return cuda_fail(c_, e, "batch status");
     }
     auto emit = [&]() -> int {
@@ -308,10 +316,18 @@ int BatchEngine::render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats)
         shape.bloom = shape.bloom || (pj.fj.flags & JF_BLOOM);
         wave.push_back(pj);
     }
-    int rc = emit();
+    return emit();
+}
+
+int BatchEngine::render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    mm3e_batch_stats st{};
+    cudaSetDevice(c_->device);
+    cudaEventRecord(c_->ev0, stream());
+    int rc = launch_jobs(jobs, n, st, true);
     if (rc) return rc;
-    cudaEventRecord(c_->ev1, c_->stream);
-    rc = check_wave_status(c_, buf_.counters + (N_COUNTERS - 1));
+    cudaEventRecord(c_->ev1, stream());
+    rc = check_wave_status(c_, stream(), buf_.counters + (N_COUNTERS - 1));
     if (rc) return rc;
     for (int r = 0; r < 2; ++r) {
         rc = flush_ring(r);
@@ -326,6 +342,14 @@ int BatchEngine::render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats)
     }
     return MM3E_OK;
 }
+
+int BatchEngine::enqueue(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats) {
+    mm3e_batch_stats st{};
+    int rc = launch_jobs(jobs, n, st, false);
+    if (stats) *stats = st;
+    return rc;
+}
+
 
 }  // namespace mm3e
 

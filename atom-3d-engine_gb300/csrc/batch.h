@@ -37,16 +37,28 @@ struct PackedJob {
     size_t stage_offset;   // byte offset in the host staging area (host-output jobs)
 };
 
+int status_error(mm3e_ctx* c, uint32_t status_word);
+
 class BatchEngine {
   public:
-    explicit BatchEngine(mm3e_ctx* c);
+    // `stream` null: the context's current stream.
+    explicit BatchEngine(mm3e_ctx* c, cudaStream_t stream = nullptr);
     ~BatchEngine();
     int configure(const mm3e_batch_config& cfg);
+    // Renders and waits; host-output jobs are copied out before it returns.
     int render(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats);
+    // Enqueues the pass sequences of device-output jobs on the engine's stream and returns;
+    // the caller orders later work on the stream and reads status_word() afterwards.
+    int enqueue(const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats);
+    const uint32_t* status_word() const { return buf_.counters ? buf_.counters + (N_COUNTERS - 1) : nullptr; }
+    cudaStream_t stream() const { return s_ ? s_ : c_->stream; }
     // Bytes of device memory the engine holds.
     size_t device_bytes() const;
+    // Allocates the pass buffers for `samples` samples up front.
+    int reserve(uint64_t samples, uint32_t lights, uint32_t levels);
 
   private:
+    int launch_jobs(const mm3e_job* jobs, size_t n, mm3e_batch_stats& st, bool allow_host);
     int ensure(uint64_t samples, uint64_t pixels, uint32_t lights, uint32_t levels, size_t stage_bytes, uint32_t jobs,
                int ring);
     int run_wave(std::vector<PackedJob>& wave, const WaveShape& shape, uint64_t samples, uint64_t slots,
@@ -55,6 +67,7 @@ class BatchEngine {
     cudaError_t launch_sequence(const WaveShape& shape, uint32_t* launches, bool* used_graph);
 
     mm3e_ctx* c_;
+    cudaStream_t s_ = nullptr;
     uint64_t max_samples_ = 1ull << 24;
     bool use_graphs_ = true;
     PassBuffers buf_;

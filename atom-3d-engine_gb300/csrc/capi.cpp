@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <set>
 #include <string>
 #include <vector>
@@ -64,7 +65,11 @@ void SceneCopy::fix() {
 }
 
 int fail(mm3e_ctx* c, int code, const std::string& msg) {
-    if (c) c->err = msg;
+    static std::mutex mu;  // a server's worker and its clients may report errors concurrently
+    if (c) {
+        std::lock_guard<std::mutex> lk(mu);
+        c->err = msg;
+    }
     return code;
 }
 
@@ -121,6 +126,25 @@ FrameJob scene_job(const mm3e_scene* s, const unsigned char* tape, const mm3e_ca
     return j;
 }
 
+PassPlan plain_plan(const mm3e_scene* s, const mm3e_camera& cam, uint32_t w, uint32_t h, uint32_t format, void* dout,
+                    uint32_t wlog) {
+    const TapeHeader* hd = reinterpret_cast<const TapeHeader*>(s->low.blob.data());
+    PassPlan p;
+    p.job0 = scene_job(s, nullptr, cam, w, h, wlog);
+    p.job0.format = format;
+    p.job0.out = dout;
+    p.tape_bytes = (uint32_t)s->low.blob.size();
+    p.n_samples = p.job0.n_samples;
+    p.n_slots = p.job0.n_slots;
+    p.n_pixels = p.job0.n_pixels;
+    p.levels = s->low.bounces + 1;
+    p.lights_max = hd->n_lights;
+    p.ao = (hd->flags & SF_AO) && hd->ao_samples > 0;
+    p.shadows = (hd->flags & SF_SHADOWS) && hd->shadow_steps > 0 && hd->n_lights > 0;
+    p.bloom = (p.job0.flags & JF_BLOOM) != 0;
+    return p;
+}
+
 }  // namespace mm3e
 
 uint32_t mm3e_scene::n_lights() const {
@@ -128,7 +152,7 @@ uint32_t mm3e_scene::n_lights() const {
 }
 
 size_t mm3e_scene::device_bytes() const {
-    size_t b = tape_cap + dyn_cap + buf.bytes() + pixels * sizeof(float4);
+    size_t b = tape_cap + dyn_cap + buf.bytes() + (d_out ? pixels * sizeof(float4) : 0);
     for (const auto& p : low.payloads) b += p.bytes;
     return b;
 }
@@ -181,29 +205,38 @@ int upload_tape(mm3e_scene* s, const LoweredScene& low, unsigned char** dst, siz
     return MM3E_OK;
 }
 
-// Frame buffers of the scene for the context's tile shape.
-int ensure_frame_buffers(mm3e_scene* s) {
+// Frame buffers of the scene for the context's tile shape, allocated on the first frame (a
+// scene that is only rendered through batches or the server holds just its tape). `host`
+// also allocates the output framebuffer and pinned staging used by host-output calls.
+int ensure_frame_buffers(mm3e_scene* s, bool host) {
     mm3e_ctx* c = s->ctx;
     cudaError_t e;
     uint32_t wlog = c->tune.tile_wlog;
     size_t n = (size_t)s->low.width * s->low.height;
     size_t samples = slots_of(s->low.width, s->low.height, wlog) * s->low.aa * s->low.aa;
-    if (n != s->pixels || (n && !s->d_out)) {
+    if (n != s->pixels) {
         cudaFree(s->d_out);
         if (s->h_stage) cudaFreeHost(s->h_stage);
         s->d_out = nullptr;
         s->h_stage = nullptr;
         s->pixels = n;
-        if (n) {
-            e = cudaMalloc(reinterpret_cast<void**>(&s->d_out), n * sizeof(float4));
-            if (e != cudaSuccess) return cuda_fail(c, e, "frame buffer allocation");
-            e = cudaMallocHost(&s->h_stage, n * sizeof(float4));
-            if (e != cudaSuccess) return cuda_fail(c, e, "pinned staging allocation");
+    }
+    if (host && n && !s->d_out) {
+        e = cudaMalloc(reinterpret_cast<void**>(&s->d_out), n * sizeof(float4));
+        if (e != cudaSuccess) return cuda_fail(c, e, "frame buffer allocation");
+        e = cudaMallocHost(&s->h_stage, n * sizeof(float4));
+        if (e != cudaSuccess) {
+            cudaFree(s->d_out);
+            s->d_out = nullptr;
+            return cuda_fail(c, e, "pinned staging allocation");
         }
     }
-    e = s->buf.ensure(samples ? samples : 1, s->n_lights(), s->low.bounces + 1, n ? n : 1);
-    if (e != cudaSuccess) return cuda_fail(c, e, "pass buffer allocation");
-    s->buf_wlog = wlog;
+    if (!s->buf.counters || s->buf_wlog != wlog || s->buf.cap < samples || s->buf.pixels < n ||
+        s->buf.lights < s->n_lights() || s->buf.levels < s->low.bounces + 1) {
+        e = s->buf.ensure(samples ? samples : 1, s->n_lights(), s->low.bounces + 1, n ? n : 1);
+        if (e != cudaSuccess) return cuda_fail(c, e, "pass buffer allocation");
+        s->buf_wlog = wlog;
+    }
     return MM3E_OK;
 }
 
@@ -229,8 +262,6 @@ int relower(mm3e_scene* s) {
     s->low = std::move(low);
     rc = upload_tape(s, s->low, &s->d_tape, &s->tape_cap, true);
     if (rc) return rc;
-    rc = ensure_frame_buffers(s);
-    if (rc) return rc;
     return upload_post_kernel(s);
 }
 
@@ -255,20 +286,9 @@ int check_status(mm3e_scene* s) { return check_status(s->ctx, s->buf.counters + 
 // Single-job plan of one beauty frame of `s`.
 PassPlan scene_plan(mm3e_scene* s, const unsigned char* tape, uint32_t tape_bytes, const mm3e_camera& cam,
                     uint32_t format, void* dout) {
-    const TapeHeader* h = reinterpret_cast<const TapeHeader*>(s->low.blob.data());
-    PassPlan p;
-    p.job0 = scene_job(s, tape, cam, 0, 0, s->buf_wlog);
-    p.job0.format = format;
-    p.job0.out = dout;
+    PassPlan p = plain_plan(s, cam, 0, 0, format, dout, s->buf_wlog);
+    p.job0.tape = tape;
     p.tape_bytes = tape_bytes;
-    p.n_samples = p.job0.n_samples;
-    p.n_slots = p.job0.n_slots;
-    p.n_pixels = p.job0.n_pixels;
-    p.levels = s->low.bounces + 1;
-    p.lights_max = h->n_lights;
-    p.ao = (h->flags & SF_AO) && h->ao_samples > 0;
-    p.shadows = (h->flags & SF_SHADOWS) && h->shadow_steps > 0 && h->n_lights > 0;
-    p.bloom = (p.job0.flags & JF_BLOOM) != 0;
     return p;
 }
 
@@ -307,8 +327,8 @@ int render_to_device(mm3e_scene* s, const mm3e_camera* cam, const mm3e_dyn_spher
     const unsigned char* tape = s->d_tape;
     uint32_t tape_bytes = (uint32_t)s->low.blob.size();
     uint32_t mode = s->low.mode;
-    if (s->buf_wlog != c->tune.tile_wlog) {
-        int rc = ensure_frame_buffers(s);
+    {
+        int rc = ensure_frame_buffers(s, false);
         if (rc) return rc;
     }
     if (n_dyn > 0) {
@@ -641,6 +661,8 @@ int mm3e_render(mm3e_scene* s, const mm3e_camera* camera, const mm3e_dyn_sphere*
     int rc = validate_dynamic(s->src.d, dyn, n_dyn, err);
     if (rc) return fail(c, rc, err);
     cudaSetDevice(c->device);
+    rc = ensure_frame_buffers(s, true);
+    if (rc) return rc;
     LaunchLog log = c->prof.log();
     cudaEventRecord(c->ev0, c->stream);
     rc = render_to_device(s, camera, dyn, n_dyn, format, (void*)s->d_out, false, &log);
@@ -671,8 +693,10 @@ int mm3e_render_linear(mm3e_scene* s, const mm3e_camera* camera, float* host_rgb
     size_t n = (size_t)s->low.width * s->low.height;
     if (n && (!host_rgb || n_floats < 3 * n)) return fail(c, MM3E_ERR_INVALID, "output buffer too small");
     cudaSetDevice(c->device);
+    int rc = ensure_frame_buffers(s, true);
+    if (rc) return rc;
     LaunchLog log = c->prof.log();
-    int rc = render_to_device(s, camera, nullptr, 0, MM3E_FB_RGBA_F32, nullptr, true, &log);
+    rc = render_to_device(s, camera, nullptr, 0, MM3E_FB_RGBA_F32, nullptr, true, &log);
     if (rc) return rc;
     if (n) {
         cudaError_t e = cudaMemcpyAsync(s->h_stage, s->buf.hdr, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream);
@@ -700,13 +724,11 @@ int mm3e_render_device(mm3e_scene* s, const mm3e_camera* camera, uint32_t format
     LaunchLog log = c->prof.log();
     if (format == MM3E_FB_LINEAR_F32) {
         if (s->low.mode != MM3E_MODE_BEAUTY) return fail(c, MM3E_ERR_INVALID, "linear output needs beauty mode");
-        if (s->buf_wlog != c->tune.tile_wlog) {
-            int rc = ensure_frame_buffers(s);
-            if (rc) return rc;
-        }
+        int rc = ensure_frame_buffers(s, false);
+        if (rc) return rc;
         float4* keep = s->buf.hdr;
         s->buf.hdr = static_cast<float4*>(device_out);
-        int rc = render_to_device(s, camera, nullptr, 0, format, device_out, true, &log);
+        rc = render_to_device(s, camera, nullptr, 0, format, device_out, true, &log);
         s->buf.hdr = keep;
         return rc;
     }
@@ -840,7 +862,9 @@ int mm3e_render_hits(mm3e_scene* s, const mm3e_camera* camera, float* t, uint32_
     if (n == 0) return MM3E_OK;
     WaveArgs a;
     LaunchLog log = c->prof.log();
-    int rc = march_centers(s, camera, s->d_tape, (uint32_t)s->low.blob.size(), false, &log, a);
+    int rc = ensure_frame_buffers(s, false);
+    if (rc) return rc;
+    rc = march_centers(s, camera, s->d_tape, (uint32_t)s->low.blob.size(), false, &log, a);
     if (rc) return rc;
     return download_hits(c, s->buf, n, t, mat, steps, normal3);
 }

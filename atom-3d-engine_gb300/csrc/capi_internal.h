@@ -84,4 +84,8 @@ namespace mm3e {
 // A frame job of `s` (its tape, or `tape` when given) for `cam` at w x h (0: the scene's).
 FrameJob scene_job(const mm3e_scene* s, const unsigned char* tape, const mm3e_camera& cam, uint32_t w, uint32_t h,
                    uint32_t wlog);
+// The per-frame launch sequence's plan (one inline job, tape staged in shared memory) for a
+// beauty frame of `s` at w x h (0: the scene's) into device memory `dout`.
+PassPlan plain_plan(const mm3e_scene* s, const mm3e_camera& cam, uint32_t w, uint32_t h, uint32_t format, void* dout,
+                    uint32_t wlog);
 }  // namespace mm3e

@@ -121,6 +121,28 @@ class Context:
                    "unroll": rep[i].tuning.unroll}, rep[i].device_ms) for i in range(n.value)]
         return {"block": best.block, "tile_wlog": best.tile_wlog, "unroll": best.unroll}, table
 
+    # ---- mesh -> SDF bake -------------------------------------------------------------------------
+    def bake_mesh_sdf(self, positions, triangles, resolution, padding, device_out=None):
+        """mesh::bake_sdf on the GPU. Returns an SdfVolume (host samples), or, with `device_out`
+        (a device pointer with room for the grid), the grid (dims, min, cell) only."""
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+        tri = np.ascontiguousarray(triangles, np.uint32).reshape(-1)
+        m = abi.Mesh(pos.ctypes.data_as(C.POINTER(C.c_float)), len(pos) // 3,
+                     tri.ctypes.data_as(C.POINTER(C.c_uint32)), len(tri) // 3)
+        v = abi.Volume()
+        self.check(lib().mm3e_bake_mesh_sdf(self._ptr, C.byref(m), resolution, padding, C.byref(v), None, 0, 0))
+        n = v.nx * v.ny * v.nz
+        dims, vmin, cell = (v.nx, v.ny, v.nz), tuple(v.min), tuple(v.cell)
+        if device_out is not None:
+            self.check(lib().mm3e_bake_mesh_sdf(self._ptr, C.byref(m), resolution, padding, C.byref(v),
+                                                C.c_void_p(device_out), n, 1))
+            return dims, vmin, cell
+        data = np.zeros(n, np.float32)
+        self.check(lib().mm3e_bake_mesh_sdf(self._ptr, C.byref(m), resolution, padding, C.byref(v),
+                                            data.ctypes.data_as(C.c_void_p), n, 0))
+        from .scene import SdfVolume
+        return SdfVolume(dims, vmin, cell, data)
+
     def close(self):
         """Destroy the context; scenes compiled on it are destroyed first."""
         if self._ptr:
@@ -301,3 +323,88 @@ __all__ = [
     "Post", "Transform", "Expr", "SdfVolume", "GiVolume", "DynSphere", "look_at", "orbit_camera", "mat3_from_euler",
     "quat_to_mat3", "normalize_f32", "radians",
 ]
+
+
+class Server:
+    """The served form (mm3e_server): continuous batching of render requests on one GPU.
+
+    While a server runs on a Context, use the context only through the server."""
+
+    def __init__(self, ctx, hbm_budget_bytes=0, max_samples=0, max_inflight=0, use_graphs=True, plain=False):
+        self.ctx = ctx
+        self._ptr = C.c_void_p()
+        self._keep = {}  # request inputs that must outlive submission (ticket -> objects)
+        cfg = abi.ServerConfig(hbm_budget_bytes, max_samples, max_inflight, 1 if use_graphs else 0, 1 if plain else 0)
+        ctx.check(lib().mm3e_server_create(ctx.handle, C.byref(cfg), C.byref(self._ptr)))
+
+    def add_scene(self, scene):
+        sid = C.c_uint32()
+        h = scene.desc()
+        self.ctx.check(lib().mm3e_server_add_scene(self._ptr, h.ptr, C.byref(sid)))
+        return sid.value
+
+    @staticmethod
+    def request(camera, out, scene_id=0, new_scene=None, mesh=None, mesh_volume=0, mesh_resolution=128,
+                mesh_padding=0.1, width=0, height=0, fmt=abi.FB_RGBA8):
+        """A Request struct plus the objects it points to (keep them alive until completion).
+        `out`: host ndarray for the frame; `new_scene`: Scene; `mesh`: (positions, triangles)."""
+        r = abi.Request()
+        keep = [out]
+        r.scene_id = scene_id
+        if new_scene is not None:
+            h = new_scene.desc()
+            keep.append(h)
+            r.new_scene = C.pointer(h.desc)
+        if mesh is not None:
+            pos = np.ascontiguousarray(mesh[0], np.float32).reshape(-1)
+            tri = np.ascontiguousarray(mesh[1], np.uint32).reshape(-1)
+            m = abi.Mesh(pos.ctypes.data_as(C.POINTER(C.c_float)), len(pos) // 3,
+                         tri.ctypes.data_as(C.POINTER(C.c_uint32)), len(tri) // 3)
+            keep += [pos, tri, m]
+            r.mesh = C.pointer(m)
+            r.mesh_volume, r.mesh_resolution, r.mesh_padding = mesh_volume, mesh_resolution, mesh_padding
+        r.camera = camera
+        r.width, r.height, r.format = width, height, fmt
+        r.host_out = out.ctypes.data
+        r.out_bytes = out.nbytes
+        return r, keep
+
+    def submit(self, req, keep=None):
+        t = C.c_uint64()
+        self.ctx.check(lib().mm3e_server_submit(self._ptr, C.byref(req), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout_ms=0):
+        res = abi.RequestResult()
+        rc = lib().mm3e_server_wait(self._ptr, ticket, timeout_ms, C.byref(res))
+        if rc == abi.ERR_BUSY:
+            return None
+        return {"status": res.status, "scene_id": res.scene_id, "submit_ms": res.submit_ms,
+                "start_ms": res.start_ms, "done_ms": res.done_ms}
+
+    def stats(self):
+        st = abi.ServerStats()
+        self.ctx.check(lib().mm3e_server_get_stats(self._ptr, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in abi.ServerStats._fields_}
+
+    def replay(self, requests, arrivals_s):
+        """Open-loop replay of a Request array at the given arrival times (seconds)."""
+        n = len(requests)
+        arr = (abi.Request * n)(*requests)
+        times = (C.c_double * n)(*arrivals_s)
+        res = (abi.RequestResult * n)()
+        rc = lib().mm3e_server_replay(self._ptr, arr, times, n, res)
+        out = [{"status": r.status, "scene_id": r.scene_id, "submit_ms": r.submit_ms, "start_ms": r.start_ms,
+                "done_ms": r.done_ms} for r in res]
+        return rc, out
+
+    def close(self):
+        if self._ptr:
+            lib().mm3e_server_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

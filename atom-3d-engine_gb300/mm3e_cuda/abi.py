@@ -120,6 +120,35 @@ class BatchStats(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
 
 
+class Mesh(C.Structure):
+    _fields_ = [("positions", C.POINTER(C.c_float)), ("n_positions", C.c_uint32),
+                ("triangles", C.POINTER(C.c_uint32)), ("n_triangles", C.c_uint32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_samples", C.c_uint64), ("max_inflight", C.c_uint32),
+                ("use_graphs", C.c_uint32), ("plain", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("new_scene", C.POINTER(SceneDesc)), ("mesh", C.POINTER(Mesh)),
+                ("mesh_volume", C.c_uint32), ("mesh_resolution", C.c_uint32), ("mesh_padding", C.c_float),
+                ("camera", Camera), ("width", C.c_uint32), ("height", C.c_uint32), ("format", C.c_uint32),
+                ("host_out", C.c_void_p), ("out_bytes", C.c_size_t)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("scene_id", C.c_uint32), ("submit_ms", C.c_double), ("start_ms", C.c_double),
+                ("done_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "sequences", "frames_in_sequences",
+                                          "scenes_compiled", "scenes_evicted", "mesh_bakes", "mesh_bake_hits",
+                                          "admitted_bytes", "peak_admitted_bytes", "budget_bytes",
+                                          "reserved_bytes")]
+
+
 class TuneEntry(C.Structure):
     _fields_ = [("tuning", Tuning), ("device_ms", C.c_double)]
 
@@ -134,4 +163,7 @@ EXPORTED_SYMBOLS = [
     "mm3e_march_rays_noalloc",
     "mm3e_ctx_set_tuning", "mm3e_ctx_get_tuning", "mm3e_ctx_set_profiling", "mm3e_ctx_kernel_times",
     "mm3e_scene_device_bytes", "mm3e_batch_configure", "mm3e_render_batch", "mm3e_autotune",
+    "mm3e_bake_mesh_sdf",
+    "mm3e_server_create", "mm3e_server_add_scene", "mm3e_server_submit", "mm3e_server_wait", "mm3e_server_get_stats",
+    "mm3e_server_replay", "mm3e_server_destroy",
 ]

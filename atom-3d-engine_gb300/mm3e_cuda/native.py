@@ -70,6 +70,16 @@ def _declare_extra(lib):
         "mm3e_scene_device_bytes": (C.c_int, [C.c_void_p, P(C.c_size_t)]),
         "mm3e_batch_configure": (C.c_int, [C.c_void_p, P(abi.BatchConfig)]),
         "mm3e_render_batch": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, P(abi.BatchStats)]),
+        "mm3e_bake_mesh_sdf": (C.c_int, [C.c_void_p, P(abi.Mesh), C.c_uint32, C.c_float, P(abi.Volume),
+                                         C.c_void_p, C.c_size_t, C.c_int]),
+        "mm3e_server_create": (C.c_int, [C.c_void_p, P(abi.ServerConfig), P(C.c_void_p)]),
+        "mm3e_server_add_scene": (C.c_int, [C.c_void_p, P(abi.SceneDesc), P(C.c_uint32)]),
+        "mm3e_server_submit": (C.c_int, [C.c_void_p, P(abi.Request), P(C.c_uint64)]),
+        "mm3e_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, P(abi.RequestResult)]),
+        "mm3e_server_get_stats": (C.c_int, [C.c_void_p, P(abi.ServerStats)]),
+        "mm3e_server_replay": (C.c_int, [C.c_void_p, P(abi.Request), P(C.c_double), C.c_size_t,
+                                         P(abi.RequestResult)]),
+        "mm3e_server_destroy": (None, [C.c_void_p]),
         "mm3e_autotune": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, C.c_uint32, P(abi.Tuning),
                                     P(abi.TuneEntry), C.c_uint32, P(C.c_uint32)]),
     }

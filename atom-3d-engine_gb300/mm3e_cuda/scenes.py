@@ -407,3 +407,122 @@ def reference_gi_demo_scene():
     s.light(Light.sphere((0.0, 3.7, 0.0), (14.0, 14.0, 14.0), 1.2))
     cam = look_at((0.0, 2.0, 7.5), (0.0, 1.6, 0.0), (0.0, 1.0, 0.0), radians(50.0))
     return s, cam
+
+
+# ------------------------------------------------------------------------------------------
+# Meshes for the mesh -> SDF bake (the served stream's mesh requests). The reference has no
+# icosphere or noise generator; these are seeded generators of this package.
+# ------------------------------------------------------------------------------------------
+def uv_sphere_mesh(rings, segments, radius):
+    """UV sphere with poles, as the reference's engine tests build it (tests/engine.rs:370-401):
+    (positions (n, 3) f32, triangles (m, 3) u32)."""
+    pos = [(0.0, radius, 0.0)]
+    for r in range(1, rings):
+        phi = np.float32(math.pi) * np.float32(r) / np.float32(rings)
+        for s in range(segments):
+            theta = np.float32(2.0 * math.pi) * np.float32(s) / np.float32(segments)
+            pos.append((radius * np.sin(phi) * np.cos(theta), radius * np.cos(phi), radius * np.sin(phi) * np.sin(theta)))
+    pos.append((0.0, -radius, 0.0))
+
+    def ring(r, s):
+        return 1 + (r - 1) * segments + (s % segments)
+
+    tris = [(0, ring(1, s + 1), ring(1, s)) for s in range(segments)]
+    for r in range(1, rings - 1):
+        for s in range(segments):
+            a, b, c, d = ring(r, s), ring(r, s + 1), ring(r + 1, s + 1), ring(r + 1, s)
+            tris += [(a, b, c), (a, c, d)]
+    south = len(pos) - 1
+    tris += [(south, ring(rings - 1, s), ring(rings - 1, s + 1)) for s in range(segments)]
+    return np.asarray(pos, np.float32), np.asarray(tris, np.uint32)
+
+
+def icosphere(subdivisions):
+    """Unit icosphere: the icosahedron with every triangle split into four `subdivisions` times,
+    new vertices projected to the sphere. 10*4^n + 2 vertices, 20*4^n triangles."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [tuple(np.asarray(v, np.float64) / np.linalg.norm(v)) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = (np.asarray(verts[a]) + np.asarray(verts[b])) * 0.5
+                verts.append(tuple(m / np.linalg.norm(m)))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.asarray(verts, np.float64), np.asarray(faces, np.uint32)
+
+
+def value_noise3(p, seed):
+    """Seeded 3-D value noise in [-1, 1]: hashed lattice values, smoothstep-weighted trilinear
+    blend. p: (n, 3) float64."""
+    p = np.asarray(p, np.float64)
+    i0 = np.floor(p).astype(np.int64)
+    f = p - i0
+    w = f * f * (3.0 - 2.0 * f)
+
+    def lattice(ix, iy, iz):
+        h = (ix * 73856093) ^ (iy * 19349663) ^ (iz * 83492791) ^ (seed * 2654435761)
+        h = (h ^ (h >> 13)) * 1274126177
+        h = h ^ (h >> 16)
+        return (h & 0xFFFF).astype(np.float64) / 32767.5 - 1.0
+
+    out = 0.0
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                wx = w[:, 0] if dx else 1.0 - w[:, 0]
+                wy = w[:, 1] if dy else 1.0 - w[:, 1]
+                wz = w[:, 2] if dz else 1.0 - w[:, 2]
+                out = out + wx * wy * wz * lattice(i0[:, 0] + dx, i0[:, 1] + dy, i0[:, 2] + dz)
+    return out
+
+
+def displaced_icosphere(seed, subdivisions=5, amplitude=0.15, octaves=3, frequency=2.0, radius=1.0):
+    """Icosphere (subdivision 5: 20,480 triangles) displaced radially by `octaves`-octave value
+    noise of amplitude `amplitude`: (positions f32 (n, 3), triangles u32 (m, 3))."""
+    v, f = icosphere(subdivisions)
+    n = np.zeros(len(v))
+    amp, freq, norm = 1.0, frequency, 0.0
+    for o in range(octaves):
+        n += amp * value_noise3(v * freq, seed * 131 + o)
+        norm += amp
+        amp *= 0.5
+        freq *= 2.0
+    r = radius * (1.0 + amplitude * n / norm)
+    return (v * r[:, None]).astype(np.float32), f
+
+
+def mesh_volume_scene(volume, seed=0, width=512, height=512):
+    """A served-stream scene around a baked mesh volume: the volume object on a ground plane,
+    config-1 shading, orbit camera."""
+    rng = np.random.default_rng(seed)
+    s = Scene(width, height)
+    s.aa = 1
+    s.bounces = 0
+    s.marcher.max_steps = 128
+    s.marcher.eps = float(F32(1e-3))
+    s.marcher.max_dist = 100.0
+    s.marcher.normal_h = volume.recommended_normal_h()
+    grey = s.material(Material.solid((0.8, 0.8, 0.8)))
+    mat = s.material(Material.solid(tuple(rng.uniform(0.2, 0.9, 3)), roughness=0.5))
+    vid = s.volume(volume)
+    s.add(Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, grey))
+    s.add(Object(Prim.volume(vid), Transform.at((0.0, 1.2, 0.0)), mat))
+    s.light(directional((0.4, 0.8, -0.45), (1.0, 1.0, 1.0)).soft(1.0 / 16.0))
+    s.ambient = (0.08, 0.08, 0.1)
+    cam = orbit_camera((0.0, 1.0, 0.0), 4.5, float(rng.uniform(-math.pi, math.pi)), 0.35, math.radians(45.0))
+    return s, cam

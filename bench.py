@@ -65,7 +65,188 @@ def parse():
                     help="only render this many frames of the workload (no timing, no JSON line): the "
                          "command profilers run")
     ap.add_argument("--size", default=None, help="WxH resolution override (with --profile-frames)")
+    ap.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched-form measurement")
+    ap.add_argument("--served-seconds", type=float, default=2.0,
+                    help="arrival window per rate of the served-form measurement (the full spec is 60)")
+    ap.add_argument("--served-max-requests", type=int, default=2000,
+                    help="cap on requests per rate (the arrival window shrinks to fit)")
+    ap.add_argument("--no-forms", action="store_true", help="skip the Cornell / batched / served measurements")
     return ap.parse_args()
+
+
+def _pct(v, q):
+    import numpy as np
+
+    return float(np.percentile(np.asarray(v, np.float64), q)) if len(v) else None
+
+
+def bench_cornell(ctx, stream, torch):
+    """Cornell GI room at 1920x1080: GPU probe bake (32^3 ambient cubes, 5 rays per face) from the
+    tape, then frames through the plain call (L2 flushed between frames)."""
+    from mm3e_cuda import abi, scenes
+
+    import mm3e_cuda
+
+    s, cam = scenes.cornell_scene(1920, 1080)
+    cs = mm3e_cuda.CompiledScene(ctx, s)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    cs.bake_gi((32, 32, 32), 5)  # warm-up (first-use allocations)
+    t0 = time.perf_counter()
+    cs.bake_gi((32, 32, 32), 5)
+    bake_s = time.perf_counter() - t0
+    out = torch.empty(1920 * 1080 * 4, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        cs.render_device(cam, abi.FB_RGBA8, out.data_ptr(), out.numel())
+    ms = []
+    with torch.cuda.stream(stream):
+        for i in range(10):
+            flush.fill_(float(i))
+            ev[0].record(stream)
+            cs.render_device(cam, abi.FB_RGBA8, out.data_ptr(), out.numel())
+            ev[1].record(stream)
+            stream.synchronize()
+            ms.append(ev[0].elapsed_time(ev[1]))
+    cs.close()
+    return {"workload": "cornell_gi_1080p", "frames_per_s": 1000.0 / statistics.median(ms),
+            "frame_ms_median": statistics.median(ms), "gi_probes": "32^3 ambient cubes, 5 rays per face",
+            "gi_bake_ms_host_wall": bake_s * 1000.0, "gi_bake_rays": 32 ** 3 * 6 * 5}
+
+
+def bench_batched(ctx, stream, torch, n_scenes):
+    """Batched form: n seeded procedural scenes (8-64 primitives, random CSG, mixed resolutions
+    256^2 / 512^2 / 1280x720 / 1920x1080, orbit cameras) rendered as one batch (autotuned launch
+    shape, CUDA-graph pass sequences) vs the plain per-frame call of every scene in turn."""
+    from mm3e_cuda import abi, scenes
+
+    import mm3e_cuda
+
+    items = [scenes.procedural_scene(seed) for seed in range(n_scenes)]
+    compiled = [mm3e_cuda.CompiledScene(ctx, s) for s, _ in items]
+    outs = [torch.empty(s.width * s.height * 4, dtype=torch.uint8, device="cuda") for s, _ in items]
+    pixels = sum(s.width * s.height for s, _ in items)
+    jobs = ctx.make_jobs([(c, cam, 0, 0, abi.FB_RGBA8, o.data_ptr(), None)
+                          for c, (s, cam), o in zip(compiled, items, outs)])
+    ctx.configure_batch(max_samples=1 << 24, use_graphs=True)
+    t0 = time.perf_counter()
+    best, table = ctx.autotune(ctx.make_jobs([(c, cam, 0, 0, abi.FB_RGBA8, o.data_ptr(), None)
+                                              for c, (s, cam), o in list(zip(compiled, items, outs))[:32]]))
+    tune_s = time.perf_counter() - t0
+    ctx.render_batch(jobs)  # warm-up: graphs captured, buffers grown
+    batch_ms, stats = [], None
+    for _ in range(3):
+        stats = ctx.render_batch(jobs)
+        batch_ms.append(stats["device_ms"])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for c, (s, cam), o in zip(compiled, items, outs):  # warm-up: per-scene buffers
+        c.render_device(cam, abi.FB_RGBA8, o.data_ptr(), o.numel())
+    ctx.sync()
+    plain_ms = []
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            ev[0].record(stream)
+            for c, (s, cam), o in zip(compiled, items, outs):
+                c.render_device(cam, abi.FB_RGBA8, o.data_ptr(), o.numel())
+            ev[1].record(stream)
+            stream.synchronize()
+            plain_ms.append(ev[0].elapsed_time(ev[1]))
+    b = statistics.median(batch_ms)
+    p = statistics.median(plain_ms)
+    for c in compiled:
+        c.close()
+    return {"workload": f"procedural_batch_{n_scenes}", "frames": n_scenes, "pixels": pixels,
+            "batched_frames_per_s": n_scenes * 1000.0 / b, "batched_mrays_per_s_primary": pixels / b / 1e3,
+            "plain_frames_per_s": n_scenes * 1000.0 / p, "batched_over_plain": p / b,
+            "batch_ms": b, "plain_ms": p, "sequences": stats["sequences"],
+            "kernel_launches": stats["kernel_launches"], "graph_launches": stats["graph_launches"],
+            "tuning": best, "autotune_s": tune_s, "autotune_table": table}
+
+
+def bench_served(ctx_factory, seconds, max_requests, rates=(200, 1000, 5000), seed=7):
+    """Served form: Poisson arrivals at each rate; 70% camera updates of resident procedural
+    scenes, 20% new procedural scenes, 10% scenes around a 128^3 grid baked on the GPU from a
+    seeded displaced icosphere (subdivision 5); HBM budget 40 GB. The same trace replayed through
+    the continuous-batching server and through the plain per-request launch (one at a time)."""
+    import numpy as np
+
+    import mm3e_cuda
+    from mm3e_cuda import scenes
+    from mm3e_cuda.scene import SdfVolume, orbit_camera
+
+    rng = np.random.default_rng(seed)
+    resident = [scenes.procedural_scene(1000 + i) for i in range(64)]
+    fresh = [scenes.procedural_scene(5000 + i) for i in range(32)]
+    meshes = [scenes.displaced_icosphere(k, 5) for k in range(4)]
+    placeholder = SdfVolume((2, 2, 2), (0, 0, 0), (1, 1, 1), np.zeros(8, np.float32))
+    mesh_scenes = []
+    for k in range(4):
+        s, cam = scenes.mesh_volume_scene(placeholder, seed=k, width=512, height=512)
+        s.marcher.normal_h = 0.02
+        mesh_scenes.append((s, cam))
+    bufs = {}
+
+    def out_for(w, h):
+        lst = bufs.setdefault((w, h), [np.zeros((h, w, 4), np.uint8) for _ in range(4)])
+        return lst[int(rng.integers(0, len(lst)))]
+
+    results = {}
+    for rate in rates:
+        n = int(min(max_requests, rate * seconds))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+        kinds = rng.random(n)
+        plan = []
+        for i in range(n):
+            if kinds[i] < 0.7:
+                j = int(rng.integers(0, len(resident)))
+                s, _ = resident[j]
+                cam = orbit_camera((0.0, 0.0, 0.0), float(rng.uniform(9, 15)), float(rng.uniform(-3.1, 3.1)),
+                                   float(rng.uniform(0.1, 0.7)), 0.8)
+                plan.append(("resident", j, cam, s.width, s.height))
+            elif kinds[i] < 0.9:
+                j = int(rng.integers(0, len(fresh)))
+                plan.append(("new", j, fresh[j][1], fresh[j][0].width, fresh[j][0].height))
+            else:
+                j = int(rng.integers(0, len(mesh_scenes)))
+                plan.append(("mesh", j, mesh_scenes[j][1], 512, 512))
+        row = {"requests": n, "arrival_window_s": float(arrivals[-1]) if n else 0.0}
+        for mode in ("batched", "plain"):
+            ctx = ctx_factory()
+            srv = mm3e_cuda.Server(ctx, hbm_budget_bytes=40 << 30, plain=(mode == "plain"))
+            try:
+                ids = [srv.add_scene(s) for s, _ in resident]
+                reqs, keep = [], []
+                for kind, j, cam, w, h in plan:
+                    out = out_for(w, h)
+                    if kind == "resident":
+                        r, k = srv.request(cam, out, scene_id=ids[j])
+                    elif kind == "new":
+                        r, k = srv.request(cam, out, new_scene=fresh[j][0])
+                    else:
+                        pos, tri = meshes[j]
+                        r, k = srv.request(cam, out, new_scene=mesh_scenes[j][0], mesh=(pos, tri), mesh_volume=0,
+                                           mesh_resolution=128, mesh_padding=0.1)
+                    reqs.append(r)
+                    keep.append(k)
+                rc, res = srv.replay(reqs, list(arrivals))
+                st = srv.stats()
+            finally:
+                srv.close()
+                ctx.close()
+            ok = [r for r in res if r["status"] == 0]
+            lat = [r["done_ms"] - r["submit_ms"] for r in ok]
+            span = (max(r["done_ms"] for r in ok) - min(r["submit_ms"] for r in ok)) / 1000.0 if ok else 0.0
+            row[mode] = {"completed": len(ok), "failed": n - len(ok), "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
+                         "mean_ms": float(np.mean(lat)) if lat else None,
+                         "frames_per_s": len(ok) / span if span > 0 else None,
+                         "sequences": st["sequences"], "frames_per_sequence":
+                             st["frames_in_sequences"] / max(1, st["sequences"]),
+                         "mesh_bakes": st["mesh_bakes"], "scenes_compiled": st["scenes_compiled"],
+                         "peak_admitted_bytes": st["peak_admitted_bytes"], "reserved_bytes": st["reserved_bytes"]}
+        if row["batched"]["frames_per_s"] and row["plain"]["frames_per_s"]:
+            row["batched_over_plain_frames_per_s"] = row["batched"]["frames_per_s"] / row["plain"]["frames_per_s"]
+        results[str(rate)] = row
+    return {"workload": "served_poisson", "rates_per_s": list(rates), "hbm_budget_bytes": 40 << 30,
+            "arrival_window_s": seconds, "max_requests_per_rate": max_requests, "by_rate": results}
 
 
 def run_profile_frames(args):
@@ -324,6 +505,11 @@ def run_ours(args):
     if cpu:
         line["speedup_vs_cpu"] = value / cpu["value"]
         line["e2e_speedup_vs_cpu"] = e2e_value / cpu["value"]
+    if not args.no_forms and world == 1:
+        line["cornell"] = bench_cornell(ctx, stream, torch)
+        line["batched"] = bench_batched(ctx, stream, torch, args.batch_scenes)
+        ctx.set_stream(None)
+        line["served"] = bench_served(lambda: mm3e_cuda.Context(local), args.served_seconds, args.served_max_requests)
     print(json.dumps(line))
     ctx.close()
 

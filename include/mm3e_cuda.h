@@ -338,6 +338,25 @@ int mm3e_bake_gi(mm3e_scene* scene, uint32_t nx, uint32_t ny, uint32_t nz, uint3
 int mm3e_scene_get_gi(mm3e_scene* scene, float min[3], float size[3], uint32_t dims[3], float* cubes,
                       size_t n_floats);
 
+/* ---- mesh -> SDF bake --------------------------------------------------------------------- */
+/* An indexed triangle mesh (mesh.rs Mesh): positions xyz, triangles as 3 vertex indices. */
+typedef struct mm3e_mesh {
+    const float* positions;
+    uint32_t n_positions;
+    const uint32_t* triangles;
+    uint32_t n_triangles;
+} mm3e_mesh;
+/* mesh::bake_sdf (mesh.rs:262-336) on the GPU: `resolution` samples along the longest padded
+ * axis (clamped to 2..=512), `padding` > 0 around the mesh bounds. Fills out->nx/ny/nz, min,
+ * cell; with `data` NULL only the grid is computed (query its size first). `data` receives
+ * nx*ny*nz samples, (k*ny + j)*nx + i, in host memory (out->data is then set to it) or, with
+ * data_on_device, in device memory. The samples equal the reference's: exact nearest-triangle
+ * distance from the same BVH walk, sign from binary64 row-parity crossings. Errors carry the
+ * reference's messages (no vertices / triangles, non-finite vertex, index out of range, bad
+ * padding, only degenerate triangles). Blocking. */
+int mm3e_bake_mesh_sdf(mm3e_ctx* ctx, const mm3e_mesh* mesh, uint32_t resolution, float padding, mm3e_volume* out,
+                       float* data, size_t n_floats, int data_on_device);
+
 /* ---- diagnostics: primary hits, arbitrary rays, field samples ------------------------------- */
 /* Primary pinhole ray through every pixel centre (the ray RenderMode AOVs and the pinhole film
  * use, lib.rs:1179): hit distance t, material id (0xFFFFFFFF on a miss), march steps and the
@@ -395,6 +414,68 @@ typedef struct mm3e_tune_entry {
 } mm3e_tune_entry;
 int mm3e_autotune(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, uint32_t repeats, mm3e_tuning* best,
                   mm3e_tune_entry* report, uint32_t report_cap, uint32_t* n_report);
+
+/* ---- served form ----------------------------------------------------------------------------- */
+/* A request loop with continuous batching: client threads submit requests, one worker thread
+ * owns the device work. Scene tapes and payloads stay resident; requests are admitted against
+ * an HBM budget and coalesced in arrival order into pass sequences on `max_inflight` slots
+ * (own stream and buffers each), so requests arriving while others run start as soon as a
+ * slot frees. While a server runs on a context, use that context only through the server. */
+typedef struct mm3e_server mm3e_server;
+
+typedef struct mm3e_server_config {
+    uint64_t hbm_budget_bytes; /* resident scenes + slot buffers + admitted frames; 0 = 40 GiB */
+    uint64_t max_samples;      /* samples per pass sequence; 0 = 2^23 */
+    uint32_t max_inflight;     /* pass sequences on the GPU at once, 1..4; 0 = 2 */
+    uint32_t use_graphs;       /* replay pass sequences from captured CUDA graphs */
+    uint32_t plain;            /* 1: no coalescing; one request at a time through the per-frame
+                                  launch sequence (the plain baseline) */
+} mm3e_server_config;
+
+typedef struct mm3e_request {
+    uint32_t scene_id;                /* a resident scene (when new_scene is NULL) */
+    const mm3e_scene_desc* new_scene; /* or a new scene: copied at submit, compiled, kept resident */
+    const mm3e_mesh* mesh;            /* with new_scene: baked (mm3e_bake_mesh_sdf) into volume
+                                         `mesh_volume` of the new scene before it is compiled;
+                                         bakes are cached by mesh content */
+    uint32_t mesh_volume, mesh_resolution;
+    float mesh_padding;
+    mm3e_camera camera;
+    uint32_t width, height; /* 0: the scene's size */
+    uint32_t format;        /* MM3E_FB_RGBA8 or MM3E_FB_RGBA_F32 */
+    void* host_out;         /* receives the frame; must stay valid until the request completes */
+    size_t out_bytes;
+} mm3e_request;
+
+typedef struct mm3e_request_result {
+    int status;        /* MM3E_OK or the request's error code */
+    uint32_t scene_id; /* scene rendered (new scenes are given an id) */
+    double submit_ms;  /* server clock, ms: arrival (replay: the scheduled arrival) */
+    double start_ms;   /* its pass sequence was launched */
+    double done_ms;    /* its frame was in host memory */
+} mm3e_request_result;
+
+typedef struct mm3e_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t sequences, frames_in_sequences;
+    uint64_t scenes_compiled, scenes_evicted, mesh_bakes, mesh_bake_hits;
+    uint64_t admitted_bytes, peak_admitted_bytes, budget_bytes;
+    uint64_t reserved_bytes; /* pass-sequence slot buffers, allocated when the server starts */
+} mm3e_server_stats;
+
+int mm3e_server_create(mm3e_ctx* ctx, const mm3e_server_config* cfg, mm3e_server** out);
+/* Compiles `desc` and keeps it resident; blocking. */
+int mm3e_server_add_scene(mm3e_server* srv, const mm3e_scene_desc* desc, uint32_t* scene_id);
+int mm3e_server_submit(mm3e_server* srv, const mm3e_request* req, uint64_t* ticket);
+/* Waits up to timeout_ms (0: forever) for the request; MM3E_ERR_BUSY if it has not completed. */
+int mm3e_server_wait(mm3e_server* srv, uint64_t ticket, uint32_t timeout_ms, mm3e_request_result* result);
+int mm3e_server_get_stats(mm3e_server* srv, mm3e_server_stats* stats);
+/* Open-loop load replay: a driver thread submits reqs[i] at arrival_s[i] seconds after the
+ * call starts; returns when all completed. results[i] times are ms since the call started. */
+int mm3e_server_replay(mm3e_server* srv, const mm3e_request* reqs, const double* arrival_s, size_t n,
+                       mm3e_request_result* results);
+/* Waits for every submitted request, then frees the server and its resident scenes. */
+void mm3e_server_destroy(mm3e_server* srv);
 
 /* ---- allocation-free ray queries --------------------------------------------------------- */
 /* No counterpart in the reference: an addition for callers that cannot allocate device memory

@@ -8,6 +8,7 @@
 #include <mutex>
 
 #include "oracle_count.hpp"
+#include "oracle_mesh.hpp"
 #include "oracle_scene.hpp"
 
 using namespace oracle;
@@ -359,6 +360,54 @@ double oracle_time_rows(const mm3e_scene_desc* d, const mm3e_camera* cam, uint32
     render_linear_rows(s, cam_from<float>(*cam), y0, y1, threads, rows.data());
     auto t1 = std::chrono::steady_clock::now();
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+
+// mesh.rs bake_sdf: positions (3 floats each), triangles (3 indices each). Writes the grid dims,
+// min corner and cell; `data` (nx*ny*nz floats) may be NULL to query the grid only. Returns 0,
+// or -1 with the reference's error message in `err`.
+int oracle_bake_mesh_sdf(const float* positions, uint32_t n_positions, const uint32_t* triangles, uint32_t n_triangles,
+                         uint32_t resolution, float padding, unsigned threads, uint32_t* dims, float* min3, float* cell3,
+                         float* data, size_t n_floats, char* err, size_t err_len) {
+    oracle::mesh::Mesh m;
+    m.pos.resize(n_positions);
+    for (uint32_t i = 0; i < n_positions; ++i)
+        m.pos[i] = oracle::mesh::F3{positions[3 * i], positions[3 * i + 1], positions[3 * i + 2]};
+    m.tri.assign(triangles, triangles + 3 * (size_t)n_triangles);
+    oracle::mesh::Grid g{};
+    std::string e;
+    std::vector<float> vol;
+    if (data) e = oracle::mesh::bake_sdf(m, resolution, padding, g, vol, threads);
+    else e = oracle::mesh::bake_grid(m, resolution, padding, g);
+    if (!e.empty()) {
+        if (err && err_len) {
+            std::strncpy(err, e.c_str(), err_len - 1);
+            err[err_len - 1] = 0;
+        }
+        return -1;
+    }
+    dims[0] = g.nx;
+    dims[1] = g.ny;
+    dims[2] = g.nz;
+    min3[0] = g.lo.x;
+    min3[1] = g.lo.y;
+    min3[2] = g.lo.z;
+    cell3[0] = g.cell.x;
+    cell3[1] = g.cell.y;
+    cell3[2] = g.cell.z;
+    if (data) {
+        if (n_floats < vol.size()) return -2;
+        std::memcpy(data, vol.data(), vol.size() * sizeof(float));
+    }
+    return 0;
+}
+
+// triangle.rs x_crossing: 1 and *x when the X-directed line at (y, z) crosses the triangle.
+int oracle_x_crossing(const float* a, const float* b, const float* c, float y, float z, float* x) {
+    return oracle::mesh::x_crossing(oracle::mesh::F3{a[0], a[1], a[2]}, oracle::mesh::F3{b[0], b[1], b[2]},
+                                    oracle::mesh::F3{c[0], c[1], c[2]}, y, z, *x)
+               ? 1
+               : 0;
 }
 
 }  // extern "C"

@@ -41,6 +41,10 @@ def lib():
         l.oracle_aces.argtypes = [P(C.c_float), P(C.c_float)]
         l.oracle_field.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_int, P(C.c_float), P(C.c_uint32)]
         l.oracle_count_frame.argtypes = [vp, vp, C.c_uint, P(C.c_uint64)]
+        l.oracle_bake_mesh_sdf.argtypes = [P(C.c_float), C.c_uint32, P(C.c_uint32), C.c_uint32, C.c_uint32, C.c_float,
+                                           C.c_uint, P(C.c_uint32), P(C.c_float), P(C.c_float), P(C.c_float),
+                                           C.c_size_t, C.c_char_p, C.c_size_t]
+        l.oracle_x_crossing.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_float, C.c_float, P(C.c_float)]
         l.oracle_count_frame_blocks.argtypes = [vp, vp, C.c_uint, P(C.c_uint64), C.c_int]
         l.oracle_bake_gi.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint, P(C.c_float),
                                      P(C.c_float), P(C.c_uint32), P(C.c_float)]
@@ -211,3 +215,37 @@ def gi_sample(handle, pts, nrm):
 
 def time_rows(handle, cam, y0, y1, threads=None):
     return lib().oracle_time_rows(C.addressof(handle.desc), C.addressof(cam), y0, y1, threads or threads_default())
+
+
+def bake_mesh_sdf(positions, triangles, resolution, padding, threads=None, grid_only=False):
+    """mesh.rs bake_sdf: (dims (nx, ny, nz), min, cell, data (nz, ny, nx) or None). Raises
+    ValueError with the reference's message on invalid input."""
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+    tri = np.ascontiguousarray(triangles, np.uint32).reshape(-1)
+    dims = np.zeros(3, np.uint32)
+    mn = np.zeros(3, np.float32)
+    cell = np.zeros(3, np.float32)
+    err = C.create_string_buffer(256)
+    l = lib()
+    rc = l.oracle_bake_mesh_sdf(_f(pos), len(pos) // 3, tri.ctypes.data_as(P(C.c_uint32)), len(tri) // 3,
+                                resolution, padding, threads or threads_default(),
+                                dims.ctypes.data_as(P(C.c_uint32)), _f(mn), _f(cell), None, 0, err, 256)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    if grid_only:
+        return tuple(int(d) for d in dims), mn, cell, None
+    data = np.zeros(int(dims[0]) * int(dims[1]) * int(dims[2]), np.float32)
+    rc = l.oracle_bake_mesh_sdf(_f(pos), len(pos) // 3, tri.ctypes.data_as(P(C.c_uint32)), len(tri) // 3,
+                                resolution, padding, threads or threads_default(),
+                                dims.ctypes.data_as(P(C.c_uint32)), _f(mn), _f(cell), _f(data), data.size, err, 256)
+    if rc != 0:
+        raise ValueError(err.value.decode())
+    return tuple(int(d) for d in dims), mn, cell, data.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
+
+
+def x_crossing(a, b, c, y, z):
+    """triangle.rs x_crossing: the crossing x (float) or None."""
+    x = C.c_float()
+    fa, fb, fc = (np.ascontiguousarray(v, np.float32) for v in (a, b, c))
+    ok = lib().oracle_x_crossing(_f(fa), _f(fb), _f(fc), y, z, C.byref(x))
+    return x.value if ok else None
