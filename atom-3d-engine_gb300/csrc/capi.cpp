@@ -19,6 +19,7 @@
 #include "batch.h"
 #include "capi_internal.h"
 #include "noalloc.h"
+#include "spec.h"
 
 using namespace mm3e;
 
@@ -157,8 +158,11 @@ size_t mm3e_scene::device_bytes() const {
     return b;
 }
 
+const SpecKernels* mm3e_scene::spec_kernels() const { return spec ? &spec->kernels : nullptr; }
+
 mm3e_scene::~mm3e_scene() {
     if (ctx) cudaSetDevice(ctx->device);
+    spec.reset();
     cudaFree(d_tape);
     cudaFree(d_dyn_tape);
     for (void* p : d_payloads) cudaFree(p);
@@ -260,6 +264,7 @@ int relower(mm3e_scene* s) {
     int rc = lower_scene(s->src.d, nullptr, 0, low, err);
     if (rc) return fail(s->ctx, rc, err);
     s->low = std::move(low);
+    s->spec.reset();  // compiled for the previous tape
     rc = upload_tape(s, s->low, &s->d_tape, &s->tape_cap, true);
     if (rc) return rc;
     return upload_post_kernel(s);
@@ -314,8 +319,9 @@ int march_centers(mm3e_scene* s, const mm3e_camera* cam, const unsigned char* ta
     a.src = SRC_CENTER;
     a.n_items = n;
     a.counter = s->buf.counters;
-    CK(launch_march(a, c->tune, c->stream, c->sm_count, log));
-    if (want_ao) CK(launch_ao(a, c->stream, log));
+    const SpecKernels* sp = tape == s->d_tape ? s->spec_kernels() : nullptr;
+    CK(launch_march(a, c->tune, c->stream, c->sm_count, log, sp));
+    if (want_ao) CK(launch_ao(a, c->stream, log, sp));
     return MM3E_OK;
 }
 
@@ -345,9 +351,7 @@ int render_to_device(mm3e_scene* s, const mm3e_camera* cam, const mm3e_dyn_spher
     if ((size_t)w * h == 0) return MM3E_OK;
     if (mode == MM3E_MODE_BEAUTY || linear_only) {
         PassPlan p = scene_plan(s, tape, tape_bytes, *cam, format, dout);
-        if (n_dyn > 0) {  // dynamic spheres add no lights; AO / shadow flags are the scene's
-            p.job0.n_lights = p.lights_max;
-        }
+        if (n_dyn == 0) p.spec = s->spec_kernels();  // the specialised field is the scene's own tape
         p.post = !linear_only;
         CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, log));
         return MM3E_OK;
@@ -932,6 +936,64 @@ int mm3e_field(mm3e_scene* s, const float* points3, size_t n, float* dist, uint3
     cudaFree(d_d);
     cudaFree(d_m);
     return e == cudaSuccess ? MM3E_OK : cuda_fail(c, e, "field");
+}
+
+int mm3e_scene_specialize(mm3e_scene* s, int mode, double* compile_ms) {
+    if (!s) return MM3E_ERR_INVALID;
+    mm3e_ctx* c = s->ctx;
+    if (compile_ms) *compile_ms = 0.0;
+    if (mode < 0 || mode > 2) return fail(c, MM3E_ERR_INVALID, "mode must be 0 (off), 1 (auto) or 2 (always)");
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->stream);  // frames in flight may use the old kernels
+    if (e != cudaSuccess) return cuda_fail(c, e, "specialize");
+    s->spec.reset();
+    if (mode == 0) return MM3E_OK;
+    if (mode == 1 && spec_size(s->low.blob).objects > SPEC_AUTO_MAX_OBJECTS) return MM3E_OK;  // interpreter is faster
+    bool smem = s->low.blob.size() <= 96 * 1024;
+    uint32_t block = c->tune.block, unroll = c->tune.unroll;
+    std::string src = spec_source(s->low.blob, block, unroll, smem);
+    std::unique_ptr<SpecModule> m(new SpecModule());
+    m->kernels.block = block;
+    m->kernels.smem_tape = smem;
+    std::string err = m->build(src, c->device, compile_ms);
+    if (!err.empty() && err.compare(0, 4, "LOG:") != 0) return fail(c, MM3E_ERR_UNSUPPORTED, "scene specialisation: " + err);
+    s->spec = std::move(m);
+    return MM3E_OK;
+}
+
+int mm3e_scene_is_specialized(mm3e_scene* s) { return s && s->spec ? 1 : 0; }
+
+int mm3e_scene_spec_source(const mm3e_scene_desc* desc, char* out, size_t cap, size_t* len) {
+    if (!desc) return MM3E_ERR_INVALID;
+    std::string msg;
+    LoweredScene low;
+    int rc = lower_scene(*desc, nullptr, 0, low, msg);
+    if (rc) return rc;
+    std::string src = spec_source(low.blob, 128, 1, low.blob.size() <= 96 * 1024);
+    if (len) *len = src.size();
+    if (out && cap) {
+        size_t n = src.size() < cap - 1 ? src.size() : cap - 1;
+        std::memcpy(out, src.data(), n);
+        out[n] = 0;
+    }
+    return MM3E_OK;
+}
+
+int mm3e_spec_compile_check(const mm3e_scene_desc* desc, char* err, size_t err_len, double* compile_ms) {
+    if (!desc) return MM3E_ERR_INVALID;
+    std::string msg;
+    LoweredScene low;
+    int rc = lower_scene(*desc, nullptr, 0, low, msg);
+    if (rc) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<char> cubin;
+    std::string e = spec_compile(spec_source(low.blob, 128, 1, low.blob.size() <= 96 * 1024), cubin);
+    if (compile_ms) *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (err && err_len) {
+        std::strncpy(err, e.c_str(), err_len - 1);
+        err[err_len - 1] = 0;
+    }
+    return (e.empty() || e.compare(0, 4, "LOG:") == 0) ? MM3E_OK : MM3E_ERR_UNSUPPORTED;
 }
 
 // Allocation-free ray queries: the scratch lives in noalloc.cu's fixed __device__ array.

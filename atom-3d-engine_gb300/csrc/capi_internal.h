@@ -14,6 +14,7 @@
 
 namespace mm3e {
 class BatchEngine;
+class SpecModule;
 }
 
 struct mm3e_ctx {
@@ -75,6 +76,8 @@ struct mm3e_scene {
     size_t pixels = 0;
     mm3e::PassBuffers buf;                // frame ray queues, hit records, HDR / bloom, counters
     uint32_t buf_wlog = 3;                // tile shape the buffers were sized for
+    std::unique_ptr<mm3e::SpecModule> spec;  // scene-specialised kernels (NVRTC), when built
+    const mm3e::SpecKernels* spec_kernels() const;
     ~mm3e_scene();
     uint32_t n_lights() const;
     size_t device_bytes() const;          // tape + payloads + frame buffers

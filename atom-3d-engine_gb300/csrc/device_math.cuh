@@ -5,8 +5,10 @@
 // order; scalar semantics follow Rust f32 (fmaxf/fminf ignore NaN, clamp is two compares,
 // signum(+-0) = +-1, round is half-away-from-zero).
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 #include "tape.h"
 
@@ -482,6 +484,63 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
         }
     }
     return acc;
+}
+
+// One plain-union run of the plan walked as Bvh::query (accel.rs:79-119): its unbounded
+// members first, then the sphere BVH near child first with the `lower > best` prune and the
+// `lower > slack` bounding-sphere substitute, folded into `acc` by (distance, lowest index).
+// The same steps as world_eval's W_UNB / W_BVH states, as one call for the scene-specialised
+// field (big runs, and LINEAR runs whose winner may undercut its bound).
+static __device__ __noinline__ Field bvh_segment(const Tape& T, uint32_t s, V p, bool seeded, Field acc) {
+    const float INF = __int_as_float(0x7f800000);
+    const float slack = T.h->slack;
+    DevSegment sg = T.seg[s];
+    float bd = seeded ? acc.d : INF;
+    int32_t bi = seeded ? -1 : 0x7FFFFFFF;
+    uint32_t bm = seeded ? acc.m : 0u;
+    for (uint32_t u = sg.ua; u < sg.ua + sg.ub; ++u) {
+        int32_t i = (int32_t)T.unb[u];
+        Field f = object_field(T, T.obj[i], p);
+        if (f.d < bd || (f.d == bd && i < bi)) {
+            bd = f.d;
+            bi = i;
+            bm = f.m;
+        }
+    }
+    NodeStack stk;
+    stk.clear();
+    if (sg.c != NIL) stk.push(sg.c);
+    while (stk.n > 0) {
+        const DevNode& nd = T.node[stk.pop()];
+        float lower = length(p - V{nd.cx, nd.cy, nd.cz}) - nd.r;
+        if (lower > bd) continue;
+        if (nd.leaf >= 0) {
+            int32_t i = nd.leaf;
+            if (lower > slack) {
+                if (lower < bd || (lower == bd && i < bi)) {
+                    bd = lower;
+                    bi = i;
+                    bm = T.obj[i].mat;
+                }
+                continue;
+            }
+            Field f = object_field(T, T.obj[i], p);
+            if (f.d < bd || (f.d == bd && i < bi)) {
+                bd = f.d;
+                bi = i;
+                bm = f.m;
+            }
+            continue;
+        }
+        const DevNode& L = T.node[nd.left];
+        const DevNode& R = T.node[nd.right];
+        float ld = length_sq(p - V{L.cx, L.cy, L.cz});
+        float rd = length_sq(p - V{R.cx, R.cy, R.cz});
+        bool lnear = ld <= rd;
+        stk.push(lnear ? (uint32_t)nd.right : (uint32_t)nd.left);
+        stk.push(lnear ? (uint32_t)nd.left : (uint32_t)nd.right);
+    }
+    return Field{bd, bm};
 }
 
 // ---- dual numbers (dual.rs) for the exact-gradient normal of dual-safe scenes ----

@@ -162,11 +162,11 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
         a.n_items_dev = level == 0 ? (plan.jobs ? &plan.totals->n_samples : nullptr) : buf.counters + 4 * (level - 1) + 2;
         a.b.nq_count = buf.counters + 4 * level + 2;
         a.counter = buf.counters + 4 * level;
-        if ((e = launch_march(a, tune, s, sm_count, log)) != cudaSuccess) return e;
-        if (plan.ao && (e = launch_ao(a, s, log)) != cudaSuccess) return e;
+        if ((e = launch_march(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+        if (plan.ao && (e = launch_ao(a, s, log, plan.spec)) != cudaSuccess) return e;
         if (plan.shadows && plan.lights_max > 0) {
             a.counter = buf.counters + 4 * level + 1;
-            if ((e = launch_shadow(a, tune, s, sm_count, log)) != cudaSuccess) return e;
+            if ((e = launch_shadow(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
         }
         if ((e = launch_shade(a, s, log)) != cudaSuccess) return e;
         std::swap(a.b.q_o, a.b.nq_o);

@@ -80,6 +80,7 @@ struct PassPlan {
     uint32_t lights_max = 0;
     bool ao = false, shadows = false, bloom = false, post = true;
     bool clear_status = true;       // also clear the status word with the work counters
+    const SpecKernels* spec = nullptr;  // scene-specialised march / shadow / AO (single job only)
 };
 
 // Enqueues the passes on `s`: counters cleared, march / AO / shadow / shade per level,

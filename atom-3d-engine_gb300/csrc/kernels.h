@@ -14,8 +14,10 @@
 // batched and served forms put many jobs of different scenes and sizes into one pass
 // sequence through a device-resident job table, so one launch per pass covers all of them.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 #include <stdint.h>
+#endif
 
 namespace mm3e {
 
@@ -108,6 +110,7 @@ struct WaveArgs {
 // Status bits written by kernels.
 enum : uint32_t { ST_TAPE_TIMEOUT = 1u, ST_TAPE_CORRUPT = 2u };
 
+#ifndef __CUDACC_RTC__
 // Kernel kinds the launch log attributes device time to.
 enum KernelKind : uint32_t {
     KK_MARCH = 0, KK_AO, KK_SHADOW, KK_SHADE, KK_RESOLVE, KK_POST, KK_AOV, KK_GI, KK_OTHER, KK_COUNT
@@ -121,9 +124,22 @@ struct LaunchLog {
     void (*end)(void* recorder, uint32_t kind, cudaStream_t s) = nullptr;
 };
 
-cudaError_t launch_march(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log);
-cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log);
-cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log);
+// Kernels of a scene-specialised program (NVRTC, see spec.h): the march / shadow / AO passes
+// with the scene's field compiled in; same parameters as the library's kernels.
+struct SpecKernels {
+    const void* march = nullptr;
+    const void* shadow = nullptr;
+    const void* ao = nullptr;
+    uint32_t block = 128;   // threads per CTA they were compiled for
+    bool smem_tape = true;  // they stage the tape in shared memory
+};
+
+// With `spec`, the pass runs the specialised kernel instead of the interpreter.
+cudaError_t launch_march(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
+                         const SpecKernels* spec = nullptr);
+cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log, const SpecKernels* spec = nullptr);
+cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
+                          const SpecKernels* spec = nullptr);
 cudaError_t launch_shade(const WaveArgs& a, cudaStream_t s, LaunchLog* log);
 // Pixel slots of the jobs (n_slots when known on the host, else capacity + a.totals).
 cudaError_t launch_resolve(const WaveArgs& a, uint32_t n_slots, cudaStream_t s, LaunchLog* log);
@@ -153,5 +169,7 @@ cudaError_t launch_field(const unsigned char* tape, const float* pts, uint32_t n
                          cudaStream_t s, LaunchLog* log);
 cudaError_t launch_gi_reduce(const float4* radiance, const float4* dirs, uint32_t dirs_per_face, uint32_t probes,
                              float4* cubes, cudaStream_t s, LaunchLog* log);
+
+#endif  // __CUDACC_RTC__
 
 }  // namespace mm3e

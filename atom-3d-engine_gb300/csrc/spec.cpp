@@ -1,0 +1,303 @@
+// spec.cpp — generator of the scene-specialised field program and its NVRTC build.
+#include "spec.h"
+
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <sstream>
+
+#include "tape.h"
+
+// Device sources of the library, embedded at build time (march_kernels.cuh and its includes).
+#include "embedded_sources.inc"
+
+namespace mm3e {
+
+namespace {
+
+// ---- NVRTC, loaded on first use -------------------------------------------------------------
+struct Nvrtc {
+    decltype(&nvrtcCreateProgram) create = nullptr;
+    decltype(&nvrtcCompileProgram) compile = nullptr;
+    decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+    decltype(&nvrtcGetProgramLog) log = nullptr;
+    decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+    decltype(&nvrtcGetCUBIN) cubin = nullptr;
+    decltype(&nvrtcDestroyProgram) destroy = nullptr;
+    decltype(&nvrtcGetErrorString) error = nullptr;
+    std::string status = "not loaded";
+};
+
+Nvrtc& nvrtc() {
+    static Nvrtc n;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        std::vector<std::string> names = {"libnvrtc.so.13", "libnvrtc.so"};
+        const char* home = std::getenv("CUDA_HOME");
+        for (std::string base : {std::string(home ? home : ""), std::string("/usr/local/cuda")}) {
+            if (base.empty()) continue;
+            for (const char* dir : {"/lib64/", "/lib/", "/targets/sbsa-linux/lib/", "/targets/x86_64-linux/lib/"}) {
+                names.push_back(base + dir + "libnvrtc.so.13");
+                names.push_back(base + dir + "libnvrtc.so");
+            }
+        }
+        void* h = nullptr;
+        for (const std::string& nm : names)
+            if ((h = dlopen(nm.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
+        if (!h) {
+            n.status = "libnvrtc not found";
+            return;
+        }
+#define MM3E_SYM(field, sym) n.field = reinterpret_cast<decltype(n.field)>(dlsym(h, #sym))
+        MM3E_SYM(create, nvrtcCreateProgram);
+        MM3E_SYM(compile, nvrtcCompileProgram);
+        MM3E_SYM(log_size, nvrtcGetProgramLogSize);
+        MM3E_SYM(log, nvrtcGetProgramLog);
+        MM3E_SYM(cubin_size, nvrtcGetCUBINSize);
+        MM3E_SYM(cubin, nvrtcGetCUBIN);
+        MM3E_SYM(destroy, nvrtcDestroyProgram);
+        MM3E_SYM(error, nvrtcGetErrorString);
+#undef MM3E_SYM
+        bool ok = n.create && n.compile && n.log_size && n.log && n.cubin_size && n.cubin && n.destroy && n.error;
+        n.status = ok ? "" : "libnvrtc lacks an entry point";
+    });
+    return n;
+}
+
+std::string embedded(const char* const* chunks) {
+    std::string s;
+    for (const char* const* c = chunks; *c; ++c) s += *c;
+    return s;
+}
+
+// ---- generator ---------------------------------------------------------------------------------
+std::string fbits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    char b[40];
+    std::snprintf(b, sizeof b, "__uint_as_float(0x%08xu)", u);
+    return b;
+}
+
+std::string farr(const float* f, int n) {
+    std::string s = "{";
+    for (int i = 0; i < n; ++i) s += (i ? ", " : "") + fbits(f[i]);
+    return s + "}";
+}
+
+std::string object_fn(uint32_t i, const DevObject& o) {
+    std::ostringstream os;
+    os << "__device__ __forceinline__ Field obj_" << i << "(const Tape& T, V p) {\n"
+       << "    const DevObject o = {" << farr(o.rot, 9) << ", " << farr(o.pos, 3) << ", " << fbits(o.inv) << ", "
+       << fbits(o.scale) << ", " << farr(o.params, 7) << ", " << o.prim << "u, " << o.mat << "u, " << o.flags << "u, "
+       << o.aux << "u, " << fbits(o.k) << ", " << farr(o.elongate, 3) << ", " << farr(o.repeat, 3) << ", "
+       << fbits(o.twist) << ", " << fbits(o.bend) << ", " << fbits(o.round) << ", " << fbits(o.onion) << ", "
+       << farr(o.bc, 3) << ", " << fbits(o.br) << "};\n"
+       << "    return object_field(T, o, p);\n}\n";
+    return os.str();
+}
+
+std::string lower_expr(const DevObject& o) {
+    return "length(p - V{" + fbits(o.bc[0]) + ", " + fbits(o.bc[1]) + ", " + fbits(o.bc[2]) + "}) - " + fbits(o.br);
+}
+
+}  // namespace
+
+std::string nvrtc_status() { return nvrtc().status; }
+
+SpecSize spec_size(const std::vector<unsigned char>& blob) {
+    const TapeHeader* h = reinterpret_cast<const TapeHeader*>(blob.data());
+    const DevObject* obj = reinterpret_cast<const DevObject*>(blob.data() + h->off_objects);
+    const DevSegment* seg = reinterpret_cast<const DevSegment*>(blob.data() + h->off_segments);
+    const uint32_t* unb = reinterpret_cast<const uint32_t*>(blob.data() + h->off_unbounded);
+    const DevCsgOp* csg = reinterpret_cast<const DevCsgOp*>(blob.data() + h->off_csg);
+    SpecSize z;
+    auto count = [&](uint32_t i) {
+        z.objects += 1;
+        if (obj[i].prim == 11u)
+            for (const DevCsgOp* op = csg + obj[i].aux; op->op != CSG_OP_END && z.csg_ops < (1u << 20); ++op)
+                z.csg_ops += 1;
+    };
+    for (uint32_t s = 0; s < h->n_segments; ++s) {
+        if (seg[s].kind == SEG_ONE) count(seg[s].a);
+        if (seg[s].kind == SEG_LINEAR)
+            for (uint32_t k = 0; k < seg[s].b; ++k) count(unb[seg[s].a + k]);
+    }
+    return z;
+}
+
+std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, uint32_t unroll, bool smem_tape) {
+    const TapeHeader* h = reinterpret_cast<const TapeHeader*>(blob.data());
+    const DevObject* obj = reinterpret_cast<const DevObject*>(blob.data() + h->off_objects);
+    const DevSegment* seg = reinterpret_cast<const DevSegment*>(blob.data() + h->off_segments);
+    const uint32_t* unb = reinterpret_cast<const uint32_t*>(blob.data() + h->off_unbounded);
+    std::ostringstream os;
+    os << "// scene-specialised world field (generated)\n"
+          "typedef unsigned int uint32_t;\ntypedef int int32_t;\ntypedef unsigned long long uint64_t;\n"
+          "typedef unsigned short uint16_t;\ntypedef unsigned char uint8_t;\ntypedef long long int64_t;\n"
+          "#include \"march_kernels.cuh\"\n"
+          "namespace mm3e {\nnamespace spec {\n";
+    std::vector<bool> used(h->n_objects, false);
+    for (uint32_t s = 0; s < h->n_segments; ++s) {
+        const DevSegment& sg = seg[s];
+        if (sg.kind == SEG_ONE) used[sg.a] = true;
+        if (sg.kind == SEG_LINEAR)
+            for (uint32_t k = 0; k < sg.b; ++k) used[unb[sg.a + k]] = true;
+    }
+    for (uint32_t i = 0; i < h->n_objects; ++i)
+        if (used[i]) os << object_fn(i, obj[i]);
+    const std::string slack = fbits(h->slack);
+    os << "__device__ __forceinline__ Field eval(const Tape& T, V p) {\n"
+          "    const float INF = __int_as_float(0x7f800000);\n"
+          "    Field acc{INF, 0u};\n";
+    for (uint32_t s = 0; s < h->n_segments; ++s) {
+        const DevSegment& sg = seg[s];
+        const bool seeded = s > 0;
+        os << "    {  // segment " << s << "\n";
+        if (sg.kind == SEG_ONE) {
+            const DevObject& o = obj[sg.a];
+            os << "        Field f;\n        bool sub = false;\n";
+            if (o.flags & OF_BOUND)
+                os << "        {\n            float lower = " << lower_expr(o) << ";\n"
+                   << "            if (lower > " << slack << ") {\n                f = Field{lower, " << o.mat
+                   << "u};\n                sub = true;\n            }\n        }\n";
+            os << "        if (!sub) f = obj_" << sg.a << "(T, p);\n";
+            // the bound substitute folds with the segment's combine, the exact field with the
+            // object's own (the same value; both kept as the interpreter has them)
+            uint32_t comb_exact = (o.flags >> 16) & 3u;
+            auto fold = [&](uint32_t comb) -> std::string {
+                if (!seeded) return "acc = f;";
+                if (comb == 0u) return "acc = f_union(acc, f);";
+                if (comb == 1u) return "acc = f_smooth_union(acc, f, " + fbits(o.k) + ");";
+                return "acc = f_subtract(acc, f);";
+            };
+            if (comb_exact == sg.b) os << "        " << fold(sg.b) << "\n";
+            else os << "        if (sub) { " << fold(sg.b) << " } else { " << fold(comb_exact) << " }\n";
+        } else if (sg.kind == SEG_LINEAR) {
+            bool any_noncons = false;
+            os << "        float bd = " << (seeded ? "acc.d" : "INF") << ";\n        int32_t bi = "
+               << (seeded ? "-1" : "0x7FFFFFFF") << ";\n        uint32_t bm = " << (seeded ? "acc.m" : "0u")
+               << ";\n        bool bnc = false;\n";
+            for (uint32_t k = 0; k < sg.b; ++k) {
+                uint32_t i = unb[sg.a + k];
+                const DevObject& o = obj[i];
+                bool nc = (o.flags & OF_NONCONS) != 0;
+                any_noncons = any_noncons || nc;
+                std::string exact = "Field f = obj_" + std::to_string(i) + "(T, p);\n            if (f.d < bd || (f.d == bd && " +
+                                    std::to_string(i) + " < bi)) {\n                bd = f.d;\n                bi = " +
+                                    std::to_string(i) + ";\n                bm = f.m;\n                bnc = " +
+                                    (nc ? "true" : "false") + ";\n            }\n";
+                os << "        {  // member " << i << "\n";
+                if (o.flags & OF_BOUND) {
+                    os << "            float lower = " << lower_expr(o) << ";\n";
+                    if (!nc) os << "            if (!(lower > bd)) {\n";
+                    os << "            if (lower > " << slack << ") {\n                if (lower < bd || (lower == bd && "
+                       << i << " < bi)) {\n                    bd = lower;\n                    bi = " << i
+                       << ";\n                    bm = " << o.mat << "u;\n                    bnc = false;\n"
+                       << "                }\n            } else {\n            " << exact << "            }\n";
+                    if (!nc) os << "            }\n";
+                } else {
+                    os << "            " << exact;
+                }
+                os << "        }\n";
+            }
+            if (any_noncons)
+                os << "        if (bnc) acc = bvh_segment(T, " << s << "u, p, " << (seeded ? "true" : "false")
+                   << ", acc);\n        else acc = Field{bd, bm};\n";
+            else
+                os << "        acc = Field{bd, bm};\n";
+        } else {
+            os << "        acc = bvh_segment(T, " << s << "u, p, " << (seeded ? "true" : "false") << ", acc);\n";
+        }
+        os << "    }\n";
+    }
+    os << "    return acc;\n}\n"
+          "struct Field_ {\n    static __device__ __forceinline__ Field eval(const Tape& T, V p) { return spec::eval(T, p); }\n};\n"
+          "}  // namespace spec\n}  // namespace mm3e\n";
+    const int tm = smem_tape ? 0 : 1;
+    os << "extern \"C\" __global__ void __launch_bounds__(" << block
+       << ") mm3e_spec_march(const __grid_constant__ mm3e::WaveArgs a) {\n    mm3e::wave::march_body<" << tm << ", "
+       << unroll << ", mm3e::spec::Field_>(a);\n}\n"
+       << "extern \"C\" __global__ void __launch_bounds__(" << block
+       << ") mm3e_spec_shadow(const __grid_constant__ mm3e::WaveArgs a) {\n    mm3e::wave::shadow_body<" << tm << ", "
+       << unroll << ", mm3e::spec::Field_>(a);\n}\n"
+       << "extern \"C\" __global__ void __launch_bounds__(128) mm3e_spec_ao(const __grid_constant__ mm3e::WaveArgs a) {\n"
+          "    mm3e::wave::ao_body<mm3e::spec::Field_>(a);\n}\n";
+    return os.str();
+}
+
+SpecModule::~SpecModule() {
+    if (lib_) cudaLibraryUnload(lib_);
+}
+
+std::string spec_compile(const std::string& source, std::vector<char>& cubin) {
+    Nvrtc& n = nvrtc();
+    if (!n.status.empty()) return n.status;
+    const char* names[] = {"tape.h", "device_math.cuh", "kernels.h", "march_kernels.cuh"};
+    std::string bodies[] = {embedded(embed_tape_h), embedded(embed_device_math_cuh), embedded(embed_kernels_h),
+                            embedded(embed_march_kernels_cuh)};
+    const char* heads[] = {bodies[0].c_str(), bodies[1].c_str(), bodies[2].c_str(), bodies[3].c_str()};
+    nvrtcProgram prog = nullptr;
+    nvrtcResult r = n.create(&prog, source.c_str(), "mm3e_spec.cu", 4, heads, names);
+    if (r != NVRTC_SUCCESS) return std::string("nvrtcCreateProgram: ") + n.error(r);
+    // MM3E_SPEC_VERBOSE=1 asks ptxas for its resource report (registers, spills), returned as
+    // the log of a successful compile.
+    const char* verbose = std::getenv("MM3E_SPEC_VERBOSE");
+    bool want_log = verbose && verbose[0] == '1';
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "--fmad=false", "-DMM3E_RTC=1",
+                          "--ptxas-options=-v"};
+    r = n.compile(prog, want_log ? 5 : 4, opts);
+    if (r == NVRTC_SUCCESS && want_log) {
+        size_t ls = 0;
+        n.log_size(prog, &ls);
+        std::string log(ls, '\0');
+        if (ls) n.log(prog, &log[0]);
+        size_t cs = 0;
+        n.cubin_size(prog, &cs);
+        cubin.assign(cs, 0);
+        if (cs) n.cubin(prog, cubin.data());
+        n.destroy(&prog);
+        return cs ? "LOG:" + log : "NVRTC produced no cubin";
+    }
+    if (r != NVRTC_SUCCESS) {
+        size_t ls = 0;
+        n.log_size(prog, &ls);
+        std::string log(ls, '\0');
+        if (ls) n.log(prog, &log[0]);
+        n.destroy(&prog);
+        if (log.size() > 4000) log.resize(4000);
+        return std::string("NVRTC compile failed: ") + n.error(r) + "\n" + log;
+    }
+    size_t cs = 0;
+    n.cubin_size(prog, &cs);
+    cubin.assign(cs, 0);
+    if (cs) n.cubin(prog, cubin.data());
+    n.destroy(&prog);
+    return cs ? "" : "NVRTC produced no cubin";
+}
+
+std::string SpecModule::build(const std::string& source, int device, double* compile_ms) {
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<char> cubin;
+    std::string err = spec_compile(source, cubin);
+    if (!err.empty() && err.compare(0, 4, "LOG:") != 0) return err;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaLibraryLoadData(&lib_, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    cudaKernel_t km = nullptr, ks = nullptr, ka = nullptr;
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&km, lib_, "mm3e_spec_march");
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&ks, lib_, "mm3e_spec_shadow");
+    if (e == cudaSuccess) e = cudaLibraryGetKernel(&ka, lib_, "mm3e_spec_ao");
+    if (e != cudaSuccess) return std::string("loading the specialised kernels: ") + cudaGetErrorString(e);
+    kernels.march = reinterpret_cast<const void*>(km);
+    kernels.shadow = reinterpret_cast<const void*>(ks);
+    kernels.ao = reinterpret_cast<const void*>(ka);
+    if (compile_ms) *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return "";
+}
+
+}  // namespace mm3e

@@ -8,8 +8,10 @@
 // (cp.async.bulk) and interpret it from there. Large payloads (SDF volume samples, GI probe
 // cubes) stay in global memory and are referenced by device address.
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
 #include <vector_types.h>
+#endif
 
 namespace mm3e {
 

@@ -2,514 +2,32 @@
 //
 // A frame is a short sequence of small kernels over ray queues. Keeping each kernel's code
 // footprint small matters more here than anything else: a single kernel holding the march,
-// the shadow march, AO and all of the shading stalls on instruction fetch.
-//
-// The march and shadow kernels are persistent tape interpreters: every lane runs one ray at a
-// time, one field sample per loop iteration (or `unroll` samples between refills); a lane that
-// finishes refills from a global counter with one warp-aggregated atomic (ballot + popc +
-// shfl), so warps stay full without a separate compaction pass. With a single job whose tape
-// fits, each CTA first stages the tape into shared memory with TMA bulk copies
-// (cp.async.bulk) completing on an mbarrier; with many jobs (batched / served pass sequences)
-// every lane carries its ray's job and reads that job's tape through the L1 cache.
+// the shadow march, AO and all of the shading stalls on instruction fetch. The march,
+// shadow and AO bodies live in march_kernels.cuh (shared with the scene-specialised NVRTC
+// program); this file instantiates them with the tape interpreter and holds the shading,
+// resolve, AOV, GI and post kernels.
 #include <cuda_runtime.h>
 
 #include "../../include/mm3e_cuda.h"
-#include "device_math.cuh"
 #include "kernels.h"
+#include "march_kernels.cuh"
 
 namespace mm3e {
 namespace {
 
-constexpr uint32_t SMEM_TAPE_MAX = 96 * 1024;
-constexpr int SHADE_THREADS = 128;
-constexpr int POST_THREADS = 256;
-
-// Tape access modes of the persistent kernels.
-enum : int { TM_SMEM = 0, TM_MULTI = 1 };
-
-__device__ __forceinline__ uint32_t item_count(const WaveArgs& a) { return a.n_items_dev ? *a.n_items_dev : a.n_items; }
-
-__device__ __forceinline__ const FrameJob& job_ref(const WaveArgs& a, uint32_t j) { return a.jobs ? a.jobs[j] : a.job0; }
-
-// Job holding position `x` of a job-table range (0: samples, 1: pixel slots, 2: pixels).
-template <int FIELD> __device__ __forceinline__ uint32_t find_job(const FrameJob* jobs, uint32_t n, uint32_t x) {
-    uint32_t lo = 0, hi = n - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1u) >> 1;
-        uint32_t base = FIELD == 0 ? jobs[mid].sample_base : FIELD == 1 ? jobs[mid].slot_base : jobs[mid].pixel_base;
-        if (base <= x) lo = mid;
-        else hi = mid - 1u;
-    }
-    return lo;
-}
-
-// Job of a queue slot (its index is carried in the ray direction's w).
-__device__ __forceinline__ uint32_t slot_job(const WaveArgs& a, uint32_t slot) {
-    return a.jobs ? __float_as_uint(a.b.q_d[slot].w) : 0u;
-}
-
-// Bounded wait on an mbarrier phase; false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32_t limit) {
-    for (uint32_t it = 0; it < limit; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// Stage the tape into shared memory: TMA bulk copies (<= 32 KB each) completing on one
-// mbarrier, waited on with an iteration limit. Returns false (status word set) on failure.
-__device__ __forceinline__ bool stage_tape(unsigned char* smem, const unsigned char* tape, uint32_t bytes,
-                                           uint32_t* status) {
-    __shared__ __align__(8) uint64_t mbar_storage;
-    __shared__ uint32_t tape_ok;
-    uint32_t mbar = (uint32_t)__cvta_generic_to_shared(&mbar_storage);
-    uint32_t dst = (uint32_t)__cvta_generic_to_shared(smem);
-    if (threadIdx.x == 0) {
-        tape_ok = 1u;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
-        for (uint32_t off = 0; off < bytes; off += 32768u) {
-            uint32_t n = bytes - off < 32768u ? bytes - off : 32768u;
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                    dst + off),
-                "l"(tape + off), "r"(n), "r"(mbar)
-                : "memory");
-        }
-    }
-    if (!mbar_wait(mbar, 0u, 1u << 22)) tape_ok = 0u;
-    __syncthreads();
-    bool ok = tape_ok && reinterpret_cast<const TapeHeader*>(smem)->magic == TAPE_MAGIC;
-    if (!ok && threadIdx.x == 0) atomicOr(status, tape_ok ? ST_TAPE_CORRUPT : ST_TAPE_TIMEOUT);
-    return ok;
-}
-
-// Warp-aggregated refill of idle lanes; a lane retires once the items run out.
-__device__ __forceinline__ void refill(uint32_t& item, bool& retired, uint32_t n, uint32_t* counter, bool& fresh) {
-    fresh = false;
-    const uint32_t lane = threadIdx.x & 31u;
-    unsigned want = __ballot_sync(0xFFFFFFFFu, item == NIL && !retired);
-    if (!want) return;
-    uint32_t base = 0;
-    int leader = __ffs(want) - 1;
-    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(want));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-    if (item == NIL && !retired) {
-        uint32_t it = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
-        if (it >= n) retired = true;
-        else {
-            item = it;
-            fresh = true;
-        }
-    }
-}
-
-// Camera::ray (camera.rs:59-65)
-__device__ __forceinline__ V camera_dir(const CameraArgs& c, float sx, float sy, uint32_t w, uint32_t h) {
-    float wf = (float)w, hf = (float)h;
-    float aspect = wf / hf;
-    float ndc_x = (2.0f * sx / wf - 1.0f) * aspect * c.fov_scale;
-    float ndc_y = (1.0f - 2.0f * sy / hf) * c.fov_scale;
-    return normalize(ld3(c.fwd) + scale(ld3(c.right), ndc_x) + scale(ld3(c.up), ndc_y));
-}
-
-// Pixel of a job's pixel slot (tiles of 32 pixels, 2^wlog wide, row-major tiles); false for
-// padding slots.
-__device__ __forceinline__ bool tiled_pixel(uint32_t p, const FrameJob& J, uint32_t wlog, uint32_t& x, uint32_t& y) {
-    uint32_t tile = p >> 5, r = p & 31u;
-    uint32_t tw = 1u << wlog;
-    x = (tile % J.tiles_x) * tw + (r & (tw - 1u));
-    y = (tile / J.tiles_x) * (32u >> wlog) + (r >> wlog);
-    return x < J.width && y < J.height;
-}
-
-__device__ __forceinline__ V tetra_k(uint32_t t) {
-    // k0 = (1,-1,-1), k1 = (-1,-1,1), k2 = (-1,1,-1), k3 = (1,1,1) (march.rs:212-223)
-    return V{(t == 0u || t == 3u) ? 1.0f : -1.0f, (t >= 2u) ? 1.0f : -1.0f, (t == 1u || t == 3u) ? 1.0f : -1.0f};
-}
-
-// Tape of a lane: one staged tape for the CTA (TM_SMEM) or the lane's job's tape (TM_MULTI).
-template <int TM> struct LaneTape;
-template <> struct LaneTape<TM_SMEM> {
-    Tape T;
-    __device__ __forceinline__ const Tape& get() const { return T; }
-    __device__ __forceinline__ void set(const unsigned char*) {}
-};
-template <> struct LaneTape<TM_MULTI> {
-    const unsigned char* p;
-    __device__ __forceinline__ Tape get() const { return tape_view(p); }
-    __device__ __forceinline__ void set(const unsigned char* tp) { p = tp; }
-};
-
-// ------------------------------------------------------------------------------------------
-// march: enhanced sphere tracing (march.rs:120-209) + hit normal (march.rs:212-223 or
-// Scene::normal_dual, lib.rs:820-835), one ray per lane.
-// ------------------------------------------------------------------------------------------
-constexpr uint32_t M_IDLE = 0, M_MARCH = 1, M_COVER = 2, M_TETRA = 3;
-constexpr uint32_t BOOST_OMEGA = 0, BOOST_LEAP = 1, BOOST_SECANT = 2;
-
-struct MLane {
-    uint32_t item, phase;
-    V ro, rd;
-    float t, prev_r, step, t_prev, d_prev, omega, subz;
-    uint32_t i, secant_on, boost;
-    float sv_d, sv_r, sv_e;
-    uint32_t sv_m, hmat;
-    V g;
-    uint32_t tap;
-};
-
-__device__ __forceinline__ V m_at(const MLane& L, float t) { return L.ro + scale(L.rd, t); }
-
-// Finish a ray: write the hit record (normal, t, material or NIL, steps).
-__device__ __forceinline__ void m_write(MLane& L, const WaveArgs& a, bool hit, V n, uint32_t steps) {
-    a.b.h_n[L.item] = make_float4(n.x, n.y, n.z, L.t);
-    a.b.h_m[L.item] = make_uint2(hit ? L.hmat : NIL, steps);
-    L.item = NIL;
-    L.phase = M_IDLE;
-}
-
-// Start the lane's ray for its fresh item; false when the item needs no march.
-template <int TM>
-__device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveArgs& a) {
-    uint32_t job = 0;
-    if (a.src == SRC_SAMPLES) {
-        job = a.jobs ? find_job<0>(a.jobs, a.totals->n_jobs, L.item) : 0u;
-        const FrameJob& J = job_ref(a, job);
-        uint32_t local = L.item - J.sample_base;
-        uint32_t aa = J.aa, spp = J.spp;
-        uint32_t pix = local / spp, sub = local % spp;
-        uint32_t x, y;
-        bool inside = tiled_pixel(pix, J, a.tile_wlog, x, y);
-        uint32_t sx = sub % aa, sy = sub / aa;
-        float nf = (float)aa;
-        float ox = ((float)sx + 0.5f) / nf, oy = ((float)sy + 0.5f) / nf;
-        L.ro = ld3(J.cam.eye);
-        L.rd = inside ? camera_dir(J.cam, (float)x + ox, (float)y + oy, J.width, J.height) : V{0.f, 0.f, 1.f};
-        a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
-        a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, __uint_as_float(job));
-        if (!inside) {  // padding pixel of the last tile row / column
-            L.t = 0.0f;
-            m_write(L, a, false, V{0.f, 0.f, 0.f}, 0u);
-            return false;
-        }
-        LT.set(J.tape);
-    } else if (a.src == SRC_CENTER) {
-        const FrameJob& J = a.job0;
-        uint32_t x = L.item % J.width, y = L.item / J.width;
-        L.ro = ld3(J.cam.eye);
-        L.rd = camera_dir(J.cam, (float)x + 0.5f, (float)y + 0.5f, J.width, J.height);
-        a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
-        a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, 0.0f);
-        LT.set(J.tape);
-    } else if (a.src == SRC_QUEUE) {
-        float4 o = a.b.q_o[L.item], d = a.b.q_d[L.item];
-        L.ro = V{o.x, o.y, o.z};
-        L.rd = V{d.x, d.y, d.z};
-        job = a.jobs ? __float_as_uint(d.w) : 0u;
-        LT.set(job_ref(a, job).tape);
-    } else {  // SRC_GATHER (gi.rs:75-87)
-        uint32_t dpf = a.dirs_per_face;
-        uint32_t dd = L.item % dpf, rest = L.item / dpf;
-        uint32_t face = rest % 6u, probe = rest / 6u;
-        uint32_t i = probe % a.gi_nx, j = (probe / a.gi_nx) % a.gi_ny, k = probe / (a.gi_nx * a.gi_ny);
-        L.ro = ld3(a.gi_lo) + V{(float)i * a.gi_cell[0], (float)j * a.gi_cell[1], (float)k * a.gi_cell[2]};
-        float4 dw = a.gather_dirs[face * dpf + dd];
-        L.rd = V{dw.x, dw.y, dw.z};
-        a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
-        a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, 0.0f);
-        LT.set(a.job0.tape);
-    }
-    const TapeHeader& h = *LT.get().h;
-    // march.rs:132-141
-    L.t = 0.0f;
-    L.prev_r = 0.0f;
-    L.step = 0.0f;
-    L.t_prev = 0.0f;
-    L.d_prev = __int_as_float(0x7f800000);
-    bool lip = h.step_scale >= 1.0f;
-    L.omega = lip ? 1.4f : h.step_scale;
-    L.subz = lip ? h.subitize : 0.0f;
-    L.secant_on = ((h.flags & SF_SECANT) && lip) ? 1u : 0u;
-    L.boost = BOOST_OMEGA;
-    L.i = 0;
-    L.phase = M_MARCH;
-    if (h.max_steps == 0) {
-        m_write(L, a, false, V{0.f, 0.f, 0.f}, 0u);
-        return false;
-    }
-    return true;
-}
-
-// One field sample of the lane's ray and the state transition it causes.
-template <int TM>
-__device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const WaveArgs& a) {
-    const Tape T = LT.get();
-    const TapeHeader& h = *T.h;
-    const uint32_t max_steps = h.max_steps;
-    V p;
-    if (L.phase == M_MARCH) p = m_at(L, L.t);
-    else if (L.phase == M_COVER) p = m_at(L, 0.5f * ((L.t_prev + L.prev_r) + (L.t - L.sv_r)));
-    else p = m_at(L, L.t) + scale(tetra_k(L.tap), h.normal_h);
-    Field f = world_eval(T, p);
-    if (L.phase == M_TETRA) {
-        V kd = scale(tetra_k(L.tap), f.d);
-        L.g = L.tap == 0 ? kd : L.g + kd;
-        L.tap += 1;
-        if (L.tap == 4u) m_write(L, a, true, normalize(L.g), L.i);
-        return;
-    }
-    float d;
-    uint32_t m;
-    float radius, e;
-    if (L.phase == M_MARCH) {
-        d = f.d;
-        m = f.m;
-        radius = fabsf(d);
-        e = h.eps * (1.0f + L.t * 0.5f) + h.lod_footprint * L.t;
-        bool overlap_fail = (L.step > 0.0f && d < 0.0f) || L.step > radius + L.prev_r;
-        if (overlap_fail && d > 0.0f) {  // check the gap midpoint first
-            L.sv_d = d;
-            L.sv_m = m;
-            L.sv_r = radius;
-            L.sv_e = e;
-            L.phase = M_COVER;
-            return;
-        }
-        if (overlap_fail) goto rollback;
-    } else {  // M_COVER
-        float gap_lo = L.t_prev + L.prev_r;
-        float gap_hi = L.t - L.sv_r;
-        L.phase = M_MARCH;
-        if (!(f.d >= 0.5f * (gap_hi - gap_lo))) goto rollback;
-        d = L.sv_d;
-        m = L.sv_m;
-        radius = L.sv_r;
-        e = L.sv_e;
-    }
-    // march.rs:173-206
-    if (d < e) {
-        L.hmat = m;
-        if (h.flags & SF_DUAL_SAFE) {
-            m_write(L, a, true, normal_dual(T.obj, h.n_objects, m_at(L, L.t)), L.i);
-        } else {
-            L.phase = M_TETRA;
-            L.tap = 0;
-        }
-        return;
-    }
-    {
-        float step_len = d * L.omega;
-        uint32_t boost = BOOST_OMEGA;
-        if (L.subz > 0.0f && d > e * 6.0f) {
-            step_len = step_len * (1.0f + L.subz);
-            boost = BOOST_LEAP;
-        }
-        if (L.secant_on && d < 0.08f && isfinite(L.d_prev)) {
-            float dt = L.t - L.t_prev;
-            float dd = d - L.d_prev;
-            if (dt > 1e-6f && dd < -1e-6f) {
-                step_len = clampf(-d * dt / dd, d, d * 4.0f);
-                boost = BOOST_SECANT;
-            }
-        }
-        L.step = step_len;
-        L.boost = boost;
-        L.prev_r = radius;
-        L.d_prev = d;
-        L.t_prev = L.t;
-        L.t = L.t + step_len;
-        if (L.t > h.max_dist) {
-            m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
-            return;
-        }
-        L.i += 1;
-        if (L.i >= max_steps) m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
-        return;
-    }
-rollback:  // retreat to the last safe frontier (march.rs:155-170)
-    L.t = L.t_prev + L.prev_r;
-    if (L.boost == BOOST_OMEGA) L.omega = fminf(L.omega, 1.0f);
-    else if (L.boost == BOOST_LEAP) L.subz = 0.0f;
-    else L.secant_on = 0;
-    L.boost = BOOST_OMEGA;
-    L.prev_r = 0.0f;
-    L.step = 0.0f;
-    L.d_prev = __int_as_float(0x7f800000);
-    L.i += 1;
-    if (L.i >= max_steps) m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
-}
+using namespace wave;
 
 template <int TM, int BLOCK, int UNROLL>
 __global__ void __launch_bounds__(BLOCK) k_march(const __grid_constant__ WaveArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    LaneTape<TM> LT;
-    if constexpr (TM == TM_SMEM) {
-        if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status)) return;
-        LT.T = tape_view(smem);
-    } else {
-        LT.p = a.job0.tape;
-    }
-    const uint32_t n = item_count(a);
-    MLane L;
-    L.item = NIL;
-    L.phase = M_IDLE;
-    bool retired = false;
-    for (;;) {
-        bool fresh;
-        refill(L.item, retired, n, a.counter, fresh);
-        if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
-        if (fresh && !m_start(L, LT, a)) continue;
-#pragma unroll 1
-        for (int u = 0; u < UNROLL; ++u) {
-            if (L.phase == M_IDLE) break;
-            m_step(L, LT, a);
-        }
-    }
-}
-
-// ------------------------------------------------------------------------------------------
-// ao: Marcher::ambient_occlusion (march.rs:264-280) at every hit
-// ------------------------------------------------------------------------------------------
-__device__ __forceinline__ void ao_slot(const WaveArgs& a, uint32_t slot) {
-    uint2 hm = a.b.h_m[slot];
-    if (hm.x == NIL) {
-        a.b.occ[slot] = 1.0f;
-        return;
-    }
-    const Tape T = tape_view(job_ref(a, slot_job(a, slot)).tape);
-    const TapeHeader& h = *T.h;
-    uint32_t ns = h.ao_samples;
-    // A table of jobs runs AO for every job; the shading of a job without AO ignores it.
-    if (ns == 0 || (a.jobs && !(h.flags & SF_AO))) {
-        a.b.occ[slot] = 1.0f;
-        return;
-    }
-    float4 hn4 = a.b.h_n[slot], o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
-    V hp = V{o4.x, o4.y, o4.z} + scale(V{d4.x, d4.y, d4.z}, hn4.w);
-    V n{hn4.x, hn4.y, hn4.z};
-    float base = fmaxf(h.normal_h, 0.01f);
-    float span = (float)((ns > 2u ? ns : 2u) - 1u);
-    float occ = 0.0f, sca = 1.0f;
-    for (uint32_t i = 0; i < ns; ++i) {
-        float hr = base + 0.12f * (float)i / span;
-        float d = world_eval(T, hp + scale(n, hr)).d;
-        occ = occ + (hr - d) * sca;
-        sca = sca * 0.92f;
-    }
-    a.b.occ[slot] = clampf(1.0f - 2.6f * occ, 0.0f, 1.0f);
-}
-
-__global__ void __launch_bounds__(SHADE_THREADS) k_ao(const __grid_constant__ WaveArgs a) {
-    const uint32_t n = item_count(a);
-    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n; slot += gridDim.x * blockDim.x)
-        ao_slot(a, slot);
-}
-
-// ------------------------------------------------------------------------------------------
-// shadow: Marcher::soft_shadow (march.rs:227-259) per (hit, light), one march per lane
-// ------------------------------------------------------------------------------------------
-struct SLane {
-    uint32_t item, si;
-    V so, sdir;
-    float st, sres, sk, smax;
-};
-
-template <int TM>
-__device__ __forceinline__ bool s_start(SLane& S, LaneTape<TM>& LT, const WaveArgs& a) {
-    const uint32_t nl = a.lights_max;
-    uint32_t slot = S.item / nl, li = S.item % nl;
-    uint2 hm = a.b.h_m[slot];
-    if (hm.x != NIL) {
-        float4 hn4 = a.b.h_n[slot], o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
-        uint32_t job = a.jobs ? __float_as_uint(d4.w) : 0u;
-        LT.set(job_ref(a, job).tape);
-        const Tape T = LT.get();
-        const TapeHeader& h = *T.h;
-        if (li < h.n_lights && (h.flags & SF_SHADOWS) && h.shadow_steps > 0) {
-            V hp = V{o4.x, o4.y, o4.z} + scale(V{d4.x, d4.y, d4.z}, hn4.w);
-            V hn{hn4.x, hn4.y, hn4.z};
-            const DevLight& lt = T.light[li];
-            V ldir;
-            float ldist;
-            light_toward(lt, hp, ldir, ldist);
-            if (fmaxf(dot(hn, ldir), 0.0f) > 0.0f) {  // lib.rs:1315-1322
-                float lift = fmaxf(h.normal_h * 2.0f, 0.01f);
-                S.so = hp + scale(hn, lift);
-                S.sdir = ldir;
-                S.smax = fminf(ldist, h.max_dist);
-                S.sk = light_shadow_k(lt, ldist);
-                float hb = S.so.x * 127.1f + S.so.y * 311.7f + S.so.z * 74.7f;
-                float sv = sinf(hb) * 43758.547f;
-                S.st = 0.02f + fabsf(sv - truncf(sv)) * 0.16f;
-                S.sres = 1.0f;
-                S.si = 0;
-                return true;
-            }
-        }
-    }
-    a.b.shadow[S.item] = -1.0f;
-    S.item = NIL;
-    return false;
-}
-
-template <int TM>
-__device__ __forceinline__ void s_step(SLane& S, const LaneTape<TM>& LT, const WaveArgs& a) {
-    const Tape T = LT.get();
-    float hh = world_eval(T, S.so + scale(S.sdir, S.st)).d;
-    if (hh < 0.0008f) {
-        a.b.shadow[S.item] = 0.0f;
-        S.item = NIL;
-        return;
-    }
-    S.sres = fminf(S.sres, S.sk * hh / S.st);
-    S.st = S.st + clampf(hh, 0.06f, 0.5f + 0.7f * S.st);
-    S.si += 1;
-    if (S.st > S.smax || S.si >= T.h->shadow_steps) {
-        a.b.shadow[S.item] = clampf(S.sres, 0.0f, 1.0f);
-        S.item = NIL;
-    }
+    march_body<TM, UNROLL, InterpField>(a);
 }
 
 template <int TM, int BLOCK, int UNROLL>
 __global__ void __launch_bounds__(BLOCK) k_shadow(const __grid_constant__ WaveArgs a) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    LaneTape<TM> LT;
-    if constexpr (TM == TM_SMEM) {
-        if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status)) return;
-        LT.T = tape_view(smem);
-    } else {
-        LT.p = a.job0.tape;
-    }
-    const uint32_t n = item_count(a) * a.lights_max;
-    SLane S;
-    S.item = NIL;
-    bool retired = false;
-    for (;;) {
-        bool fresh;
-        refill(S.item, retired, n, a.counter, fresh);
-        if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
-        if (fresh && !s_start(S, LT, a)) continue;
-#pragma unroll 1
-        for (int u = 0; u < UNROLL; ++u) {
-            if (S.item == NIL) break;
-            s_step(S, LT, a);
-        }
-    }
+    shadow_body<TM, UNROLL, InterpField>(a);
 }
+
+__global__ void __launch_bounds__(SHADE_THREADS) k_ao(const __grid_constant__ WaveArgs a) { ao_body<InterpField>(a); }
 
 // ------------------------------------------------------------------------------------------
 // shade: shade_hit (lib.rs:1286-1360) / sky on a miss; reflection rays go to the next queue
@@ -839,6 +357,24 @@ struct PersistentSet {
          {{K<TM_MULTI, 128, 1>, K<TM_MULTI, 128, 2>}, {K<TM_MULTI, 256, 1>, K<TM_MULTI, 256, 2>}}} \
     }
 
+// Grid of a persistent launch: every CTA the SMs hold at once, fewer when the host knows
+// that fewer items exist.
+cudaError_t persistent_grid(const void* k, int block, size_t smem, const WaveArgs& a, int sm_count,
+                            uint32_t items_per_item, uint32_t* blocks_out) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    uint32_t blocks = (uint32_t)(per_sm * sm_count);
+    if (!a.n_items_dev) {
+        uint64_t items = (uint64_t)a.n_items * items_per_item;
+        uint64_t needed = (items + block - 1) / block;
+        if (needed < blocks) blocks = needed > 0 ? (uint32_t)needed : 1u;
+    }
+    *blocks_out = blocks;
+    return cudaSuccess;
+}
+
 cudaError_t launch_persistent(const PersistentSet& set, const WaveArgs& a, const TuneParams& t, cudaStream_t s,
                               int sm_count, uint32_t items_per_item) {
     bool use_smem = !a.jobs && a.tape_bytes <= SMEM_TAPE_MAX;
@@ -851,18 +387,27 @@ cudaError_t launch_persistent(const PersistentSet& set, const WaveArgs& a, const
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TAPE_MAX);
         if (e != cudaSuccess) return e;
     }
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, smem);
+    uint32_t blocks = 0;
+    cudaError_t e = persistent_grid(reinterpret_cast<const void*>(k), block, smem, a, sm_count, items_per_item, &blocks);
     if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    uint32_t blocks = (uint32_t)(per_sm * sm_count);
-    if (!a.n_items_dev) {
-        uint64_t items = (uint64_t)a.n_items * items_per_item;
-        uint64_t needed = (items + block - 1) / block;
-        if (needed < blocks) blocks = needed > 0 ? (uint32_t)needed : 1u;
-    }
     k<<<blocks, block, smem, s>>>(a);
     return cudaGetLastError();
+}
+
+// A specialised (run-time compiled) persistent kernel.
+cudaError_t launch_persistent_spec(const void* k, const SpecKernels& sp, const WaveArgs& a, cudaStream_t s,
+                                   int sm_count, uint32_t items_per_item) {
+    size_t smem = sp.smem_tape ? a.tape_bytes : 0;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TAPE_MAX);
+        if (e != cudaSuccess) return e;
+    }
+    uint32_t blocks = 0;
+    cudaError_t e = persistent_grid(k, (int)sp.block, smem, a, sm_count, items_per_item, &blocks);
+    if (e != cudaSuccess) return e;
+    WaveArgs arg = a;
+    void* args[] = {&arg};
+    return cudaLaunchKernel(k, dim3(blocks), dim3(sp.block), args, smem, s);
 }
 
 unsigned grid_for(uint64_t n, int threads, uint32_t cap = 0) {
@@ -873,23 +418,34 @@ unsigned grid_for(uint64_t n, int threads, uint32_t cap = 0) {
 
 }  // namespace
 
-cudaError_t launch_march(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log) {
+cudaError_t launch_march(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
+                         const SpecKernels* spec) {
     static const PersistentSet set = MM3E_PERSISTENT_SET(k_march);
     LogScope sc(log, KK_MARCH, s, 1);
+    if (spec && spec->march && !a.jobs) return launch_persistent_spec(spec->march, *spec, a, s, sm_count, 1);
     return launch_persistent(set, a, t, s, sm_count, 1);
 }
 
-cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log) {
+cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
+                          const SpecKernels* spec) {
     static const PersistentSet set = MM3E_PERSISTENT_SET(k_shadow);
     LogScope sc(log, KK_SHADOW, s, 1);
-    return launch_persistent(set, a, t, s, sm_count, a.lights_max ? a.lights_max : 1);
+    uint32_t per = a.lights_max ? a.lights_max : 1;
+    if (spec && spec->shadow && !a.jobs) return launch_persistent_spec(spec->shadow, *spec, a, s, sm_count, per);
+    return launch_persistent(set, a, t, s, sm_count, per);
 }
 
 // Non-persistent kernels are sized for the largest queue (a.n_items) and read the live count
 // from n_items_dev when set.
-cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log) {
+cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log, const SpecKernels* spec) {
     LogScope sc(log, KK_AO, s, 1);
-    k_ao<<<grid_for(a.n_items, SHADE_THREADS, a.grid_cap), SHADE_THREADS, 0, s>>>(a);
+    unsigned grid = grid_for(a.n_items, SHADE_THREADS, a.grid_cap);
+    if (spec && spec->ao && !a.jobs) {
+        WaveArgs arg = a;
+        void* args[] = {&arg};
+        return cudaLaunchKernel(spec->ao, dim3(grid), dim3(SHADE_THREADS), args, 0, s);
+    }
+    k_ao<<<grid, SHADE_THREADS, 0, s>>>(a);
     return cudaGetLastError();
 }
 

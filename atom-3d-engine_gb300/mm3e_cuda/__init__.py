@@ -193,6 +193,20 @@ class CompiledScene:
         except Exception:
             pass
 
+    SPEC_OFF, SPEC_AUTO, SPEC_ALWAYS = 0, 1, 2
+
+    def specialize(self, mode=2):
+        """Scene-specialised march / shadow / AO kernels (NVRTC): mode 0 off, 1 auto (only
+        fields of at most 24 objects), 2 always (True/False map to 2/0). Returns compile ms."""
+        mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else mode
+        ms = C.c_double()
+        self.ctx.check(lib().mm3e_scene_specialize(self._ptr, int(mode), C.byref(ms)))
+        return ms.value
+
+    @property
+    def specialized(self):
+        return bool(lib().mm3e_scene_is_specialized(self._ptr))
+
     def device_bytes(self):
         n = C.c_size_t()
         self.ctx.check(lib().mm3e_scene_device_bytes(self._ptr, C.byref(n)))
@@ -286,6 +300,27 @@ class CudaRenderer:
 
     def compile(self, scene):
         return CompiledScene(self.ctx, scene)
+
+
+def spec_source(scene):
+    """The generated scene-specialised program (host only)."""
+    h = scene.desc()
+    n = C.c_size_t()
+    lib().mm3e_scene_spec_source(h.ptr, None, 0, C.byref(n))
+    buf = C.create_string_buffer(n.value + 1)
+    rc = lib().mm3e_scene_spec_source(h.ptr, buf, n.value + 1, C.byref(n))
+    if rc != abi.OK:
+        raise RenderError(rc, "spec source")
+    return buf.value.decode()
+
+
+def spec_compile_check(scene):
+    """NVRTC compile of the scene's specialised program (host only): (ok, message, ms)."""
+    h = scene.desc()
+    err = C.create_string_buffer(8192)
+    ms = C.c_double()
+    rc = lib().mm3e_spec_compile_check(h.ptr, err, 8192, C.byref(ms))
+    return rc == abi.OK, err.value.decode(errors="replace"), ms.value
 
 
 def validate(scene):

@@ -23,8 +23,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["wavefront.cu", "noalloc.cu", "mesh_bake.cu"]
-CPP_SOURCES = ["lower.cpp", "capi.cpp", "engine.cpp", "batch.cpp", "mesh.cpp", "server.cpp"]
-HEADERS = ["tape.h", "lower.h", "kernels.h", "device_math.cuh", "noalloc.h", "engine.h", "capi_internal.h", "batch.h", "mesh.h", "server.h"]
+CPP_SOURCES = ["lower.cpp", "capi.cpp", "engine.cpp", "batch.cpp", "mesh.cpp", "server.cpp", "spec.cpp"]
+HEADERS = ["tape.h", "lower.h", "kernels.h", "device_math.cuh", "noalloc.h", "engine.h", "capi_internal.h", "batch.h", "mesh.h", "server.h", "march_kernels.cuh", "spec.h"]
 
 
 def _cudart_dir():
@@ -49,12 +49,33 @@ def stale():
     return any(os.path.getmtime(f) > t for f in _deps())
 
 
+# Device sources compiled again at run time by NVRTC for scene-specialised programs.
+EMBEDDED = ["tape.h", "device_math.cuh", "kernels.h", "march_kernels.cuh"]
+
+
+def write_embedded(path):
+    """C++ include with the EMBEDDED sources as null-terminated arrays of string-literal chunks."""
+    out = ["// generated by mm3e_cuda/build.py from csrc/: device sources for NVRTC", "namespace mm3e {"]
+    for name in EMBEDDED:
+        with open(os.path.join(CSRC, name)) as f:
+            src = f.read()
+        ident = "embed_" + name.replace(".", "_")
+        out.append(f"static const char* const {ident}[] = {{")
+        for i in range(0, len(src), 16000):
+            out.append('R"MM3E_EMBED(' + src[i:i + 16000] + ')MM3E_EMBED",')
+        out.append("nullptr};")
+    out.append("}  // namespace mm3e")
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")
+
+
 def build(force=False, verbose=False, extra_nvcc=()):
     """Compile (in parallel) and link the library if any input changed. Returns the .so path."""
     if not force and not stale():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
+    write_embedded(os.path.join(OBJ_DIR, "embedded_sources.inc"))
     jobs = []
     objs = []
     for src in CU_SOURCES:
@@ -69,7 +90,8 @@ def build(force=False, verbose=False, extra_nvcc=()):
     for src in CPP_SOURCES:
         obj = os.path.join(OBJ_DIR, src + ".o")
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
-               "-I", os.path.join(CUDA_HOME, "include"), "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+               "-I", os.path.join(CUDA_HOME, "include"), "-I", INCLUDE, "-I", OBJ_DIR, "-c", os.path.join(CSRC, src),
+               "-o", obj]
         jobs.append((cmd, obj))
         objs.append(obj)
     procs = []

@@ -80,6 +80,10 @@ def _declare_extra(lib):
         "mm3e_server_replay": (C.c_int, [C.c_void_p, P(abi.Request), P(C.c_double), C.c_size_t,
                                          P(abi.RequestResult)]),
         "mm3e_server_destroy": (None, [C.c_void_p]),
+        "mm3e_scene_specialize": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double)]),
+        "mm3e_scene_is_specialized": (C.c_int, [C.c_void_p]),
+        "mm3e_scene_spec_source": (C.c_int, [P(abi.SceneDesc), C.c_char_p, C.c_size_t, P(C.c_size_t)]),
+        "mm3e_spec_compile_check": (C.c_int, [P(abi.SceneDesc), C.c_char_p, C.c_size_t, P(C.c_double)]),
         "mm3e_autotune": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, C.c_uint32, P(abi.Tuning),
                                     P(abi.TuneEntry), C.c_uint32, P(C.c_uint32)]),
     }

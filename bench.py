@@ -76,6 +76,7 @@ def parse():
     ap.add_argument("--served-max-requests", type=int, default=2000,
                     help="cap on requests per rate (the arrival window shrinks to fit)")
     ap.add_argument("--no-forms", action="store_true", help="skip the Cornell / batched / served measurements")
+    ap.add_argument("--no-spec", action="store_true", help="time the tape interpreter (no NVRTC specialisation)")
     return ap.parse_args()
 
 
@@ -99,6 +100,7 @@ def bench_cornell(ctx, stream, torch):
     t0 = time.perf_counter()
     cs.bake_gi((32, 32, 32), 5)
     bake_s = time.perf_counter() - t0
+    cs.specialize(cs.SPEC_AUTO)  # after the bake (a bake re-lowers the scene)
     out = torch.empty(1920 * 1080 * 4, dtype=torch.uint8, device="cuda")
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(3):
@@ -112,10 +114,12 @@ def bench_cornell(ctx, stream, torch):
             ev[1].record(stream)
             stream.synchronize()
             ms.append(ev[0].elapsed_time(ev[1]))
+    specialized = cs.specialized
     cs.close()
     return {"workload": "cornell_gi_1080p", "frames_per_s": 1000.0 / statistics.median(ms),
             "frame_ms_median": statistics.median(ms), "gi_probes": "32^3 ambient cubes, 5 rays per face",
-            "gi_bake_ms_host_wall": bake_s * 1000.0, "gi_bake_rays": 32 ** 3 * 6 * 5}
+            "gi_bake_ms_host_wall": bake_s * 1000.0, "gi_bake_rays": 32 ** 3 * 6 * 5,
+            "field": "scene-specialised (NVRTC)" if specialized else "tape interpreter"}
 
 
 def bench_batched(ctx, stream, torch, n_scenes):
@@ -265,11 +269,14 @@ def run_profile_frames(args):
     scene, cam = workloads(size)[args.workload]()
     ctx = mm3e_cuda.Context(0)
     compiled = mm3e_cuda.CompiledScene(ctx, scene)
+    if not args.no_spec:
+        compiled.specialize(compiled.SPEC_AUTO)
     out = torch.empty(scene.width * scene.height * 4, dtype=torch.uint8, device="cuda")
     for _ in range(args.profile_frames):
         compiled.render_device(cam, abi.FB_RGBA8, out.data_ptr(), out.numel())
     ctx.sync()
-    print(f"rendered {args.profile_frames} frame(s) of {args.workload} at {scene.width}x{scene.height}")
+    print(f"rendered {args.profile_frames} frame(s) of {args.workload} at {scene.width}x{scene.height}"
+          f" ({'specialised' if compiled.specialized else 'interpreted'} field)")
     ctx.close()
 
 
@@ -405,7 +412,6 @@ def run_ours(args):
     compiled = mm3e_cuda.CompiledScene(ctx, scene)
     w, h = scene.width, scene.height
     out8 = torch.empty(h * w * 4, dtype=torch.uint8, device=dev)
-    hdr = torch.empty(h * w * 4, dtype=torch.float32, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
 
     def frame():
@@ -422,6 +428,15 @@ def run_ours(args):
         stream.synchronize()
         return [a.elapsed_time(b) for a, b in ev]
 
+    # the interpreter first (reported beside), then the scene-specialised kernels the fixed scene
+    # renders with (auto policy: small fields only), compiled before the timed region
+    for _ in range(max(3, args.warmup)):
+        frame()
+    interp_ms = timed(frame, max(3, args.steps // 2))
+    spec_compile_ms = None
+    if not args.no_spec:
+        spec_compile_ms = compiled.specialize(compiled.SPEC_AUTO)
+    specialized = compiled.specialized
     for _ in range(max(3, args.warmup)):
         frame()
     stream.synchronize()
@@ -504,7 +519,11 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded scene (no dataset)",
         "config": {"workload": args.workload, "width": w, "height": h, "aa": scene.aa, "bounces": scene.bounces,
                    "max_steps": scene.marcher.max_steps, "parallelism": f"replicas x{world}",
-                   "l2": "flushed between timed frames (256 MB write)"},
+                   "l2": "flushed between timed frames (256 MB write)",
+                   "field": "scene-specialised (NVRTC)" if specialized else "tape interpreter",
+                   "spec_compile_ms": spec_compile_ms},
+        "interpreter": {"frames_per_s": 1000.0 / statistics.median(interp_ms),
+                        "frame_ms_median": statistics.median(interp_ms)},
         "mrays_per_s": mrays, "frame_ms": {"min": min(frame_ms), "median": statistics.median(frame_ms),
                                            "max": max(frame_ms)},
         "wall_s_timed_region": wall, "roofline": roofline, "cpu_baseline": cpu,

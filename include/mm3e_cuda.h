@@ -357,6 +357,27 @@ typedef struct mm3e_mesh {
 int mm3e_bake_mesh_sdf(mm3e_ctx* ctx, const mm3e_mesh* mesh, uint32_t resolution, float padding, mm3e_volume* out,
                        float* data, size_t n_floats, int data_on_device);
 
+/* ---- scene-specialised field (NVRTC) -------------------------------------------------------- */
+/* Compiles, for this scene, march / shadow / AO kernels whose world field is generated from the
+ * scene (the reference's GPU twin generates its `map` the same way, mm3e-gpu/src/wgsl.rs:277-319,
+ * here with the CPU path's semantics): every object becomes a call of the library's own field
+ * code on a constant copy of its record, every world-plan segment straight-line code with the
+ * interpreter's fold, so frames are identical to the interpreted ones. Later mm3e_render /
+ * mm3e_render_device / mm3e_render_linear / mm3e_render_hits calls of the scene use them (not
+ * with dynamic spheres, not in batches). The launch shape is the context's tuning at this call.
+ * mode 0 drops them; 2 always compiles; 1 (auto) compiles only scenes whose field inlines at
+ * most 24 objects (larger fields outgrow the instruction cache and the shared-code interpreter
+ * is faster) and otherwise returns MM3E_OK leaving the interpreter. MM3E_ERR_UNSUPPORTED when
+ * NVRTC cannot be loaded or compile fails. A GI bake (re-lowering) drops them. compile_ms may be
+ * NULL. Blocking. */
+int mm3e_scene_specialize(mm3e_scene* scene, int mode, double* compile_ms);
+/* 1 when the scene renders with specialised kernels. */
+int mm3e_scene_is_specialized(mm3e_scene* scene);
+/* Host-only helpers (no device): the generated program of a scene description, and an NVRTC
+ * compile of it to an sm_103a cubin (err receives the compiler log on failure). */
+int mm3e_scene_spec_source(const mm3e_scene_desc* desc, char* out, size_t cap, size_t* len);
+int mm3e_spec_compile_check(const mm3e_scene_desc* desc, char* err, size_t err_len, double* compile_ms);
+
 /* ---- diagnostics: primary hits, arbitrary rays, field samples ------------------------------- */
 /* Primary pinhole ray through every pixel centre (the ray RenderMode AOVs and the pinhole film
  * use, lib.rs:1179): hit distance t, material id (0xFFFFFFFF on a miss), march steps and the
