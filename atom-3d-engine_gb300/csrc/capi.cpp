@@ -597,7 +597,8 @@ int mm3e_ctx_set_profiling(mm3e_ctx* ctx, int enable) {
 
 int mm3e_ctx_kernel_times(mm3e_ctx* ctx, mm3e_kernel_time* out, uint32_t cap, uint32_t* n_out) {
     if (!ctx) return MM3E_ERR_INVALID;
-    static const char* names[KK_COUNT] = {"march", "ao", "shadow", "shade", "resolve", "post", "aov", "gi", "other"};
+    static const char* names[KK_COUNT] = {"march", "ao", "shadow", "shade", "resolve", "post", "aov", "gi", "other",
+                                          "march_refl", "ao_refl", "shadow_refl"};
     cudaError_t e = ctx->prof.collect(ctx->kk_ms, ctx->kk_launches);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel times");
     uint32_t n = 0;

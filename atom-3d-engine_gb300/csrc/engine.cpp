@@ -12,15 +12,21 @@ template <class T> cudaError_t grow(T** p, size_t n) {
 }  // namespace
 
 void PassBuffers::release() {
-    void* ps[] = {qa_o, qa_d, qb_o, qb_d, h_n, h_m, occ, shadow, lvl, term, hdr, bright, blur, counters};
+    void* ps[] = {qa_o, qa_d, qb_o, qb_d, qc_o, qc_d, h_n, h_m, occ, shadow, h_n1, h_m1, occ1, shadow1,
+                  lvl, term, hdr, bright, blur, counters};
     for (void* p : ps) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (aux) cudaStreamDestroy(aux);
     *this = PassBuffers();
 }
 
 size_t PassBuffers::bytes_for(size_t cap, size_t lights, size_t levels, size_t pixels) {
     size_t l = lights ? lights : 1, v = levels ? levels : 1;
-    return cap * (5 * sizeof(float4) + sizeof(uint2) + sizeof(float) + l * sizeof(float) + 2 * v * sizeof(float4) +
-                  sizeof(float4)) +
+    size_t queues = v >= 3 ? 6 : 4, hit_sets = v >= 2 ? 2 : 1;
+    return cap * (queues * sizeof(float4) + hit_sets * (sizeof(float4) + sizeof(uint2) + sizeof(float) +
+                                                         l * sizeof(float)) +
+                  2 * v * sizeof(float4) + sizeof(float4)) +
            pixels * 3 * sizeof(float4) + N_COUNTERS * sizeof(uint32_t);
 }
 
@@ -40,6 +46,18 @@ cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need
         (e = grow(&h_n, c)) || (e = grow(&h_m, c)) || (e = grow(&occ, c)) || (e = grow(&shadow, c * (l ? l : 1))) ||
         (e = grow(&lvl, c * 2 * (v ? v : 1))) || (e = grow(&term, c)) || (e = grow(&hdr, px)) ||
         (e = grow(&bright, px)) || (e = grow(&blur, px)) || (e = grow(&counters, (size_t)N_COUNTERS))) {
+        release();
+        return e;
+    }
+    if (v >= 2 && ((e = grow(&h_n1, c)) || (e = grow(&h_m1, c)) || (e = grow(&occ1, c)) ||
+                   (e = grow(&shadow1, c * (l ? l : 1))) ||
+                   (e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) ||
+                   (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)) ||
+                   (e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming)))) {
+        release();
+        return e;
+    }
+    if (v >= 3 && ((e = grow(&qc_o, c)) || (e = grow(&qc_d, c)))) {
         release();
         return e;
     }
@@ -150,27 +168,76 @@ WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tun
 }
 }  // namespace
 
+namespace {
+// The passes of one level: march, AO, shadows, (reflection rays of the next level), shading.
+cudaError_t level_passes(const PassPlan& plan, WaveArgs& a, PassBuffers& buf, const TuneParams& tune, cudaStream_t s,
+                         int sm_count, LaunchLog* log, uint32_t level, bool reflect_next) {
+    cudaError_t e;
+    a.level = level;
+    a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
+    a.n_items = plan.n_samples;
+    a.n_items_dev = level == 0 ? (plan.jobs ? &plan.totals->n_samples : nullptr) : buf.counters + 4 * (level - 1) + 2;
+    a.b.nq_count = buf.counters + 4 * level + 2;
+    a.counter = buf.counters + 4 * level;
+    if ((e = launch_march(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+    if (reflect_next && (e = launch_reflect(a, s, log)) != cudaSuccess) return e;
+    if (plan.ao && (e = launch_ao(a, s, log, plan.spec)) != cudaSuccess) return e;
+    if (plan.shadows && plan.lights_max > 0) {
+        a.counter = buf.counters + 4 * level + 1;
+        if ((e = launch_shadow(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+    }
+    return launch_shade(a, s, log);
+}
+}  // namespace
+
 cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams& tune, cudaStream_t s, int sm_count,
                        LaunchLog* log) {
     cudaError_t e = cudaMemsetAsync(buf.counters, 0, (N_COUNTERS - (plan.clear_status ? 0 : 1)) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     WaveArgs a = wave_args(plan, buf, tune, sm_count);
-    for (uint32_t level = 0; level < plan.levels; ++level) {
-        a.level = level;
-        a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
-        a.n_items = plan.n_samples;
-        a.n_items_dev = level == 0 ? (plan.jobs ? &plan.totals->n_samples : nullptr) : buf.counters + 4 * (level - 1) + 2;
-        a.b.nq_count = buf.counters + 4 * level + 2;
-        a.counter = buf.counters + 4 * level;
-        if ((e = launch_march(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
-        if (plan.ao && (e = launch_ao(a, s, log, plan.spec)) != cudaSuccess) return e;
-        if (plan.shadows && plan.lights_max > 0) {
-            a.counter = buf.counters + 4 * level + 1;
-            if ((e = launch_shadow(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+    a.emit = 0;  // reflection rays come from the reflect pass, right after each level's march
+    const uint32_t levels = plan.levels > buf.levels ? (uint32_t)buf.levels : plan.levels;
+    if (levels <= 1) {
+        if ((e = level_passes(plan, a, buf, tune, s, sm_count, log, 0, false)) != cudaSuccess) return e;
+    } else {
+        // primary level on `s`; its reflection rays fork the deeper levels onto the aux stream
+        WaveArgs a0 = a;
+        a0.b.nq_o = buf.qb_o;
+        a0.b.nq_d = buf.qb_d;
+        a0.level = 0;
+        a0.src = SRC_SAMPLES;
+        a0.n_items = plan.n_samples;
+        a0.n_items_dev = plan.jobs ? &plan.totals->n_samples : nullptr;
+        a0.b.nq_count = buf.counters + 2;
+        a0.counter = buf.counters;
+        if ((e = launch_march(a0, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+        if ((e = launch_reflect(a0, s, log)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(buf.ev_fork, s)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(buf.aux, buf.ev_fork, 0)) != cudaSuccess) return e;
+        for (uint32_t level = 1; level < levels; ++level) {
+            WaveArgs ak = a;
+            bool odd = (level & 1u) != 0;
+            ak.b.q_o = odd ? buf.qb_o : buf.qc_o;
+            ak.b.q_d = odd ? buf.qb_d : buf.qc_d;
+            ak.b.nq_o = odd ? buf.qc_o : buf.qb_o;
+            ak.b.nq_d = odd ? buf.qc_d : buf.qb_d;
+            ak.b.h_n = buf.h_n1;
+            ak.b.h_m = buf.h_m1;
+            ak.b.occ = buf.occ1;
+            ak.b.shadow = buf.shadow1;
+            if ((e = level_passes(plan, ak, buf, tune, buf.aux, sm_count, log, level, level + 1 < levels)) != cudaSuccess)
+                return e;
         }
-        if ((e = launch_shade(a, s, log)) != cudaSuccess) return e;
-        std::swap(a.b.q_o, a.b.nq_o);
-        std::swap(a.b.q_d, a.b.nq_d);
+        if ((e = cudaEventRecord(buf.ev_join, buf.aux)) != cudaSuccess) return e;
+        // the primary level's AO, shadows and shading overlap the reflection levels
+        a0.counter = buf.counters;
+        if (plan.ao && (e = launch_ao(a0, s, log, plan.spec)) != cudaSuccess) return e;
+        if (plan.shadows && plan.lights_max > 0) {
+            a0.counter = buf.counters + 1;
+            if ((e = launch_shadow(a0, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+        }
+        if ((e = launch_shade(a0, s, log)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s, buf.ev_join, 0)) != cudaSuccess) return e;
     }
     if ((e = launch_resolve(a, plan.n_slots, s, log)) != cudaSuccess) return e;
     if (!plan.post) return cudaSuccess;

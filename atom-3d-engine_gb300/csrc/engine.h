@@ -28,14 +28,24 @@ constexpr int N_COUNTERS = 64;  // [4L] march, [4L+1] shadow, [4L+2] next queue 
 
 // Device buffers of a pass sequence: ray queues and per-sample records for `cap` samples,
 // HDR / bloom arrays for `pixels` output pixels, and the work counters.
+// The primary level and the reflection levels run concurrently (the reflection levels on an
+// auxiliary stream, forked as soon as the primary hits exist), so the reflection levels have
+// their own hit records and a third ray queue: level 0 uses queue a and hit set 0, levels
+// 1, 2, 3 ... use queues b, c, b ... and hit set 1.
 struct PassBuffers {
     size_t cap = 0, lights = 0, levels = 0, pixels = 0;
-    float4 *qa_o = nullptr, *qa_d = nullptr, *qb_o = nullptr, *qb_d = nullptr, *h_n = nullptr;
+    float4 *qa_o = nullptr, *qa_d = nullptr, *qb_o = nullptr, *qb_d = nullptr, *qc_o = nullptr, *qc_d = nullptr;
+    float4* h_n = nullptr;
     uint2* h_m = nullptr;
     float *occ = nullptr, *shadow = nullptr;
+    float4* h_n1 = nullptr;  // hit set 1 (reflection levels)
+    uint2* h_m1 = nullptr;
+    float *occ1 = nullptr, *shadow1 = nullptr;
     float4 *lvl = nullptr, *term = nullptr;
     float4 *hdr = nullptr, *bright = nullptr, *blur = nullptr;
     uint32_t* counters = nullptr;
+    cudaStream_t aux = nullptr;  // reflection levels' stream
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void release();
     // Grows the buffers to hold at least the given sizes (contents are not kept).
     cudaError_t ensure(size_t cap, size_t lights, size_t levels, size_t pixels);

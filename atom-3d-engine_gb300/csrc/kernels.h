@@ -105,6 +105,7 @@ struct WaveArgs {
     uint32_t gi_nx, gi_ny, gi_nz, dirs_per_face;
     const float4* gather_dirs;
     uint32_t aov_mode;          // RenderMode for the AOV resolve
+    uint32_t emit;              // shade appends reflection rays (else a reflect pass did)
 };
 
 // Status bits written by kernels.
@@ -112,8 +113,10 @@ enum : uint32_t { ST_TAPE_TIMEOUT = 1u, ST_TAPE_CORRUPT = 2u };
 
 #ifndef __CUDACC_RTC__
 // Kernel kinds the launch log attributes device time to.
+// (the primary level's march / AO / shadow passes apart from the reflection levels').
 enum KernelKind : uint32_t {
-    KK_MARCH = 0, KK_AO, KK_SHADOW, KK_SHADE, KK_RESOLVE, KK_POST, KK_AOV, KK_GI, KK_OTHER, KK_COUNT
+    KK_MARCH = 0, KK_AO, KK_SHADOW, KK_SHADE, KK_RESOLVE, KK_POST, KK_AOV, KK_GI, KK_OTHER,
+    KK_MARCH_REFL, KK_AO_REFL, KK_SHADOW_REFL, KK_COUNT
 };
 
 // Counts launches and, when a recorder is attached, brackets each with CUDA events.
@@ -141,6 +144,8 @@ cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log, const S
 cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
                           const SpecKernels* spec = nullptr);
 cudaError_t launch_shade(const WaveArgs& a, cudaStream_t s, LaunchLog* log);
+// Reflection rays of the level's hits (the rays shade would append), into the next queue.
+cudaError_t launch_reflect(const WaveArgs& a, cudaStream_t s, LaunchLog* log);
 // Pixel slots of the jobs (n_slots when known on the host, else capacity + a.totals).
 cudaError_t launch_resolve(const WaveArgs& a, uint32_t n_slots, cudaStream_t s, LaunchLog* log);
 // AOV modes: display value per pixel-centre hit of job 0 (lib.rs:1185-1217), written as RGBA f32.

@@ -90,6 +90,7 @@ __device__ __forceinline__ void shade_slots(const WaveArgs& a, uint32_t slot, bo
         }
     }
     // append reflection rays to the next level's queue (one atomic per warp)
+    if (!a.emit) return;
     const uint32_t lane = threadIdx.x & 31u;
     unsigned mask = __ballot_sync(0xFFFFFFFFu, emit);
     if (mask) {
@@ -109,6 +110,53 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_shade(const __grid_constant__
     const uint32_t n = item_count(a);
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
         shade_slots(a, base + threadIdx.x, base + threadIdx.x < n);  // block-uniform trip count
+}
+
+// The reflection ray shade_hit recurses into (lib.rs:1336-1343), emitted as soon as the level's
+// hits exist so the next level can march while this level's AO / shadows / shading run.
+__device__ __forceinline__ void reflect_slots(const WaveArgs& a, uint32_t slot, bool active) {
+    bool emit = false;
+    V rorig{0.f, 0.f, 0.f}, rdir{0.f, 0.f, 0.f};
+    uint32_t sample = 0, job = 0;
+    if (active) {
+        uint2 hm = a.b.h_m[slot];
+        if (hm.x != NIL) {
+            float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
+            job = a.jobs ? __float_as_uint(d4.w) : 0u;
+            const Tape T = tape_view(job_ref(a, job).tape);
+            const TapeHeader& h = *T.h;
+            const DevMaterial& m = T.mat[hm.x % h.n_materials];
+            if (a.level < h.bounces && m.reflectivity > 0.0f) {
+                sample = __float_as_uint(o4.w);
+                float4 hn4 = a.b.h_n[slot];
+                V rd{d4.x, d4.y, d4.z};
+                V hp = V{o4.x, o4.y, o4.z} + scale(rd, hn4.w);
+                V hn{hn4.x, hn4.y, hn4.z};
+                rdir = normalize(reflect(rd, hn));
+                rorig = hp + scale(hn, fmaxf(h.normal_h * 2.0f, 0.02f));
+                emit = true;
+            }
+        }
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned mask = __ballot_sync(0xFFFFFFFFu, emit);
+    if (mask) {
+        uint32_t base = 0;
+        int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(a.b.nq_count, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (emit) {
+            uint32_t q = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+            a.b.nq_o[q] = make_float4(rorig.x, rorig.y, rorig.z, __uint_as_float(sample));
+            a.b.nq_d[q] = make_float4(rdir.x, rdir.y, rdir.z, __uint_as_float(job));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SHADE_THREADS) k_reflect(const __grid_constant__ WaveArgs a) {
+    const uint32_t n = item_count(a);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+        reflect_slots(a, base + threadIdx.x, base + threadIdx.x < n);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -421,7 +469,7 @@ unsigned grid_for(uint64_t n, int threads, uint32_t cap = 0) {
 cudaError_t launch_march(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
                          const SpecKernels* spec) {
     static const PersistentSet set = MM3E_PERSISTENT_SET(k_march);
-    LogScope sc(log, KK_MARCH, s, 1);
+    LogScope sc(log, a.level == 0 ? KK_MARCH : KK_MARCH_REFL, s, 1);
     if (spec && spec->march && !a.jobs) return launch_persistent_spec(spec->march, *spec, a, s, sm_count, 1);
     return launch_persistent(set, a, t, s, sm_count, 1);
 }
@@ -429,7 +477,7 @@ cudaError_t launch_march(const WaveArgs& a, const TuneParams& t, cudaStream_t s,
 cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s, int sm_count, LaunchLog* log,
                           const SpecKernels* spec) {
     static const PersistentSet set = MM3E_PERSISTENT_SET(k_shadow);
-    LogScope sc(log, KK_SHADOW, s, 1);
+    LogScope sc(log, a.level == 0 ? KK_SHADOW : KK_SHADOW_REFL, s, 1);
     uint32_t per = a.lights_max ? a.lights_max : 1;
     if (spec && spec->shadow && !a.jobs) return launch_persistent_spec(spec->shadow, *spec, a, s, sm_count, per);
     return launch_persistent(set, a, t, s, sm_count, per);
@@ -438,7 +486,7 @@ cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s
 // Non-persistent kernels are sized for the largest queue (a.n_items) and read the live count
 // from n_items_dev when set.
 cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log, const SpecKernels* spec) {
-    LogScope sc(log, KK_AO, s, 1);
+    LogScope sc(log, a.level == 0 ? KK_AO : KK_AO_REFL, s, 1);
     unsigned grid = grid_for(a.n_items, SHADE_THREADS, a.grid_cap);
     if (spec && spec->ao && !a.jobs) {
         WaveArgs arg = a;
@@ -452,6 +500,12 @@ cudaError_t launch_ao(const WaveArgs& a, cudaStream_t s, LaunchLog* log, const S
 cudaError_t launch_shade(const WaveArgs& a, cudaStream_t s, LaunchLog* log) {
     LogScope sc(log, KK_SHADE, s, 1);
     k_shade<<<grid_for(a.n_items, SHADE_THREADS, a.grid_cap), SHADE_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reflect(const WaveArgs& a, cudaStream_t s, LaunchLog* log) {
+    LogScope sc(log, KK_SHADE, s, 1);
+    k_reflect<<<grid_for(a.n_items, SHADE_THREADS, a.grid_cap), SHADE_THREADS, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -300,7 +300,8 @@ int mm3e_ctx_get_tuning(mm3e_ctx* ctx, mm3e_tuning* t);
 /* Per-kernel device time: when enabled, every pass is bracketed with CUDA events on the
  * context's stream (batched pass sequences then run without CUDA graphs).
  * mm3e_ctx_kernel_times waits for the recorded passes, writes one entry per kernel kind that
- * ran (march, ao, shadow, shade, resolve, post, aov, gi, other) and clears the totals. */
+ * ran (march, ao, shadow, shade, resolve, post, aov, gi, other, march_refl, ao_refl,
+ * shadow_refl: the *_refl kinds are the reflection levels' passes) and clears the totals. */
 typedef struct mm3e_kernel_time {
     char name[16];
     uint32_t launches;

@@ -214,8 +214,9 @@ void put_counts(const OpCounts& t, uint64_t* out) {
 // [fp32, add, mul, cmp, minmax, div, sqrt, trans, field_evals, dual_evals,
 //  primary_rays, reflection_rays, shadow_rays, gi_rays].
 // Blocks: 0 render phase (tape interpretation + shading), 1 post phase (bloom + tone map),
-// then, when `n_blocks` is 6, the render phase split by kernel: 2 march (+ hit normal), 3 AO,
-// 4 soft shadow, 5 shading (camera rays, BRDF / IBL / GI / fog, reflection set-up).
+// then the render phase split by kernel: 2 march (+ hit normal), 3 AO, 4 soft shadow of the
+// primary level, 5 shading (camera rays, BRDF / IBL / GI / fog, reflection set-up, all levels),
+// 6 march, 7 AO, 8 soft shadow of the reflection levels (as many blocks as `n_blocks` asks).
 int oracle_count_frame_blocks(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, uint64_t* counts,
                               int n_blocks) {
     Scene<CountF> s = scene_from_desc<CountF>(*d);

@@ -7,8 +7,9 @@
 //   div, sqrt and transcendentals (sin/cos/tan/exp/pow/acos) are counted separately and are not
 //   part of the FP32-pipe numerator.
 // Counters are thread-local; the render driver sums them over worker threads. They are kept per
-// render phase (PH_MARCH: primary/reflection march + hit normal, PH_AO, PH_SHADOW, PH_SHADE:
-// everything else), matching the kernels the CUDA path splits a frame into.
+// render phase (PH_MARCH: march + hit normal, PH_AO, PH_SHADOW, each for the primary level and
+// for the reflection levels, PH_SHADE: everything else), matching the kernels the CUDA path
+// splits a frame into.
 #pragma once
 #include <cstdint>
 

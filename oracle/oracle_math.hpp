@@ -99,7 +99,11 @@ template <class T> inline uint64_t o_to_usize(T x) {
 template <class T> inline T o_inf() { return T(std::numeric_limits<float>::infinity()); }
 
 // Render phases the counting instantiation attributes work to.
-enum : int { PH_MARCH = 0, PH_AO = 1, PH_SHADOW = 2, PH_SHADE = 3, PH_COUNT = 4 };
+// The first four are the primary level's; the *_REFL phases are the reflection levels' passes.
+enum : int {
+    PH_MARCH = 0, PH_AO = 1, PH_SHADOW = 2, PH_SHADE = 3,
+    PH_MARCH_REFL = 4, PH_AO_REFL = 5, PH_SHADOW_REFL = 6, PH_COUNT = 7
+};
 
 // Event hooks for the counting instantiation (no-ops for float / double).
 template <class T> struct Hooks {

@@ -176,12 +176,13 @@ COUNT_KEYS = ["fp32", "add", "mul", "cmp", "minmax", "div", "sqrt", "trans", "fi
               "primary_rays", "reflection_rays", "shadow_rays", "gi_rays"]
 
 
-COUNT_BLOCKS = ("render", "post", "march", "ao", "shadow", "shade")
+COUNT_BLOCKS = ("render", "post", "march", "ao", "shadow", "shade", "march_refl", "ao_refl", "shadow_refl")
 
 
 def count_frame(handle, cam, threads=None):
     """Algorithmic work of one frame (f32 op counts, rays): {"render", "post"} plus the render
-    phase split by kernel ("march" incl. hit normals, "ao", "shadow", "shade")."""
+    phase split by kernel ("march" incl. hit normals, "ao", "shadow" of the primary level,
+    "shade" of all levels, "march_refl", "ao_refl", "shadow_refl" of the reflection levels)."""
     out = (C.c_uint64 * (14 * len(COUNT_BLOCKS)))()
     lib().oracle_count_frame_blocks(C.addressof(handle.desc), C.addressof(cam), threads or threads_default(), out,
                                     len(COUNT_BLOCKS))

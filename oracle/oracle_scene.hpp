@@ -648,8 +648,9 @@ template <class T> struct World {
 // ------------------------------------------------------------------------------------------
 // lib.rs render path
 // ------------------------------------------------------------------------------------------
-template <class T> inline Hit<T> march_scene(const Scene<T>& s, const World<T>& w, bool dual_safe, const Ray<T>& ray) {
-    PhaseScope<T> ph(PH_MARCH);
+template <class T>
+inline Hit<T> march_scene(const Scene<T>& s, const World<T>& w, bool dual_safe, const Ray<T>& ray, uint32_t depth = 0) {
+    PhaseScope<T> ph(depth == 0 ? PH_MARCH : PH_MARCH_REFL);
     if (dual_safe) return s.marcher.march_with(w, [&](V3<T> p) { return normal_dual(s, p); }, ray);
     return s.marcher.march_with(w, [&](V3<T> p) { return s.marcher.normal(w, p); }, ray);
 }
@@ -713,7 +714,7 @@ inline V3<T> shade_hit(const Scene<T>& s, const World<T>& w, const Hit<T>& hit, 
     V3<T> view = scale(ray.dir, T(-1));
     T occ = T(1);
     if (s.ao) {
-        PhaseScope<T> ph(PH_AO);
+        PhaseScope<T> ph(depth == 0 ? PH_AO : PH_AO_REFL);
         occ = s.marcher.ambient_occlusion(w, hit.pos, hit.normal);
     }
     V3<T> gi = s.gi ? s.gi->sample(hit.pos, normal) : zero3<T>();
@@ -729,7 +730,7 @@ inline V3<T> shade_hit(const Scene<T>& s, const World<T>& w, const Hit<T>& hit, 
             T max_t = o_min(l_dist, s.marcher.max_dist);
             T lift = o_max(s.marcher.normal_h * T(2), OL(0.01));
             Hooks<T>::shadow_ray();
-            PhaseScope<T> ph(PH_SHADOW);
+            PhaseScope<T> ph(depth == 0 ? PH_SHADOW : PH_SHADOW_REFL);
             shadow = s.marcher.soft_shadow(w, hit.pos + scale(hit.normal, lift), l_dir, max_t, light.shadow_k(l_dist));
         }
         if (shadow <= T(0)) continue;
@@ -752,7 +753,7 @@ inline V3<T> shade_hit(const Scene<T>& s, const World<T>& w, const Hit<T>& hit, 
 template <class T> V3<T> trace(const Scene<T>& s, const World<T>& w, const Ray<T>& ray, uint32_t depth, bool dual_safe) {
     if (depth == 0) Hooks<T>::primary_ray();
     else Hooks<T>::reflection_ray();
-    Hit<T> hit = march_scene(s, w, dual_safe, ray);
+    Hit<T> hit = march_scene(s, w, dual_safe, ray, depth);
     if (!hit.hit) return sky(ray.dir, s.sun_dir);
     return shade_hit(s, w, hit, ray, depth, dual_safe);
 }

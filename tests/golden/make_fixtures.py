@@ -4,8 +4,9 @@
 
 * workload_counts.json  algorithmic work per frame of the benchmark workloads (the oracle's
                         counting instantiation: f32 ops, field evaluations, rays), render and
-                        post phases and the render phase split by kernel (march, ao, shadow,
-                        shade); bench.py reads it for Mrays/s and the roofline.
+                        post phases and the render phase split by kernel and level (march,
+                        ao, shadow, shade, march_refl, ao_refl, shadow_refl); bench.py reads
+                        it for Mrays/s and the roofline.
 * oracle_frames.npz     small RGB8 frames of the parity scenes rendered by the oracle; the CPU
                         suite checks the oracle still reproduces them bit-exactly and the GPU
                         suite compares the CUDA path against them.
