@@ -403,6 +403,7 @@ int mm3e_autotune(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, uint32_t repeat
                     report[k].tuning.block = b;
                     report[k].tuning.tile_wlog = wl;
                     report[k].tuning.unroll = u;
+                    report[k].tuning.min_blocks = keep.min_blocks;
                     report[k].device_ms = ms;
                 }
                 ++k;
@@ -416,6 +417,7 @@ int mm3e_autotune(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, uint32_t repeat
         best->block = best_t.block;
         best->tile_wlog = best_t.tile_wlog;
         best->unroll = best_t.unroll;
+        best->min_blocks = best_t.min_blocks;
     }
     if (n_report) *n_report = k;
     return MM3E_OK;

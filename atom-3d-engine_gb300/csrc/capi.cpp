@@ -573,11 +573,13 @@ int mm3e_ctx_set_tuning(mm3e_ctx* ctx, const mm3e_tuning* t) {
     if (t->block != 128 && t->block != 256) return fail(ctx, MM3E_ERR_INVALID, "block must be 128 or 256");
     if (t->tile_wlog > 5) return fail(ctx, MM3E_ERR_INVALID, "tile_wlog must be 0..5");
     if (t->unroll != 1 && t->unroll != 2) return fail(ctx, MM3E_ERR_INVALID, "unroll must be 1 or 2");
+    if (t->min_blocks > 16) return fail(ctx, MM3E_ERR_INVALID, "min_blocks must be 0..16");
     cudaError_t e = cudaStreamSynchronize(ctx->stream);  // frames in flight keep their buffers
     if (e != cudaSuccess) return cuda_fail(ctx, e, "set tuning");
     ctx->tune.block = t->block;
     ctx->tune.tile_wlog = t->tile_wlog;
     ctx->tune.unroll = t->unroll;
+    ctx->tune.min_blocks = t->min_blocks;
     return MM3E_OK;
 }
 
@@ -586,6 +588,7 @@ int mm3e_ctx_get_tuning(mm3e_ctx* ctx, mm3e_tuning* t) {
     t->block = ctx->tune.block;
     t->tile_wlog = ctx->tune.tile_wlog;
     t->unroll = ctx->tune.unroll;
+    t->min_blocks = ctx->tune.min_blocks;
     return MM3E_OK;
 }
 
@@ -952,7 +955,7 @@ int mm3e_scene_specialize(mm3e_scene* s, int mode, double* compile_ms) {
     if (mode == 1 && spec_size(s->low.blob).objects > SPEC_AUTO_MAX_OBJECTS) return MM3E_OK;  // interpreter is faster
     bool smem = s->low.blob.size() <= 96 * 1024;
     uint32_t block = c->tune.block, unroll = c->tune.unroll;
-    std::string src = spec_source(s->low.blob, block, unroll, smem);
+    std::string src = spec_source(s->low.blob, block, unroll, smem, c->tune.min_blocks);
     std::unique_ptr<SpecModule> m(new SpecModule());
     m->kernels.block = block;
     m->kernels.smem_tape = smem;
@@ -970,7 +973,7 @@ int mm3e_scene_spec_source(const mm3e_scene_desc* desc, char* out, size_t cap, s
     LoweredScene low;
     int rc = lower_scene(*desc, nullptr, 0, low, msg);
     if (rc) return rc;
-    std::string src = spec_source(low.blob, 128, 1, low.blob.size() <= 96 * 1024);
+    std::string src = spec_source(low.blob, 128, 1, low.blob.size() <= 96 * 1024, 0);
     if (len) *len = src.size();
     if (out && cap) {
         size_t n = src.size() < cap - 1 ? src.size() : cap - 1;
@@ -988,7 +991,7 @@ int mm3e_spec_compile_check(const mm3e_scene_desc* desc, char* err, size_t err_l
     if (rc) return rc;
     auto t0 = std::chrono::steady_clock::now();
     std::vector<char> cubin;
-    std::string e = spec_compile(spec_source(low.blob, 128, 1, low.blob.size() <= 96 * 1024), cubin);
+    std::string e = spec_compile(spec_source(low.blob, 128, 1, low.blob.size() <= 96 * 1024, 0), cubin);
     if (compile_ms) *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (err && err_len) {
         std::strncpy(err, e.c_str(), err_len - 1);

@@ -65,6 +65,7 @@ struct TuneParams {
     uint32_t block = 128;    // threads per CTA: 128 or 256
     uint32_t tile_wlog = 3;  // pixel tile 2^tile_wlog x 2^(5 - tile_wlog): 8x4 by default
     uint32_t unroll = 1;     // field samples per lane between refills: 1 or 2
+    uint32_t min_blocks = 0; // specialised kernels: CTAs per SM the register budget must allow (0: free)
 };
 
 // Device buffers of one pass sequence.

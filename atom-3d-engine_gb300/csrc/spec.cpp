@@ -131,7 +131,8 @@ SpecSize spec_size(const std::vector<unsigned char>& blob) {
     return z;
 }
 
-std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, uint32_t unroll, bool smem_tape) {
+std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, uint32_t unroll, bool smem_tape,
+                        uint32_t min_blocks) {
     const TapeHeader* h = reinterpret_cast<const TapeHeader*>(blob.data());
     const DevObject* obj = reinterpret_cast<const DevObject*>(blob.data() + h->off_objects);
     const DevSegment* seg = reinterpret_cast<const DevSegment*>(blob.data() + h->off_segments);
@@ -220,10 +221,11 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
           "struct Field_ {\n    static __device__ __forceinline__ Field eval(const Tape& T, V p) { return spec::eval(T, p); }\n};\n"
           "}  // namespace spec\n}  // namespace mm3e\n";
     const int tm = smem_tape ? 0 : 1;
-    os << "extern \"C\" __global__ void __launch_bounds__(" << block
+    const std::string bounds = min_blocks ? std::to_string(block) + ", " + std::to_string(min_blocks) : std::to_string(block);
+    os << "extern \"C\" __global__ void __launch_bounds__(" << bounds
        << ") mm3e_spec_march(const __grid_constant__ mm3e::WaveArgs a) {\n    mm3e::wave::march_body<" << tm << ", "
        << unroll << ", mm3e::spec::Field_>(a);\n}\n"
-       << "extern \"C\" __global__ void __launch_bounds__(" << block
+       << "extern \"C\" __global__ void __launch_bounds__(" << bounds
        << ") mm3e_spec_shadow(const __grid_constant__ mm3e::WaveArgs a) {\n    mm3e::wave::shadow_body<" << tm << ", "
        << unroll << ", mm3e::spec::Field_>(a);\n}\n"
        << "extern \"C\" __global__ void __launch_bounds__(128) mm3e_spec_ao(const __grid_constant__ mm3e::WaveArgs a) {\n"

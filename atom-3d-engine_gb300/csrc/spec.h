@@ -23,7 +23,8 @@
 namespace mm3e {
 
 // Source of the specialised program for a lowered tape blob (host copy).
-std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, uint32_t unroll, bool smem_tape);
+std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, uint32_t unroll, bool smem_tape,
+                        uint32_t min_blocks);
 
 // Size of the generated field: objects it inlines and CSG program ops among them. Every inlined
 // object is its own code (the interpreter shares one copy per primitive kind), so past a few

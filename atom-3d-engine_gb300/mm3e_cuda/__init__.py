@@ -67,13 +67,13 @@ class Context:
         return {"sm_count": sm.value, "clock_khz": clk.value}
 
     # ---- launch shape, profiling -------------------------------------------------------------
-    def set_tuning(self, block=128, tile_wlog=3, unroll=1):
-        self.check(lib().mm3e_ctx_set_tuning(self._ptr, C.byref(abi.Tuning(block, tile_wlog, unroll))))
+    def set_tuning(self, block=128, tile_wlog=3, unroll=1, min_blocks=0):
+        self.check(lib().mm3e_ctx_set_tuning(self._ptr, C.byref(abi.Tuning(block, tile_wlog, unroll, min_blocks))))
 
     def get_tuning(self):
         t = abi.Tuning()
         self.check(lib().mm3e_ctx_get_tuning(self._ptr, C.byref(t)))
-        return {"block": t.block, "tile_wlog": t.tile_wlog, "unroll": t.unroll}
+        return {"block": t.block, "tile_wlog": t.tile_wlog, "unroll": t.unroll, "min_blocks": t.min_blocks}
 
     def set_profiling(self, on=True):
         self.check(lib().mm3e_ctx_set_profiling(self._ptr, 1 if on else 0))
@@ -118,8 +118,10 @@ class Context:
         n = C.c_uint32()
         self.check(lib().mm3e_autotune(self._ptr, jobs, len(jobs), repeats, C.byref(best), rep, 64, C.byref(n)))
         table = [({"block": rep[i].tuning.block, "tile_wlog": rep[i].tuning.tile_wlog,
-                   "unroll": rep[i].tuning.unroll}, rep[i].device_ms) for i in range(n.value)]
-        return {"block": best.block, "tile_wlog": best.tile_wlog, "unroll": best.unroll}, table
+                   "unroll": rep[i].tuning.unroll, "min_blocks": rep[i].tuning.min_blocks}, rep[i].device_ms)
+                 for i in range(n.value)]
+        return {"block": best.block, "tile_wlog": best.tile_wlog, "unroll": best.unroll,
+                "min_blocks": best.min_blocks}, table
 
     # ---- mesh -> SDF bake -------------------------------------------------------------------------
     def bake_mesh_sdf(self, positions, triangles, resolution, padding, device_out=None):

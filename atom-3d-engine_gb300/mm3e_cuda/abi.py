@@ -97,7 +97,7 @@ class RenderStats(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("block", C.c_uint32), ("tile_wlog", C.c_uint32), ("unroll", C.c_uint32)]
+    _fields_ = [("block", C.c_uint32), ("tile_wlog", C.c_uint32), ("unroll", C.c_uint32), ("min_blocks", C.c_uint32)]
 
 
 class KernelTime(C.Structure):

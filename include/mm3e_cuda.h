@@ -290,9 +290,11 @@ int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
 
 /* Launch shape of the march and soft-shadow passes: threads per CTA (128 or 256), pixel tile
  * of 32 pixels 2^tile_wlog wide (tile_wlog 0..5; 3 = 8x4), and field samples per lane between
- * work refills (unroll 1 or 2). Results do not depend on it. mm3e_autotune picks one. */
+ * work refills (unroll 1 or 2); min_blocks (0..16) asks the compiler of scene-specialised
+ * kernels to fit that many CTAs per SM in the register file (0: its own choice). Results do not
+ * depend on it. mm3e_autotune picks block / tile / unroll. */
 typedef struct mm3e_tuning {
-    uint32_t block, tile_wlog, unroll;
+    uint32_t block, tile_wlog, unroll, min_blocks;
 } mm3e_tuning;
 int mm3e_ctx_set_tuning(mm3e_ctx* ctx, const mm3e_tuning* t);
 int mm3e_ctx_get_tuning(mm3e_ctx* ctx, mm3e_tuning* t);
