@@ -1000,6 +1000,73 @@ int mm3e_spec_compile_check(const mm3e_scene_desc* desc, char* err, size_t err_l
     return (e.empty() || e.compare(0, 4, "LOG:") == 0) ? MM3E_OK : MM3E_ERR_UNSUPPORTED;
 }
 
+int mm3e_render_film(mm3e_scene* s, const mm3e_camera* camera, float aperture_radius, float focus_distance,
+                     float* beauty3, float* foreground3, float* alpha, float* depth, float* normals3,
+                     uint32_t* material_ids) {
+    if (!s || !camera) return MM3E_ERR_INVALID;
+    mm3e_ctx* c = s->ctx;
+    // Lens::validate (camera.rs:25-34)
+    if (!std::isfinite(aperture_radius) || aperture_radius < 0.0f)
+        return fail(c, MM3E_ERR_INVALID, "aperture_radius must be finite and nonnegative");
+    if (!std::isfinite(focus_distance) || focus_distance <= 0.0f)
+        return fail(c, MM3E_ERR_INVALID, "focus_distance must be finite and positive");
+    size_t n = (size_t)s->low.width * s->low.height;
+    if (n == 0) return MM3E_OK;
+    cudaSetDevice(c->device);
+    int rc = ensure_frame_buffers(s, true);
+    if (rc) return rc;
+    LaunchLog log = c->prof.log();
+    PassPlan p = scene_plan(s, s->d_tape, (uint32_t)s->low.blob.size(), *camera, MM3E_FB_RGBA_F32, nullptr);
+    p.spec = s->spec_kernels();
+    p.post = false;
+    p.film = true;
+    p.job0.lens_radius = aperture_radius;
+    p.job0.focus_distance = focus_distance;
+    CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, &log));
+    std::vector<float4> hdr(n), fg(n), hn(n), qd(n);
+    std::vector<uint2> hm(n);
+    CK(cudaMemcpyAsync(hdr.data(), s->buf.hdr, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(fg.data(), s->buf.bright, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    // geometric AOVs: the centre pinhole ray of every pixel (film.rs:111-116)
+    WaveArgs a;
+    rc = march_centers(s, camera, s->d_tape, (uint32_t)s->low.blob.size(), false, &log, a);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(hn.data(), s->buf.h_n, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hm.data(), s->buf.h_m, n * sizeof(uint2), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(qd.data(), s->buf.qa_d, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    rc = check_status(s);
+    if (rc) return rc;
+    const float* eye = camera->eye;
+    const float* fwd = camera->forward;
+    for (size_t i = 0; i < n; ++i) {
+        if (beauty3) {
+            beauty3[3 * i] = hdr[i].x;
+            beauty3[3 * i + 1] = hdr[i].y;
+            beauty3[3 * i + 2] = hdr[i].z;
+        }
+        if (alpha) alpha[i] = hdr[i].w;
+        if (foreground3) {
+            foreground3[3 * i] = fg[i].x;
+            foreground3[3 * i + 1] = fg[i].y;
+            foreground3[3 * i + 2] = fg[i].z;
+        }
+        bool hit = hm[i].x != NIL;
+        if (depth) {
+            // (hit.pos - eye) . forward with hit.pos = eye + dir * t (Ray::at), in binary32
+            float t = hn[i].w;
+            float px = eye[0] + qd[i].x * t, py = eye[1] + qd[i].y * t, pz = eye[2] + qd[i].z * t;
+            depth[i] = hit ? (px - eye[0]) * fwd[0] + (py - eye[1]) * fwd[1] + (pz - eye[2]) * fwd[2] : INFINITY;
+        }
+        if (normals3) {
+            normals3[3 * i] = hit ? hn[i].x : 0.0f;
+            normals3[3 * i + 1] = hit ? hn[i].y : 0.0f;
+            normals3[3 * i + 2] = hit ? hn[i].z : 0.0f;
+        }
+        if (material_ids) material_ids[i] = hit ? hm[i].x : NIL;
+    }
+    return MM3E_OK;
+}
+
 // Allocation-free ray queries: the scratch lives in noalloc.cu's fixed __device__ array.
 int mm3e_march_rays_noalloc(mm3e_scene* s, const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat,
                             uint32_t* d_steps) {

@@ -164,6 +164,8 @@ WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tun
     a.b.lvl = buf.lvl;
     a.b.term = buf.term;
     a.b.hdr = buf.hdr;
+    a.b.fg = buf.bright;
+    a.film = plan.film ? 1u : 0u;
     return a;
 }
 }  // namespace

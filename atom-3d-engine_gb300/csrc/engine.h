@@ -91,6 +91,7 @@ struct PassPlan {
     bool ao = false, shadows = false, bloom = false, post = true;
     bool clear_status = true;       // also clear the status word with the work counters
     const SpecKernels* spec = nullptr;  // scene-specialised march / shadow / AO (single job only)
+    bool film = false;              // resolve coverage + foreground (into buf.bright) too
 };
 
 // Enqueues the passes on `s`: counters cleared, march / AO / shadow / shade per level,

@@ -53,6 +53,7 @@ struct FrameJob {
     uint32_t n_lights;
     uint32_t bloom_radius, format, flags;
     float threshold, intensity, exposure;
+    float lens_radius, focus_distance;  // thin lens (camera.rs Lens); radius 0: pinhole
 };
 
 // Sizes of a device job table (read by the kernels when the table is on the device).
@@ -82,6 +83,7 @@ struct WaveBuffers {
     float4* lvl;         // per sample and level: [(level * cap + sample) * 2 + {0, 1}]
     float4* term;        // per sample: terminal radiance xyz, w = level it ended at (uint bits)
     float4* hdr;         // per output pixel (job.pixel_base + y * w + x)
+    float4* fg;          // film: premultiplied foreground per output pixel
 };
 
 struct WaveArgs {
@@ -107,6 +109,7 @@ struct WaveArgs {
     const float4* gather_dirs;
     uint32_t aov_mode;          // RenderMode for the AOV resolve
     uint32_t emit;              // shade appends reflection rays (else a reflect pass did)
+    uint32_t film;              // resolve also writes coverage (hdr.w) and the foreground (b.fg)
 };
 
 // Status bits written by kernels.

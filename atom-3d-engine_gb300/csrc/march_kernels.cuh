@@ -138,6 +138,50 @@ __device__ __forceinline__ bool tiled_pixel(uint32_t p, const FrameJob& J, uint3
     return x < J.width && y < J.height;
 }
 
+// film.rs:218-224
+__device__ __forceinline__ uint32_t film_hash(uint32_t v) {
+    v ^= v >> 16;
+    v *= 0x7feb352du;
+    v ^= v >> 15;
+    v *= 0x846ca68bu;
+    return v ^ (v >> 16);
+}
+
+// Thin-lens ray of AA sample (sx, sy) of pixel (x, y): film.rs:199-215's jittered aperture cell,
+// camera.rs:92-102's concentric disk and camera.rs:71-90's focus-plane ray; `rd` holds the
+// pinhole direction through the image sample on entry.
+__device__ __forceinline__ void lens_ray(const FrameJob& J, uint32_t x, uint32_t y, uint32_t sx, uint32_t sy,
+                                         uint32_t n, V& ro, V& rd) {
+    uint32_t pixel_seed = film_hash(x ^ film_hash(y));
+    uint64_t n64 = n;
+    uint32_t cell_x = (uint32_t)(((uint64_t)sx + sy + pixel_seed) % n64);
+    uint32_t cell_y = (uint32_t)(((uint64_t)sx + 2ull * sy + film_hash(pixel_seed)) % n64);
+    uint32_t seed = film_hash(pixel_seed ^ film_hash(sx) ^ film_hash(sy + 0xa511e9b3u));
+    float nf = (float)n;
+    float u = ((float)cell_x + (float)(seed >> 8) * (1.0f / 16777216.0f)) / nf;
+    float v = ((float)cell_y + (float)(film_hash(seed) >> 8) * (1.0f / 16777216.0f)) / nf;
+    float px = 2.0f * u - 1.0f, py = 2.0f * v - 1.0f;
+    float dx = 0.0f, dy = 0.0f;
+    if (!(px == 0.0f && py == 0.0f)) {
+        float radius, theta;
+        if (fabsf(px) > fabsf(py)) {
+            radius = px;
+            theta = 0.785398163397448309616f * (py / px);
+        } else {
+            radius = py;
+            theta = 1.57079632679489661923f - 0.785398163397448309616f * (px / py);
+        }
+        dx = radius * cosf(theta);
+        dy = radius * sinf(theta);
+    }
+    float r = J.lens_radius;
+    V eye = ld3(J.cam.eye);
+    V origin = eye + scale(ld3(J.cam.right), dx * r) + scale(ld3(J.cam.up), dy * r);
+    V focus = eye + scale(rd, J.focus_distance / dot(rd, ld3(J.cam.fwd)));
+    ro = origin;
+    rd = normalize(focus - origin);
+}
+
 __device__ __forceinline__ V tetra_k(uint32_t t) {
     // k0 = (1,-1,-1), k1 = (-1,-1,1), k2 = (-1,1,-1), k3 = (1,1,1) (march.rs:212-223)
     return V{(t == 0u || t == 3u) ? 1.0f : -1.0f, (t >= 2u) ? 1.0f : -1.0f, (t == 1u || t == 3u) ? 1.0f : -1.0f};
@@ -201,6 +245,7 @@ __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveAr
         float ox = ((float)sx + 0.5f) / nf, oy = ((float)sy + 0.5f) / nf;
         L.ro = ld3(J.cam.eye);
         L.rd = inside ? camera_dir(J.cam, (float)x + ox, (float)y + oy, J.width, J.height) : V{0.f, 0.f, 1.f};
+        if (inside && aa > 1u && J.lens_radius > 0.0f) lens_ray(J, x, y, sx, sy, aa, L.ro, L.rd);
         a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
         a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, __uint_as_float(job));
         if (!inside) {  // padding pixel of the last tile row / column

@@ -171,7 +171,8 @@ __device__ __forceinline__ void resolve_slot(const WaveArgs& a, uint32_t slot, u
     uint32_t spp = J.spp;
     V fog = ld3(h->fog);
     float density = h->fog_density;
-    V acc{0.f, 0.f, 0.f};
+    V acc{0.f, 0.f, 0.f}, fg{0.f, 0.f, 0.f};
+    uint32_t hits = 0;
     for (uint32_t sub = 0; sub < spp; ++sub) {
         uint32_t s = J.sample_base + p * spp + sub;
         float4 t4 = a.b.term[s];
@@ -186,9 +187,21 @@ __device__ __forceinline__ void resolve_slot(const WaveArgs& a, uint32_t slot, u
             v = apply_fog(r, fog, B.w, density);
         }
         acc = acc + v;
+        if (a.film && a.b.h_m[s].x != NIL) {  // film.rs:182-190: coverage of primary hits
+            fg = fg + v;
+            hits += 1;
+        }
     }
-    V o = scale(acc, 1.0f / (float)spp);
-    a.b.hdr[(size_t)J.pixel_base + (size_t)y * J.width + x] = make_float4(o.x, o.y, o.z, 1.0f);
+    float inv = 1.0f / (float)spp;
+    V o = scale(acc, inv);
+    size_t px = (size_t)J.pixel_base + (size_t)y * J.width + x;
+    if (a.film) {
+        V f = scale(fg, inv);
+        a.b.hdr[px] = make_float4(o.x, o.y, o.z, (float)hits * inv);
+        a.b.fg[px] = make_float4(f.x, f.y, f.z, 0.0f);
+    } else {
+        a.b.hdr[px] = make_float4(o.x, o.y, o.z, 1.0f);
+    }
 }
 
 __global__ void __launch_bounds__(SHADE_THREADS) k_resolve(const __grid_constant__ WaveArgs a, uint32_t n_slots) {

@@ -256,6 +256,21 @@ class CompiledScene:
         return {"t": t.reshape(shape), "mat": m.reshape(shape), "steps": s.reshape(shape),
                 "normal": nrm.reshape(shape + (3,))}
 
+    def render_film(self, camera, aperture_radius=0.0, focus_distance=1.0):
+        """render_film: dict of beauty / foreground (h, w, 3), alpha / depth (h, w), normals
+        (h, w, 3), material_ids (h, w)."""
+        h, w = self.height, self.width
+        out = {"beauty": np.zeros((h, w, 3), np.float32), "foreground": np.zeros((h, w, 3), np.float32),
+               "alpha": np.zeros((h, w), np.float32), "depth": np.zeros((h, w), np.float32),
+               "normals": np.zeros((h, w, 3), np.float32), "material_ids": np.zeros((h, w), np.uint32)}
+        P = C.POINTER
+        f = lambda a: a.ctypes.data_as(P(C.c_float))
+        self.ctx.check(lib().mm3e_render_film(self._ptr, C.byref(camera), aperture_radius, focus_distance,
+                                              f(out["beauty"]), f(out["foreground"]), f(out["alpha"]),
+                                              f(out["depth"]), f(out["normals"]),
+                                              out["material_ids"].ctypes.data_as(P(C.c_uint32))))
+        return out
+
     def march_rays(self, rays6):
         rays6 = np.ascontiguousarray(rays6, dtype=np.float32).reshape(-1, 6)
         n = len(rays6)

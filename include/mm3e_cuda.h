@@ -388,6 +388,15 @@ int mm3e_spec_compile_check(const mm3e_scene_desc* desc, char* err, size_t err_l
  * Replaces render_film's depth / matId AOVs for the pinhole lens (film.rs:89-146). */
 int mm3e_render_hits(mm3e_scene* scene, const mm3e_camera* camera, float* t, uint32_t* mat, uint32_t* steps,
                      float* normal3);
+/* render_film (mm3e-orchestrator/src/film.rs:63-139) with a thin lens (camera.rs Lens): per pixel
+ * the scene-linear beauty (aa^2 samples through the lens; equal to mm3e_render_linear for a
+ * zero aperture), the foreground premultiplied by coverage, the coverage alpha, and the centre
+ * pinhole ray's geometric AOVs: camera-forward depth (+inf on a miss), world normal (zero on a
+ * miss), material id (0xFFFFFFFF on a miss). Host outputs, width*height elements (3 floats for
+ * beauty / foreground / normals); any may be NULL. Lens errors as Lens::validate. Blocking. */
+int mm3e_render_film(mm3e_scene* scene, const mm3e_camera* camera, float aperture_radius, float focus_distance,
+                     float* beauty3, float* foreground3, float* alpha, float* depth, float* normals3,
+                     uint32_t* material_ids);
 /* March `n` rays (origin xyz, unit direction xyz) with the scene's Marcher (march.rs:120-209). */
 int mm3e_march_rays(mm3e_scene* scene, const float* rays6, size_t n, float* t, uint32_t* mat, uint32_t* steps);
 /* World field (accelerated plan) at `n` points: Scene::field (lib.rs:715-717). */

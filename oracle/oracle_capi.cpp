@@ -411,4 +411,36 @@ int oracle_x_crossing(const float* a, const float* b, const float* c, float y, f
                : 0;
 }
 
+
+// film.rs render_film: beauty3 / foreground3 / normals3 (3 floats per pixel), alpha, depth (+inf
+// on a miss), mat_ids (0xFFFFFFFF on a miss); any output may be NULL. Returns 0, or -1 with an
+// invalid lens (Lens::validate).
+int oracle_render_film(const mm3e_scene_desc* d, const mm3e_camera* cam, float aperture_radius, float focus_distance,
+                       unsigned threads, float* beauty3, float* fg3, float* alpha, float* depth, float* normals3,
+                       uint32_t* mat_ids) {
+    if (!std::isfinite(aperture_radius) || aperture_radius < 0.0f) return -1;
+    if (!std::isfinite(focus_distance) || focus_distance <= 0.0f) return -1;
+    Scene<float> s = scene_from_desc<float>(*d);
+    Camera<float> c = cam_from<float>(*cam);
+    bool dual_safe = scene_dual_safe(s);
+    for_row_bands(0, s.height, threads, [&](uint32_t a, uint32_t b, size_t) {
+        World<float> w(s);
+        for (uint32_t y = a; y < b; ++y)
+            for (uint32_t x = 0; x < s.width; ++x) {
+                FilmSample<float> f = film_sample_pixel(s, w, c, aperture_radius, focus_distance, x, y, dual_safe);
+                size_t i = (size_t)y * s.width + x;
+                if (beauty3) std::memcpy(beauty3 + 3 * i, &f.beauty, 12);
+                if (fg3) std::memcpy(fg3 + 3 * i, &f.foreground, 12);
+                if (alpha) alpha[i] = f.alpha;
+                if (depth) depth[i] = f.center.hit ? dot(f.center.pos - c.eye, c.forward) : INFINITY;
+                if (normals3) {
+                    V3<float> nrm = f.center.hit ? f.center.normal : zero3<float>();
+                    std::memcpy(normals3 + 3 * i, &nrm, 12);
+                }
+                if (mat_ids) mat_ids[i] = f.center.hit ? f.center.mat : 0xFFFFFFFFu;
+            }
+    });
+    return 0;
+}
+
 }  // extern "C"

@@ -45,6 +45,8 @@ def lib():
                                            C.c_uint, P(C.c_uint32), P(C.c_float), P(C.c_float), P(C.c_float),
                                            C.c_size_t, C.c_char_p, C.c_size_t]
         l.oracle_x_crossing.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_float, C.c_float, P(C.c_float)]
+        l.oracle_render_film.argtypes = [vp, vp, C.c_float, C.c_float, C.c_uint, P(C.c_float), P(C.c_float),
+                                         P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_uint32)]
         l.oracle_count_frame_blocks.argtypes = [vp, vp, C.c_uint, P(C.c_uint64), C.c_int]
         l.oracle_bake_gi.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint, P(C.c_float),
                                      P(C.c_float), P(C.c_uint32), P(C.c_float)]
@@ -250,3 +252,20 @@ def x_crossing(a, b, c, y, z):
     fa, fb, fc = (np.ascontiguousarray(v, np.float32) for v in (a, b, c))
     ok = lib().oracle_x_crossing(_f(fa), _f(fb), _f(fc), y, z, C.byref(x))
     return x.value if ok else None
+
+
+def render_film(handle, cam, aperture_radius=0.0, focus_distance=1.0, threads=None):
+    """film.rs render_film: dict of beauty (h, w, 3), foreground (h, w, 3), alpha, depth (h, w),
+    normals (h, w, 3), material_ids (h, w)."""
+    d = handle.desc
+    h, w = d.height, d.width
+    out = {"beauty": np.zeros((h, w, 3), np.float32), "foreground": np.zeros((h, w, 3), np.float32),
+           "alpha": np.zeros((h, w), np.float32), "depth": np.zeros((h, w), np.float32),
+           "normals": np.zeros((h, w, 3), np.float32), "material_ids": np.zeros((h, w), np.uint32)}
+    rc = lib().oracle_render_film(C.addressof(d), C.addressof(cam), aperture_radius, focus_distance,
+                                  threads or threads_default(), _f(out["beauty"]), _f(out["foreground"]),
+                                  _f(out["alpha"]), _f(out["depth"]), _f(out["normals"]),
+                                  out["material_ids"].ctypes.data_as(P(C.c_uint32)))
+    if rc != 0:
+        raise ValueError("invalid thin lens")
+    return out

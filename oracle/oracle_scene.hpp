@@ -749,6 +749,105 @@ inline V3<T> shade_hit(const Scene<T>& s, const World<T>& w, const Hit<T>& hit, 
     return apply_fog(radiance, s.fog, hit.t, s.fog_density);
 }
 
+// ------------------------------------------------------------------------------------------
+// film.rs — render_film samples (thin lens, coverage, premultiplied foreground)
+// ------------------------------------------------------------------------------------------
+// film.rs:218-224
+inline uint32_t film_hash(uint32_t v) {
+    v ^= v >> 16;
+    v *= 0x7feb352du;
+    v ^= v >> 15;
+    v *= 0x846ca68bu;
+    return v ^ (v >> 16);
+}
+
+// film.rs:199-215: one jittered sample per aperture grid cell, pixel-dependent shifts.
+template <class T> inline void aperture_sample(uint32_t px, uint32_t py, uint32_t sx, uint32_t sy, uint32_t n, T& u,
+                                               T& v) {
+    if (n == 1) {
+        u = OL(0.5);
+        v = OL(0.5);
+        return;
+    }
+    uint32_t pixel_seed = film_hash(px ^ film_hash(py));
+    uint64_t n64 = n;
+    uint32_t cell_x = (uint32_t)(((uint64_t)sx + sy + pixel_seed) % n64);
+    uint32_t cell_y = (uint32_t)(((uint64_t)sx + 2ull * sy + film_hash(pixel_seed)) % n64);
+    uint32_t seed = film_hash(pixel_seed ^ film_hash(sx) ^ film_hash(sy + 0xa511e9b3u));
+    auto unit = [](uint32_t value) { return T((float)(value >> 8)) * OL(1.0 / 16777216.0); };
+    u = (T((float)cell_x) + unit(seed)) / T((float)n);
+    v = (T((float)cell_y) + unit(film_hash(seed))) / T((float)n);
+}
+
+// camera.rs:92-102: equal-area concentric square-to-disk map.
+template <class T> inline void concentric_disk(T s0, T s1, T& dx, T& dy) {
+    T x = T(2) * s0 - T(1);
+    T y = T(2) * s1 - T(1);
+    if (x == T(0) && y == T(0)) {
+        dx = T(0);
+        dy = T(0);
+        return;
+    }
+    T radius, theta;
+    if (o_abs(x) > o_abs(y)) {
+        radius = x;
+        theta = OL(0.785398163397448309616) * (y / x);
+    } else {
+        radius = y;
+        theta = OL(1.57079632679489661923) - OL(0.785398163397448309616) * (x / y);
+    }
+    dx = radius * o_cos(theta);
+    dy = radius * o_sin(theta);
+}
+
+// camera.rs:71-90: thin-lens ray through a fractional image sample.
+template <class T>
+inline Ray<T> camera_ray_lens(const Camera<T>& c, T ix, T iy, uint32_t w, uint32_t h, T radius, T focus, T a0, T a1) {
+    Ray<T> pinhole = camera_ray(c, ix, iy, w, h);
+    if (radius == T(0)) return pinhole;
+    T dx, dy;
+    concentric_disk(a0, a1, dx, dy);
+    V3<T> origin = c.eye + scale(c.right, dx * radius) + scale(c.up, dy * radius);
+    V3<T> fp = c.eye + scale(pinhole.dir, focus / dot(pinhole.dir, c.forward));
+    return Ray<T>{origin, normalize(fp - origin)};
+}
+
+template <class T> struct FilmSample {
+    V3<T> beauty, foreground;
+    T alpha;
+    Hit<T> center;
+};
+
+// film.rs:147-196 (sample_pixel)
+template <class T>
+inline FilmSample<T> film_sample_pixel(const Scene<T>& s, const World<T>& w, const Camera<T>& cam, T radius, T focus,
+                                       uint32_t x, uint32_t y, bool dual_safe) {
+    Ray<T> center_ray = camera_ray(cam, T((float)x) + OL(0.5), T((float)y) + OL(0.5), s.width, s.height);
+    Hit<T> center = march_scene(s, w, dual_safe, center_ray, 0);
+    uint32_t n = s.aa > 1 ? s.aa : 1;
+    T inv_samples = T(1) / T((float)((uint64_t)n * n));
+    V3<T> beauty = zero3<T>(), fg = zero3<T>();
+    uint64_t hits = 0;
+    for (uint32_t sy = 0; sy < n; ++sy)
+        for (uint32_t sx = 0; sx < n; ++sx) {
+            T ix = T((float)x) + (T((float)sx) + OL(0.5)) / T((float)n);
+            T iy = T((float)y) + (T((float)sy) + OL(0.5)) / T((float)n);
+            T a0, a1;
+            aperture_sample(x, y, sx, sy, n, a0, a1);
+            Ray<T> ray = n == 1 ? center_ray : camera_ray_lens(cam, ix, iy, s.width, s.height, radius, focus, a0, a1);
+            Hit<T> hit = n == 1 ? center : march_scene(s, w, dual_safe, ray, 0);
+            if (hit.hit) {
+                V3<T> rad = shade_hit(s, w, hit, ray, 0, dual_safe);
+                beauty = beauty + rad;
+                fg = fg + rad;
+                hits += 1;
+            } else {
+                beauty = beauty + sky(ray.dir, s.sun_dir);
+            }
+        }
+    return FilmSample<T>{scale(beauty, inv_samples), scale(fg, inv_samples), T((float)hits) * inv_samples, center};
+}
+
 // lib.rs:1265-1282
 template <class T> V3<T> trace(const Scene<T>& s, const World<T>& w, const Ray<T>& ray, uint32_t depth, bool dual_safe) {
     if (depth == 0) Hooks<T>::primary_ray();
