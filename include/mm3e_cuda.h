@@ -276,6 +276,21 @@ int mm3e_scene_validate(const mm3e_scene_desc* desc, char* err, size_t err_len);
 /* Size in bytes of the lowered scene tape (host-side lowering, no device). */
 int mm3e_scene_tape_bytes(const mm3e_scene_desc* desc, size_t* out_bytes);
 
+/* ---- `.mm3e` text scenes (mm3e-orchestrator/src/scene_io.rs) -------------------------------- */
+/* Parses a `.mm3e` document (scene_io::parse, scene_io.rs:196-281) into an owned scene
+ * description and camera: same directives, defaults (Scene::new(640, 360), materials from the
+ * file or one default) and validation, errors as "line N: ..." in `err`. Host only. */
+typedef struct mm3e_parsed_scene mm3e_parsed_scene;
+int mm3e_scene_parse_mm3e(const char* text, mm3e_parsed_scene** out, char* err, size_t err_len);
+const mm3e_scene_desc* mm3e_parsed_scene_desc(const mm3e_parsed_scene* parsed);
+int mm3e_parsed_scene_camera(const mm3e_parsed_scene* parsed, mm3e_camera* out);
+void mm3e_parsed_scene_free(mm3e_parsed_scene* parsed);
+/* scene_io::try_serialize (scene_io.rs:38-95): the `.mm3e` text of a scene + camera (numbers as
+ * the shortest round-trip decimal). CSG / surface objects give MM3E_ERR_UNSUPPORTED with the
+ * reference's message; volume objects become a comment. `out` may be NULL to query `len`. */
+int mm3e_scene_write_mm3e(const mm3e_scene_desc* desc, const mm3e_camera* camera, char* out, size_t cap, size_t* len,
+                          char* err, size_t err_len);
+
 /* ---- context ----------------------------------------------------------------------------- */
 int mm3e_ctx_create(int device, mm3e_ctx** out);
 /* Destroys the context and every scene still compiled on it (their handles become invalid). */

@@ -1,0 +1,72 @@
+"""`.mm3e` text scenes, against the reference's own scene_io tests
+(mm3e-orchestrator/tests/engine.rs:33-82) and its writer / parser rules (scene_io.rs)."""
+import numpy as np
+import pytest
+
+import oracle_py
+from mm3e_cuda import abi, scene_io, scenes
+from mm3e_cuda.scene import Expr, Object, Prim, Transform
+
+
+def test_roundtrip_is_stable_and_keeps_the_mode():
+    scene, cam = scenes.demo_scene()
+    scene.mode = abi.MODE_STEPS
+    text = scene_io.serialize(scene, cam)
+    parsed, _ = scene_io.parse(text)
+    assert len(parsed.objects) == len(scene.objects)
+    assert len(parsed.materials) == len(scene.materials)
+    assert len(parsed.lights) == len(scene.lights)
+    assert parsed.mode == abi.MODE_STEPS
+    assert scene_io.serialize(parsed, cam) == text
+
+
+def test_camera_roundtrips():
+    scene, cam = scenes.demo_scene()
+    _, c2 = scene_io.parse(scene_io.serialize(scene, cam))
+    for k in ("eye", "forward", "up"):
+        assert np.linalg.norm(np.array(getattr(c2, k)) - np.array(getattr(cam, k))) < 1e-4
+    assert abs(c2.fov_scale - cam.fov_scale) < 1e-4
+
+
+def test_parsed_scene_renders_like_the_original():
+    scene, cam = scenes.demo_scene()
+    parsed, cam2 = scene_io.parse(scene_io.serialize(scene, cam))
+    a = oracle_py.render(scene.desc(), cam, threads=4)
+    b = oracle_py.render(parsed.desc(), cam, threads=4)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("text", [
+    "size 10\n", "obj banana 1 2 3\n", "wat 1 2 3\n", "size 0 100\n", "size 100000 100\n", "sun 0 0 0\n",
+    "ambient NaN 0 0\n", "cam 1 2 3 1 2 3 0 1 0 50\n", "cam 0 0 0 0 1 0 0 1 0 50\n", "cam 0 0 5 0 0 0 0 1 0 180\n",
+    "marcher 0 120 0.0006 1\n", "marcher 160 120 -1 1\n",
+    "obj sphere -1 pos 0 0 0 basis 1 0 0 0 1 0 0 0 1 scale 1 mat 0 combine union\n",
+    "obj plane 0 0 0 0 pos 0 0 0 basis 1 0 0 0 1 0 0 0 1 scale 1 mat 0 combine union\n",
+    "obj sphere 1 pos 0 0 0 basis 1 0 0 0 1 0 0 0 1 scale 0 mat 0 combine union\n",
+    "obj sphere 1 pos 0 0 0 basis 1 0 0 0 1 0 0 0 1 scale 1 mat 5 combine union\n",
+])
+def test_rejects_garbage(text):
+    with pytest.raises(scene_io.SceneFormatError):
+        scene_io.parse(text)
+
+
+def test_messages_name_the_line():
+    with pytest.raises(scene_io.SceneFormatError, match="line 2: unknown directive 'wat'"):
+        scene_io.parse("# comment\nwat 1\n")
+    with pytest.raises(scene_io.SceneFormatError, match="object 1: material index 5 out of range"):
+        scene_io.parse("obj sphere 1 mat 5\n")
+
+
+def test_csg_objects_are_not_representable():
+    scene, cam = scenes.demo_scene()
+    eid = scene.csg(Expr.union(Expr(abi.PRIM_SPHERE, (0.5,)), Expr(abi.PRIM_BOX, (0.3, 0.3, 0.3))))
+    scene.add(Object(Prim.csg(eid), Transform.IDENTITY, 0))
+    with pytest.raises(scene_io.SceneFormatError, match="CSG"):
+        scene_io.serialize(scene, cam)
+
+
+def test_defaults_and_comments():
+    s, cam = scene_io.parse("# only a size\nsize 32 24  # trailing comment\n")
+    assert (s.width, s.height) == (32, 24) and s.aa == 2 and s.bounces == 1
+    assert len(s.materials) == 1
+    assert abs(cam.fov_scale - np.tan(0.5)) < 1e-6
