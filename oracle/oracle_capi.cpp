@@ -443,4 +443,150 @@ int oracle_render_film(const mm3e_scene_desc* d, const mm3e_camera* cam, float a
     return 0;
 }
 
+
+namespace {
+// render_gbuffer's per-pixel display value (lib.rs:1016-1018)
+inline void display_u8(V3<float> hdr, float exposure, uint8_t* px) {
+    V3<float> d = clamp01(gamma(aces(scale(hdr, exposure))));
+    px[0] = (uint8_t)(d.x * 255.0f + 0.5f);
+    px[1] = (uint8_t)(d.y * 255.0f + 0.5f);
+    px[2] = (uint8_t)(d.z * 255.0f + 0.5f);
+    px[3] = 255;
+}
+
+// reproject.rs:55-70
+inline bool project(const Camera<float>& c, V3<float> world, uint32_t w, uint32_t h, float& sx, float& sy, float& fz) {
+    V3<float> v = world - c.eye;
+    fz = dot(v, c.forward);
+    if (fz <= 1e-4f) return false;
+    float aspect = (float)w / (float)h;
+    float ndc_x = dot(v, c.right) / fz;
+    float ndc_y = dot(v, c.up) / fz;
+    sx = (ndc_x / (aspect * c.fov_scale) + 1.0f) * 0.5f * (float)w;
+    sy = (1.0f - ndc_y / c.fov_scale) * 0.5f * (float)h;
+    return true;
+}
+}  // namespace
+
+// render_gbuffer (lib.rs:951-1039): display RGBA8, primary hit distance (+inf: sky), mover
+// index (-1: none) per pixel; movers4 = (centre xyz, radius) per mover.
+int oracle_render_gbuffer(const mm3e_scene_desc* d, const mm3e_camera* cam, const float* movers4, uint32_t n_movers,
+                          unsigned threads, uint8_t* color4, float* depth, int32_t* obj) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    Camera<float> c = cam_from<float>(*cam);
+    bool dual_safe = scene_dual_safe(s);
+    for_row_bands(0, s.height, threads, [&](uint32_t a, uint32_t b, size_t) {
+        World<float> w(s);
+        for (uint32_t y = a; y < b; ++y)
+            for (uint32_t x = 0; x < s.width; ++x) {
+                size_t i = (size_t)y * s.width + x;
+                Ray<float> ray = camera_ray(c, (float)x + 0.5f, (float)y + 0.5f, s.width, s.height);
+                Hit<float> hit = march_scene(s, w, dual_safe, ray, 0);
+                V3<float> hdr;
+                if (hit.hit) {
+                    int32_t o = -1;
+                    for (uint32_t k = 0; k < n_movers; ++k) {
+                        V3<float> ctr{movers4[4 * k], movers4[4 * k + 1], movers4[4 * k + 2]};
+                        if (length(hit.pos - ctr) <= movers4[4 * k + 3] + 0.05f) {
+                            o = (int32_t)k;
+                            break;
+                        }
+                    }
+                    hdr = shade_hit(s, w, hit, ray, 0, dual_safe);
+                    depth[i] = hit.t;
+                    obj[i] = o;
+                } else {
+                    hdr = sky(ray.dir, s.sun_dir);
+                    depth[i] = INFINITY;
+                    obj[i] = -1;
+                }
+                display_u8(hdr, s.post.exposure, color4 + 4 * i);
+            }
+    });
+    return 0;
+}
+
+// reproject::warp (reproject.rs:77-113): out color4 and filled (0/1) per pixel of the new view.
+int oracle_reproject_warp(uint32_t w, uint32_t h, const mm3e_camera* prev_cam, const uint8_t* color4,
+                          const float* depth, const int32_t* obj, const mm3e_camera* new_cam, const float* deltas3,
+                          uint32_t n_deltas, uint8_t* out4, uint8_t* filled) {
+    Camera<float> pc = cam_from<float>(*prev_cam), nc = cam_from<float>(*new_cam);
+    size_t n = (size_t)w * h;
+    std::vector<float> zbuf(n, INFINITY);
+    std::memset(out4, 0, 4 * n);
+    std::memset(filled, 0, n);
+    for (uint32_t y = 0; y < h; ++y)
+        for (uint32_t x = 0; x < w; ++x) {
+            size_t i = (size_t)y * w + x;
+            V3<float> dir = camera_ray(pc, (float)x + 0.5f, (float)y + 0.5f, w, h).dir;
+            float dd = std::isfinite(depth[i]) ? depth[i] : 1.0e6f;
+            V3<float> world = pc.eye + scale(dir, dd);
+            if (obj[i] >= 0 && (uint32_t)obj[i] < n_deltas)
+                world = world + V3<float>{deltas3[3 * obj[i]], deltas3[3 * obj[i] + 1], deltas3[3 * obj[i] + 2]};
+            float sx, sy, fz;
+            if (!project(nc, world, w, h, sx, sy, fz)) continue;
+            int32_t nx = (int32_t)std::floor(sx), ny = (int32_t)std::floor(sy);
+            if (nx >= 0 && ny >= 0 && (uint32_t)nx < w && (uint32_t)ny < h) {
+                size_t j = (size_t)ny * w + nx;
+                if (fz < zbuf[j]) {
+                    zbuf[j] = fz;
+                    std::memcpy(out4 + 4 * j, color4 + 4 * i, 4);
+                    filled[j] = 1;
+                }
+            }
+        }
+    return 0;
+}
+
+// reproject::reproject's row hole fill (reproject.rs:118-146), in place.
+int oracle_reproject_fill(uint32_t w, uint32_t h, uint8_t* out4, uint8_t* filled) {
+    for (uint32_t y = 0; y < h; ++y) {
+        bool have = false;
+        uint8_t last[4];
+        for (uint32_t x = 0; x < w; ++x) {
+            size_t i = (size_t)y * w + x;
+            if (filled[i]) {
+                std::memcpy(last, out4 + 4 * i, 4);
+                have = true;
+            } else if (have) {
+                std::memcpy(out4 + 4 * i, last, 4);
+                filled[i] = 1;
+            }
+        }
+        have = false;
+        for (uint32_t x = w; x-- > 0;) {
+            size_t i = (size_t)y * w + x;
+            if (filled[i]) {
+                std::memcpy(last, out4 + 4 * i, 4);
+                have = true;
+            } else if (have) {
+                std::memcpy(out4 + 4 * i, last, 4);
+            }
+        }
+    }
+    return 0;
+}
+
+// reproject_hybrid's hole rerender (lib.rs:1047-1080): every unfilled pixel is marched and
+// shaded at the new camera, in place.
+int oracle_rerender_holes(const mm3e_scene_desc* d, const mm3e_camera* new_cam, unsigned threads, uint8_t* out4,
+                          const uint8_t* filled) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    Camera<float> c = cam_from<float>(*new_cam);
+    bool dual_safe = scene_dual_safe(s);
+    for_row_bands(0, s.height, threads, [&](uint32_t a, uint32_t b, size_t) {
+        World<float> w(s);
+        for (uint32_t y = a; y < b; ++y)
+            for (uint32_t x = 0; x < s.width; ++x) {
+                size_t i = (size_t)y * s.width + x;
+                if (filled[i]) continue;
+                Ray<float> ray = camera_ray(c, (float)x + 0.5f, (float)y + 0.5f, s.width, s.height);
+                Hit<float> hit = march_scene(s, w, dual_safe, ray, 0);
+                V3<float> hdr = hit.hit ? shade_hit(s, w, hit, ray, 0, dual_safe) : sky(ray.dir, s.sun_dir);
+                display_u8(hdr, s.post.exposure, out4 + 4 * i);
+            }
+    });
+    return 0;
+}
+
 }  // extern "C"

@@ -47,6 +47,13 @@ def lib():
         l.oracle_x_crossing.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_float, C.c_float, P(C.c_float)]
         l.oracle_render_film.argtypes = [vp, vp, C.c_float, C.c_float, C.c_uint, P(C.c_float), P(C.c_float),
                                          P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_uint32)]
+        u8p = P(C.c_uint8)
+        l.oracle_render_gbuffer.argtypes = [vp, vp, P(C.c_float), C.c_uint32, C.c_uint, u8p, P(C.c_float),
+                                            P(C.c_int32)]
+        l.oracle_reproject_warp.argtypes = [C.c_uint32, C.c_uint32, vp, u8p, P(C.c_float), P(C.c_int32), vp,
+                                            P(C.c_float), C.c_uint32, u8p, u8p]
+        l.oracle_reproject_fill.argtypes = [C.c_uint32, C.c_uint32, u8p, u8p]
+        l.oracle_rerender_holes.argtypes = [vp, vp, C.c_uint, u8p, u8p]
         l.oracle_count_frame_blocks.argtypes = [vp, vp, C.c_uint, P(C.c_uint64), C.c_int]
         l.oracle_bake_gi.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint, P(C.c_float),
                                      P(C.c_float), P(C.c_uint32), P(C.c_float)]
@@ -268,4 +275,39 @@ def render_film(handle, cam, aperture_radius=0.0, focus_distance=1.0, threads=No
                                   out["material_ids"].ctypes.data_as(P(C.c_uint32)))
     if rc != 0:
         raise ValueError("invalid thin lens")
+    return out
+
+
+def _u8(a):
+    return a.ctypes.data_as(P(C.c_uint8))
+
+
+def render_gbuffer(handle, cam, movers=(), threads=None):
+    """render_gbuffer: {"color": (h, w, 4) u8, "depth": (h, w) f32, "obj": (h, w) i32}."""
+    d = handle.desc
+    h, w = d.height, d.width
+    mv = np.ascontiguousarray(np.asarray(movers, np.float32).reshape(-1, 4))
+    out = {"color": np.zeros((h, w, 4), np.uint8), "depth": np.zeros((h, w), np.float32),
+           "obj": np.zeros((h, w), np.int32)}
+    lib().oracle_render_gbuffer(C.addressof(d), C.addressof(cam), _f(mv), len(mv), threads or threads_default(),
+                                _u8(out["color"]), _f(out["depth"]), out["obj"].ctypes.data_as(P(C.c_int32)))
+    return out
+
+
+def reproject(g, prev_cam, new_cam, deltas=(), hybrid_handle=None, threads=None):
+    """reproject::reproject (cheap row fill) or, with hybrid_handle (the scene), reproject_hybrid:
+    (h, w, 4) u8."""
+    h, w = g["depth"].shape
+    dl = np.ascontiguousarray(np.asarray(deltas, np.float32).reshape(-1, 3))
+    out = np.zeros((h, w, 4), np.uint8)
+    filled = np.zeros((h, w), np.uint8)
+    color = np.ascontiguousarray(g["color"])
+    lib().oracle_reproject_warp(w, h, C.addressof(prev_cam), _u8(color), _f(np.ascontiguousarray(g["depth"])),
+                                np.ascontiguousarray(g["obj"]).ctypes.data_as(P(C.c_int32)), C.addressof(new_cam),
+                                _f(dl), len(dl), _u8(out), _u8(filled))
+    if hybrid_handle is None:
+        lib().oracle_reproject_fill(w, h, _u8(out), _u8(filled))
+    else:
+        lib().oracle_rerender_holes(C.addressof(hybrid_handle.desc), C.addressof(new_cam), threads or threads_default(),
+                                    _u8(out), _u8(filled))
     return out
