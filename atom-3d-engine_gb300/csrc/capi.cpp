@@ -1067,6 +1067,99 @@ int mm3e_render_film(mm3e_scene* s, const mm3e_camera* camera, float aperture_ra
     return MM3E_OK;
 }
 
+// render_gbuffer: an aa-1 beauty frame without post, packed with its primary hits.
+int mm3e_render_gbuffer(mm3e_scene* s, const mm3e_camera* camera, const float* movers4, uint32_t n_movers,
+                        uint8_t* color4, float* depth, int32_t* obj) {
+    if (!s || !camera || (n_movers && !movers4)) return MM3E_ERR_INVALID;
+    mm3e_ctx* c = s->ctx;
+    size_t n = (size_t)s->low.width * s->low.height;
+    if (n == 0) return MM3E_OK;
+    cudaSetDevice(c->device);
+    int rc = ensure_frame_buffers(s, false);
+    if (rc) return rc;
+    CK(c->preview.ensure(n, n_movers, 0));
+    PreviewBuffers& pv = c->preview;
+    LaunchLog log = c->prof.log();
+    PassPlan p = scene_plan(s, s->d_tape, (uint32_t)s->low.blob.size(), *camera, MM3E_FB_RGBA_F32, nullptr);
+    p.job0.aa = 1;  // one pixel-centre sample (lib.rs:978)
+    p.job0.spp = 1;
+    p.job0.n_samples = p.job0.n_slots;
+    p.n_samples = p.job0.n_samples;
+    p.spec = s->spec_kernels();
+    p.post = false;
+    if (n_movers)
+        CK(cudaMemcpyAsync(pv.mover, movers4, n_movers * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, &log));
+    WaveArgs a{};
+    a.job0 = p.job0;
+    a.tile_wlog = s->buf_wlog;
+    a.grid_cap = (uint32_t)c->sm_count * 16u;
+    a.b.q_o = s->buf.qa_o;
+    a.b.q_d = s->buf.qa_d;
+    a.b.h_n = s->buf.h_n;
+    a.b.h_m = s->buf.h_m;
+    a.b.hdr = s->buf.hdr;
+    CK(launch_gbuffer_pack(a, p.n_slots, pv.mover, n_movers, pv.color, pv.depth, pv.obj, c->stream, &log));
+    if (color4) CK(cudaMemcpyAsync(color4, pv.color, n * sizeof(uchar4), cudaMemcpyDeviceToHost, c->stream));
+    if (depth) CK(cudaMemcpyAsync(depth, pv.depth, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (obj) CK(cudaMemcpyAsync(obj, pv.obj, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    return check_status(s);
+}
+
+// reproject / reproject_hybrid: forward warp, then the row fill or the hole re-render.
+int mm3e_reproject(mm3e_ctx* c, uint32_t w, uint32_t h, const mm3e_camera* prev_camera, const uint8_t* color4,
+                   const float* depth, const int32_t* obj, const mm3e_camera* new_camera, const float* deltas3,
+                   uint32_t n_deltas, mm3e_scene* hybrid, uint8_t* out4) {
+    if (!c || !prev_camera || !new_camera) return MM3E_ERR_INVALID;
+    size_t n = (size_t)w * h;
+    if (n == 0) return MM3E_OK;
+    if (!color4 || !depth || !obj || !out4 || (n_deltas && !deltas3)) return MM3E_ERR_INVALID;
+    if (n > 0xFFFFFFFFull) return fail(c, MM3E_ERR_INVALID, "reprojected frame too large");
+    if (hybrid && hybrid->ctx != c) return fail(c, MM3E_ERR_INVALID, "hybrid scene belongs to another context");
+    cudaSetDevice(c->device);
+    CK(c->preview.ensure(n, 0, n_deltas));
+    PreviewBuffers& pv = c->preview;
+    LaunchLog log = c->prof.log();
+    CameraArgs prev{}, next{};
+    fill_camera(prev, *prev_camera);
+    fill_camera(next, *new_camera);
+    CK(cudaMemcpyAsync(pv.color, color4, n * sizeof(uchar4), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(pv.depth, depth, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(pv.obj, obj, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    if (n_deltas) CK(cudaMemcpyAsync(pv.delta, deltas3, 3 * n_deltas * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CK(launch_warp(prev, next, w, h, pv.depth, pv.obj, pv.delta, n_deltas, pv.keys, pv.color, pv.out, pv.filled,
+                   c->stream, &log));
+    if (!hybrid) {
+        CK(launch_row_fill(w, h, pv.out, pv.filled, c->stream, &log));
+        CK(cudaMemcpyAsync(out4, pv.out, n * sizeof(uchar4), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return MM3E_OK;
+    }
+    mm3e_scene* s = hybrid;
+    int rc = ensure_frame_buffers(s, false);
+    if (rc) return rc;
+    if (s->buf.cap < n) CK(s->buf.ensure(n, s->n_lights(), s->low.bounces + 1, s->buf.pixels));
+    CK(cudaMemsetAsync(pv.count, 0, sizeof(uint32_t), c->stream));
+    CK(launch_hole_rays(next, w, h, pv.filled, s->buf.qa_o, s->buf.qa_d, pv.hole_pix, pv.count,
+                        (uint32_t)c->sm_count * 16u, c->stream, &log));
+    PassPlan p = scene_plan(s, s->d_tape, (uint32_t)s->low.blob.size(), *new_camera, MM3E_FB_RGBA_F32, nullptr);
+    p.queue0 = pv.count;
+    p.n_samples = (uint32_t)n;  // capacity: every pixel a hole
+    p.spec = s->spec_kernels();
+    p.post = false;
+    CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, &log));
+    WaveArgs a{};
+    a.job0 = p.job0;
+    a.cap = (uint32_t)s->buf.cap;
+    a.n_items = (uint32_t)n;
+    a.grid_cap = (uint32_t)c->sm_count * 16u;
+    a.b.lvl = s->buf.lvl;
+    a.b.term = s->buf.term;
+    CK(launch_hole_resolve(a, pv.count, pv.hole_pix, pv.out, c->stream, &log));
+    CK(cudaMemcpyAsync(out4, pv.out, n * sizeof(uchar4), cudaMemcpyDeviceToHost, c->stream));
+    return check_status(s);
+}
+
 // Allocation-free ray queries: the scratch lives in noalloc.cu's fixed __device__ array.
 int mm3e_march_rays_noalloc(mm3e_scene* s, const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat,
                             uint32_t* d_steps) {

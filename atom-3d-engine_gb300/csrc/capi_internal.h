@@ -30,6 +30,7 @@ struct mm3e_ctx {
     double kk_ms[mm3e::KK_COUNT] = {};
     uint32_t kk_launches[mm3e::KK_COUNT] = {};
     std::unique_ptr<mm3e::BatchEngine> batch;
+    mm3e::PreviewBuffers preview;       // render_gbuffer / reproject scratch
     ~mm3e_ctx();
 };
 

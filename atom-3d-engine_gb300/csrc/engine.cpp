@@ -72,6 +72,40 @@ cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need
     return cudaSuccess;
 }
 
+void PreviewBuffers::release() {
+    void* ps[] = {color, out, depth, obj, keys, filled, hole_pix, count, mover, delta};
+    for (void* p : ps) cudaFree(p);
+    *this = PreviewBuffers();
+}
+
+size_t PreviewBuffers::bytes() const {
+    return pixels * (2 * sizeof(uchar4) + sizeof(float) + sizeof(int32_t) + sizeof(unsigned long long) + 1 +
+                     sizeof(uint32_t)) +
+           movers * sizeof(float4) + deltas * 3 * sizeof(float) + sizeof(uint32_t);
+}
+
+cudaError_t PreviewBuffers::ensure(size_t need_pixels, size_t need_movers, size_t need_deltas) {
+    if (count && need_pixels <= pixels && need_movers <= movers && need_deltas <= deltas) return cudaSuccess;
+    size_t n = need_pixels > pixels ? need_pixels : pixels;
+    size_t m = need_movers > movers ? need_movers : movers;
+    size_t d = need_deltas > deltas ? need_deltas : deltas;
+    n = n ? n : 1;
+    m = m > 8 ? m : 8;
+    d = d > 8 ? d : 8;
+    release();
+    cudaError_t e;
+    if ((e = grow(&color, n)) || (e = grow(&out, n)) || (e = grow(&depth, n)) || (e = grow(&obj, n)) ||
+        (e = grow(&keys, n)) || (e = grow(&filled, n)) || (e = grow(&hole_pix, n)) || (e = grow(&count, 1)) ||
+        (e = grow(&mover, m)) || (e = grow(&delta, 3 * d))) {
+        release();
+        return e;
+    }
+    pixels = n;
+    movers = m;
+    deltas = d;
+    return cudaSuccess;
+}
+
 // ---------------------------------------------------------------------------------------
 Profiler::~Profiler() {
     for (cudaEvent_t e : pool_) cudaEventDestroy(e);
@@ -171,14 +205,19 @@ WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tun
 }  // namespace
 
 namespace {
+const uint32_t* primary_count(const PassPlan& plan) {
+    if (plan.queue0) return plan.queue0;
+    return plan.jobs ? &plan.totals->n_samples : nullptr;
+}
+
 // The passes of one level: march, AO, shadows, (reflection rays of the next level), shading.
 cudaError_t level_passes(const PassPlan& plan, WaveArgs& a, PassBuffers& buf, const TuneParams& tune, cudaStream_t s,
                          int sm_count, LaunchLog* log, uint32_t level, bool reflect_next) {
     cudaError_t e;
     a.level = level;
-    a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
+    a.src = level == 0 && !plan.queue0 ? SRC_SAMPLES : SRC_QUEUE;
     a.n_items = plan.n_samples;
-    a.n_items_dev = level == 0 ? (plan.jobs ? &plan.totals->n_samples : nullptr) : buf.counters + 4 * (level - 1) + 2;
+    a.n_items_dev = level == 0 ? primary_count(plan) : buf.counters + 4 * (level - 1) + 2;
     a.b.nq_count = buf.counters + 4 * level + 2;
     a.counter = buf.counters + 4 * level;
     if ((e = launch_march(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
@@ -207,9 +246,9 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
         a0.b.nq_o = buf.qb_o;
         a0.b.nq_d = buf.qb_d;
         a0.level = 0;
-        a0.src = SRC_SAMPLES;
+        a0.src = plan.queue0 ? SRC_QUEUE : SRC_SAMPLES;
         a0.n_items = plan.n_samples;
-        a0.n_items_dev = plan.jobs ? &plan.totals->n_samples : nullptr;
+        a0.n_items_dev = primary_count(plan);
         a0.b.nq_count = buf.counters + 2;
         a0.counter = buf.counters;
         if ((e = launch_march(a0, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
@@ -241,6 +280,7 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
         if ((e = launch_shade(a0, s, log)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(s, buf.ev_join, 0)) != cudaSuccess) return e;
     }
+    if (plan.queue0) return cudaSuccess;
     if ((e = launch_resolve(a, plan.n_slots, s, log)) != cudaSuccess) return e;
     if (!plan.post) return cudaSuccess;
     return run_post(plan, buf, s, sm_count, log);

@@ -53,6 +53,24 @@ struct PassBuffers {
     static size_t bytes_for(size_t cap, size_t lights, size_t levels, size_t pixels);
 };
 
+// Device scratch of the G-buffer and reprojection calls: one frame of colour / depth / object
+// tags, the warp's z-buffer keys, the filled mask, the hole list and the mover tables.
+struct PreviewBuffers {
+    size_t pixels = 0, movers = 0, deltas = 0;
+    uchar4 *color = nullptr, *out = nullptr;
+    float* depth = nullptr;
+    int32_t* obj = nullptr;
+    unsigned long long* keys = nullptr;
+    unsigned char* filled = nullptr;
+    uint32_t *hole_pix = nullptr, *count = nullptr;
+    float4* mover = nullptr;  // centre xyz, radius
+    float* delta = nullptr;   // xyz per mover
+    ~PreviewBuffers() { release(); }
+    void release();
+    cudaError_t ensure(size_t pixels, size_t movers, size_t deltas);
+    size_t bytes() const;
+};
+
 // Per-kernel-kind device time, from CUDA events around each pass (off by default).
 class Profiler {
   public:
@@ -92,10 +110,14 @@ struct PassPlan {
     bool clear_status = true;       // also clear the status word with the work counters
     const SpecKernels* spec = nullptr;  // scene-specialised march / shadow / AO (single job only)
     bool film = false;              // resolve coverage + foreground (into buf.bright) too
+    // Primary rays from queue a (count in this device word, outside buf.counters) instead of
+    // the jobs' camera samples; sample k of the queue is queue entry k. The caller resolves.
+    const uint32_t* queue0 = nullptr;
 };
 
 // Enqueues the passes on `s`: counters cleared, march / AO / shadow / shade per level,
-// resolve into buf.hdr, then post into each job's `out` when plan.post. Asynchronous.
+// resolve into buf.hdr, then post into each job's `out` when plan.post (neither with
+// plan.queue0). Asynchronous.
 cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams& tune, cudaStream_t s, int sm_count,
                        LaunchLog* log);
 

@@ -131,6 +131,22 @@ struct LaunchLog {
     void (*end)(void* recorder, uint32_t kind, cudaStream_t s) = nullptr;
 };
 
+// Launch-log bracket of one pass: counts its `n` launches and brackets it for the recorder.
+struct LogScope {
+    LaunchLog* l;
+    uint32_t kind;
+    cudaStream_t s;
+    LogScope(LaunchLog* log, uint32_t k, cudaStream_t st, uint32_t n) : l(log), kind(k), s(st) {
+        if (l) {
+            l->launches += n;
+            if (l->begin) l->begin(l->recorder, kind, s);
+        }
+    }
+    ~LogScope() {
+        if (l && l->end) l->end(l->recorder, kind, s);
+    }
+};
+
 // Kernels of a scene-specialised program (NVRTC, see spec.h): the march / shadow / AO passes
 // with the scene's field compiled in; same parameters as the library's kernels.
 struct SpecKernels {
@@ -178,6 +194,24 @@ cudaError_t launch_field(const unsigned char* tape, const float* pts, uint32_t n
                          cudaStream_t s, LaunchLog* log);
 cudaError_t launch_gi_reduce(const float4* radiance, const float4* dirs, uint32_t dirs_per_face, uint32_t probes,
                              float4* cubes, cudaStream_t s, LaunchLog* log);
+
+// G-buffer and reprojection passes (reproject.cu).
+// G-buffer pixels of an aa-1 frame from its primary-level records and resolved HDR.
+cudaError_t launch_gbuffer_pack(const WaveArgs& a, uint32_t n_slots, const float4* movers, uint32_t n_movers,
+                                uchar4* color, float* depth, int32_t* obj, cudaStream_t s, LaunchLog* log);
+// Forward warp: per target pixel the nearest source (keys: scratch of w*h 64-bit words).
+cudaError_t launch_warp(const CameraArgs& prev, const CameraArgs& next, uint32_t w, uint32_t h, const float* depth,
+                        const int32_t* obj, const float* deltas3, uint32_t n_deltas, unsigned long long* keys,
+                        const uchar4* src, uchar4* out, unsigned char* filled, cudaStream_t s, LaunchLog* log);
+cudaError_t launch_row_fill(uint32_t w, uint32_t h, uchar4* out, unsigned char* filled, cudaStream_t s,
+                            LaunchLog* log);
+// Holes of `filled` as a primary ray queue (q_o / q_d, *count, hole_pix); *count must start at 0.
+cudaError_t launch_hole_rays(const CameraArgs& cam, uint32_t w, uint32_t h, const unsigned char* filled, float4* q_o,
+                             float4* q_d, uint32_t* hole_pix, uint32_t* count, uint32_t grid_cap, cudaStream_t s,
+                             LaunchLog* log);
+// Display pixel of every shaded hole (its levels folded), written at hole_pix.
+cudaError_t launch_hole_resolve(const WaveArgs& a, const uint32_t* count, const uint32_t* hole_pix, uchar4* out,
+                                cudaStream_t s, LaunchLog* log);
 
 #endif  // __CUDACC_RTC__
 

@@ -389,22 +389,6 @@ __global__ void k_gi_reduce(const float4* __restrict__ rad, const float4* __rest
     cubes[idx] = make_float4(c.x, c.y, c.z, 0.0f);
 }
 
-// Launch-log bracket of one pass.
-struct LogScope {
-    LaunchLog* l;
-    uint32_t kind;
-    cudaStream_t s;
-    LogScope(LaunchLog* log, uint32_t k, cudaStream_t st, uint32_t n) : l(log), kind(k), s(st) {
-        if (l) {
-            l->launches += n;
-            if (l->begin) l->begin(l->recorder, kind, s);
-        }
-    }
-    ~LogScope() {
-        if (l && l->end) l->end(l->recorder, kind, s);
-    }
-};
-
 typedef void (*WaveKernel)(const WaveArgs);
 
 // Instantiations of a persistent kernel over (tape mode, block, unroll).

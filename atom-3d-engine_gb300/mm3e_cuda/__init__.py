@@ -123,6 +123,27 @@ class Context:
         return {"block": best.block, "tile_wlog": best.tile_wlog, "unroll": best.unroll,
                 "min_blocks": best.min_blocks}, table
 
+    # ---- reprojection -------------------------------------------------------------------------------
+    def reproject(self, gframe, new_camera, mover_deltas=(), hybrid_scene=None):
+        """reproject::reproject (reproject.rs:118), or reproject_hybrid (lib.rs:1040) with
+        `hybrid_scene` (a CompiledScene): the G-buffer frame `gframe` (render_gbuffer's dict)
+        warped into `new_camera`; (h, w, 4) u8."""
+        h, w = gframe["depth"].shape
+        color = np.ascontiguousarray(gframe["color"], np.uint8)
+        depth = np.ascontiguousarray(gframe["depth"], np.float32)
+        obj = np.ascontiguousarray(gframe["obj"], np.int32)
+        if color.shape != (h, w, 4) or obj.shape != (h, w):
+            raise ValueError("G-buffer frame arrays disagree in shape")
+        dl = np.ascontiguousarray(np.asarray(mover_deltas, np.float32).reshape(-1, 3))
+        out = np.zeros((h, w, 4), np.uint8)
+        P = C.POINTER
+        self.check(lib().mm3e_reproject(self._ptr, w, h, C.byref(gframe["camera"]), color.ctypes.data_as(P(C.c_uint8)),
+                                        depth.ctypes.data_as(P(C.c_float)), obj.ctypes.data_as(P(C.c_int32)),
+                                        C.byref(new_camera), dl.ctypes.data_as(P(C.c_float)), len(dl),
+                                        hybrid_scene._ptr if hybrid_scene is not None else None,
+                                        out.ctypes.data_as(P(C.c_uint8))))
+        return out
+
     # ---- mesh -> SDF bake -------------------------------------------------------------------------
     def bake_mesh_sdf(self, positions, triangles, resolution, padding, device_out=None):
         """mesh::bake_sdf on the GPU. Returns an SdfVolume (host samples), or, with `device_out`
@@ -269,6 +290,20 @@ class CompiledScene:
                                               f(out["beauty"]), f(out["foreground"]), f(out["alpha"]),
                                               f(out["depth"]), f(out["normals"]),
                                               out["material_ids"].ctypes.data_as(P(C.c_uint32))))
+        return out
+
+    def render_gbuffer(self, camera, movers=()):
+        """render_gbuffer (lib.rs:951): a GFrame dict — color (h, w, 4) u8, depth (h, w) f32 (+inf on
+        a miss), obj (h, w) i32 (-1: no mover), camera. `movers`: (centre xyz, radius) per mover."""
+        h, w = self.height, self.width
+        mv = np.ascontiguousarray(np.asarray(movers, np.float32).reshape(-1, 4))
+        out = {"color": np.zeros((h, w, 4), np.uint8), "depth": np.zeros((h, w), np.float32),
+               "obj": np.zeros((h, w), np.int32), "camera": camera}
+        P = C.POINTER
+        self.ctx.check(lib().mm3e_render_gbuffer(self._ptr, C.byref(camera), mv.ctypes.data_as(P(C.c_float)), len(mv),
+                                                 out["color"].ctypes.data_as(P(C.c_uint8)),
+                                                 out["depth"].ctypes.data_as(P(C.c_float)),
+                                                 out["obj"].ctypes.data_as(P(C.c_int32))))
         return out
 
     def march_rays(self, rays6):

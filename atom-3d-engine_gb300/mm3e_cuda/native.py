@@ -86,6 +86,11 @@ def _declare_extra(lib):
         "mm3e_spec_compile_check": (C.c_int, [P(abi.SceneDesc), C.c_char_p, C.c_size_t, P(C.c_double)]),
         "mm3e_render_film": (C.c_int, [C.c_void_p, P(abi.Camera), C.c_float, C.c_float, P(C.c_float), P(C.c_float),
                                        P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_uint32)]),
+        "mm3e_render_gbuffer": (C.c_int, [C.c_void_p, P(abi.Camera), P(C.c_float), C.c_uint32, P(C.c_uint8),
+                                          P(C.c_float), P(C.c_int32)]),
+        "mm3e_reproject": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, P(abi.Camera), P(C.c_uint8), P(C.c_float),
+                                     P(C.c_int32), P(abi.Camera), P(C.c_float), C.c_uint32, C.c_void_p,
+                                     P(C.c_uint8)]),
         "mm3e_scene_parse_mm3e": (C.c_int, [C.c_char_p, P(C.c_void_p), C.c_char_p, C.c_size_t]),
         "mm3e_parsed_scene_desc": (P(abi.SceneDesc), [C.c_void_p]),
         "mm3e_parsed_scene_camera": (C.c_int, [C.c_void_p, P(abi.Camera)]),

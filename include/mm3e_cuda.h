@@ -412,6 +412,25 @@ int mm3e_render_hits(mm3e_scene* scene, const mm3e_camera* camera, float* t, uin
 int mm3e_render_film(mm3e_scene* scene, const mm3e_camera* camera, float aperture_radius, float focus_distance,
                      float* beauty3, float* foreground3, float* alpha, float* depth, float* normals3,
                      uint32_t* material_ids);
+/* render_gbuffer (mm3e-orchestrator/src/lib.rs:951-1039): one pixel-centre sample per pixel, no
+ * post pass. Per pixel (row-major, the scene's width*height): the display colour as RGBA8
+ * (clamp01(gamma(aces(hdr * exposure))) * 255 + 0.5, alpha 255), the primary hit distance t
+ * (+inf on a miss) and the index of the first mover (centre xyz, radius: 4 floats each, may be
+ * NULL when n_movers is 0) whose sphere of radius + 0.05 holds the hit point (-1: none or a miss).
+ * Host outputs; any may be NULL. Blocking. */
+int mm3e_render_gbuffer(mm3e_scene* scene, const mm3e_camera* camera, const float* movers4, uint32_t n_movers,
+                        uint8_t* color4, float* depth, int32_t* obj);
+/* reproject::reproject (mm3e-orchestrator/src/reproject.rs:118-146) when hybrid_scene is NULL:
+ * forward-warp a G-buffer frame (color4 / depth / obj as mm3e_render_gbuffer writes them, taken
+ * at prev_camera, width*height) into new_camera, nearest point per target pixel, pixels of mover
+ * k shifted by mover_deltas3[k] (xyz; k >= n_deltas: no shift), then fill each row's holes from
+ * the last filled pixel to their left (the row's leading holes from its first filled pixel).
+ * With hybrid_scene, reproject_hybrid (lib.rs:1040-1080): the holes are marched and shaded at
+ * new_camera in hybrid_scene instead (display colour as mm3e_render_gbuffer). out4: width*height
+ * RGBA8 (host). Blocking. */
+int mm3e_reproject(mm3e_ctx* ctx, uint32_t width, uint32_t height, const mm3e_camera* prev_camera,
+                   const uint8_t* color4, const float* depth, const int32_t* obj, const mm3e_camera* new_camera,
+                   const float* mover_deltas3, uint32_t n_deltas, mm3e_scene* hybrid_scene, uint8_t* out4);
 /* March `n` rays (origin xyz, unit direction xyz) with the scene's Marcher (march.rs:120-209). */
 int mm3e_march_rays(mm3e_scene* scene, const float* rays6, size_t n, float* t, uint32_t* mat, uint32_t* steps);
 /* World field (accelerated plan) at `n` points: Scene::field (lib.rs:715-717). */

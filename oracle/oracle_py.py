@@ -294,6 +294,19 @@ def render_gbuffer(handle, cam, movers=(), threads=None):
     return out
 
 
+def reproject_filled(g, prev_cam, new_cam, deltas=()):
+    """reproject::warp's filled mask (reproject.rs:77-113): (h, w) u8, 0 where a hole."""
+    h, w = g["depth"].shape
+    dl = np.ascontiguousarray(np.asarray(deltas, np.float32).reshape(-1, 3))
+    out = np.zeros((h, w, 4), np.uint8)
+    filled = np.zeros((h, w), np.uint8)
+    lib().oracle_reproject_warp(w, h, C.addressof(prev_cam), _u8(np.ascontiguousarray(g["color"])),
+                                _f(np.ascontiguousarray(g["depth"])),
+                                np.ascontiguousarray(g["obj"]).ctypes.data_as(P(C.c_int32)), C.addressof(new_cam),
+                                _f(dl), len(dl), _u8(out), _u8(filled))
+    return filled
+
+
 def reproject(g, prev_cam, new_cam, deltas=(), hybrid_handle=None, threads=None):
     """reproject::reproject (cheap row fill) or, with hybrid_handle (the scene), reproject_hybrid:
     (h, w, 4) u8."""
