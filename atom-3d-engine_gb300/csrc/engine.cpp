@@ -73,9 +73,18 @@ cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need
 }
 
 void PreviewBuffers::release() {
+    // fields reset one by one: a temporary PreviewBuffers would run this again from its destructor
     void* ps[] = {color, out, depth, obj, keys, filled, hole_pix, count, mover, delta};
     for (void* p : ps) cudaFree(p);
-    *this = PreviewBuffers();
+    color = out = nullptr;
+    depth = nullptr;
+    obj = nullptr;
+    keys = nullptr;
+    filled = nullptr;
+    hole_pix = count = nullptr;
+    mover = nullptr;
+    delta = nullptr;
+    pixels = movers = deltas = 0;
 }
 
 size_t PreviewBuffers::bytes() const {

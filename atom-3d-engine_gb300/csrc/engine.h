@@ -65,6 +65,9 @@ struct PreviewBuffers {
     uint32_t *hole_pix = nullptr, *count = nullptr;
     float4* mover = nullptr;  // centre xyz, radius
     float* delta = nullptr;   // xyz per mover
+    PreviewBuffers() = default;
+    PreviewBuffers(const PreviewBuffers&) = delete;
+    PreviewBuffers& operator=(const PreviewBuffers&) = delete;
     ~PreviewBuffers() { release(); }
     void release();
     cudaError_t ensure(size_t pixels, size_t movers, size_t deltas);
