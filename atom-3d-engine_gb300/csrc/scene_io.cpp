@@ -326,6 +326,47 @@ void put_err(const std::string& e, char* err, size_t err_len) {
     }
 }
 
+// ---- .sdfv (volume.rs:115-187, 230-248) ----------------------------------------------------
+constexpr size_t SDFV_HEADER = 8 + 3 * 4 + 3 * 4 + 3 * 4;
+const char SDFV_MAGIC[9] = "MM3ESDF1";
+
+uint32_t le_u32(const uint8_t* b) {
+    return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+}
+void put_le_u32(uint8_t* b, uint32_t v) {
+    b[0] = (uint8_t)v;
+    b[1] = (uint8_t)(v >> 8);
+    b[2] = (uint8_t)(v >> 16);
+    b[3] = (uint8_t)(v >> 24);
+}
+float f32_of(uint32_t bits) {
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+}
+uint32_t bits_of(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+
+// SdfVolume::validate_layout (volume.rs:62-87): dims, min and cell rules (the data length is
+// implied by the dims in this interface).
+std::string layout_error(uint64_t nx, uint64_t ny, uint64_t nz, const float* mn, const float* cell) {
+    if (nx < 2 || ny < 2 || nz < 2) return "SdfVolume dims must all be >= 2";
+    if (!(std::isfinite(mn[0]) && std::isfinite(mn[1]) && std::isfinite(mn[2]))) return "SdfVolume min must be finite";
+    if (!(std::isfinite(cell[0]) && std::isfinite(cell[1]) && std::isfinite(cell[2])) ||
+        !(cell[0] > 0.0f && cell[1] > 0.0f && cell[2] > 0.0f))
+        return "SdfVolume cell sizes must be positive and finite";
+    return "";
+}
+
+bool mul_overflows(uint64_t a, uint64_t b, uint64_t& r) {
+    if (a != 0 && b > UINT64_MAX / a) return true;
+    r = a * b;
+    return false;
+}
+
 }  // namespace
 
 extern "C" {
@@ -557,6 +598,93 @@ int mm3e_scene_write_mm3e(const mm3e_scene_desc* d, const mm3e_camera* cam, char
         std::memcpy(out, s.data(), n);
         out[n] = 0;
     }
+    return MM3E_OK;
+}
+
+// SdfVolume::from_sdfv_bytes (volume.rs:140-176)
+int mm3e_volume_parse_sdfv(const uint8_t* bytes, size_t n, mm3e_volume* out, float* data, size_t data_cap,
+                           size_t* n_samples, char* err, size_t err_len) {
+    if ((!bytes && n) || !out) return MM3E_ERR_INVALID;
+    auto failp = [&](const std::string& e) {
+        put_err(e, err, err_len);
+        return MM3E_ERR_INVALID;
+    };
+    if (n < SDFV_HEADER) return failp("sdfv buffer is shorter than the header");
+    if (std::memcmp(bytes, SDFV_MAGIC, 8) != 0) return failp("sdfv magic/version mismatch");
+    uint32_t dims[3] = {le_u32(bytes + 8), le_u32(bytes + 12), le_u32(bytes + 16)};
+    static const char* names[6] = {"min.x", "min.y", "min.z", "cell.x", "cell.y", "cell.z"};
+    float hv[6];
+    for (int i = 0; i < 6; ++i) {
+        hv[i] = f32_of(le_u32(bytes + 20 + 4 * i));
+        if (!std::isfinite(hv[i])) return failp(std::string("sdfv non-finite f32 while reading ") + names[i]);
+    }
+    uint64_t nxy, samples, payload;
+    if (mul_overflows(dims[0], dims[1], nxy) || mul_overflows(nxy, dims[2], samples))
+        return failp("sdfv dimensions overflow");
+    if (mul_overflows(samples, 4, payload) || payload > UINT64_MAX - SDFV_HEADER)
+        return failp("sdfv payload length overflows");
+    uint64_t expected = SDFV_HEADER + payload;
+    if ((uint64_t)n != expected)
+        return failp("sdfv byte length " + std::to_string(n) + " does not match expected " + std::to_string(expected));
+    if (n_samples) *n_samples = (size_t)samples;
+    for (uint64_t i = 0; i < samples; ++i) {
+        uint32_t b = le_u32(bytes + SDFV_HEADER + 4 * i);
+        if (!std::isfinite(f32_of(b))) return failp("sdfv non-finite f32 while reading sample " + std::to_string(i));
+    }
+    // SdfVolume::new: dims and cell rules (the samples are finite by now)
+    std::string e = layout_error(dims[0], dims[1], dims[2], hv, hv + 3);
+    if (!e.empty()) return failp(e);
+    out->nx = dims[0];
+    out->ny = dims[1];
+    out->nz = dims[2];
+    for (int i = 0; i < 3; ++i) {
+        out->min[i] = hv[i];
+        out->cell[i] = hv[3 + i];
+    }
+    out->data = data;
+    if (!data) return MM3E_OK;
+    if (data_cap < samples) return failp("sdfv sample buffer holds " + std::to_string(data_cap) + " of " +
+                                         std::to_string(samples) + " samples");
+    for (uint64_t i = 0; i < samples; ++i) data[i] = f32_of(le_u32(bytes + SDFV_HEADER + 4 * i));
+    return MM3E_OK;
+}
+
+// SdfVolume::to_sdfv_bytes (volume.rs:119-137)
+int mm3e_volume_write_sdfv(const mm3e_volume* v, uint8_t* out, size_t cap, size_t* len, char* err, size_t err_len) {
+    if (!v) return MM3E_ERR_INVALID;
+    uint64_t nxy, samples;
+    if (mul_overflows(v->nx, v->ny, nxy) || mul_overflows(nxy, v->nz, samples)) {
+        put_err("SdfVolume dimensions overflow", err, err_len);
+        return MM3E_ERR_INVALID;
+    }
+    if (!v->data && samples) {
+        put_err("SdfVolume data is missing", err, err_len);
+        return MM3E_ERR_INVALID;
+    }
+    std::string e = layout_error(v->nx, v->ny, v->nz, v->min, v->cell);
+    for (uint64_t i = 0; e.empty() && i < samples; ++i)  // SdfVolume::validate (volume.rs:33-39)
+        if (!std::isfinite(v->data[i])) e = "SdfVolume sample " + std::to_string(i) + " is non-finite";
+    if (!e.empty()) {
+        put_err(e, err, err_len);
+        return MM3E_ERR_INVALID;
+    }
+    uint64_t total = SDFV_HEADER + 4 * samples;
+    if (len) *len = (size_t)total;
+    if (!out) return MM3E_OK;
+    if (cap < total) {
+        put_err("sdfv output buffer holds " + std::to_string(cap) + " of " + std::to_string(total) + " bytes", err,
+                err_len);
+        return MM3E_ERR_INVALID;
+    }
+    std::memcpy(out, SDFV_MAGIC, 8);
+    put_le_u32(out + 8, v->nx);
+    put_le_u32(out + 12, v->ny);
+    put_le_u32(out + 16, v->nz);
+    for (int i = 0; i < 3; ++i) {
+        put_le_u32(out + 20 + 4 * i, bits_of(v->min[i]));
+        put_le_u32(out + 32 + 4 * i, bits_of(v->cell[i]));
+    }
+    for (uint64_t i = 0; i < samples; ++i) put_le_u32(out + SDFV_HEADER + 4 * i, bits_of(v->data[i]));
     return MM3E_OK;
 }
 

@@ -97,6 +97,10 @@ def _declare_extra(lib):
         "mm3e_parsed_scene_free": (None, [C.c_void_p]),
         "mm3e_scene_write_mm3e": (C.c_int, [P(abi.SceneDesc), P(abi.Camera), C.c_char_p, C.c_size_t, P(C.c_size_t),
                                             C.c_char_p, C.c_size_t]),
+        "mm3e_volume_parse_sdfv": (C.c_int, [P(C.c_uint8), C.c_size_t, P(abi.Volume), P(C.c_float), C.c_size_t,
+                                             P(C.c_size_t), C.c_char_p, C.c_size_t]),
+        "mm3e_volume_write_sdfv": (C.c_int, [P(abi.Volume), P(C.c_uint8), C.c_size_t, P(C.c_size_t), C.c_char_p,
+                                             C.c_size_t]),
         "mm3e_autotune": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, C.c_uint32, P(abi.Tuning),
                                     P(abi.TuneEntry), C.c_uint32, P(C.c_uint32)]),
     }

@@ -312,28 +312,15 @@ class SdfVolume:
     SDFV_MAGIC = b"MM3ESDF1"
 
     def to_sdfv_bytes(self):
-        """volume.rs:119-137 `.sdfv` cache format."""
-        hdr = np.array(self.dims, dtype="<u4").tobytes() + np.array(self.min + self.cell, dtype="<f4").tobytes()
-        return self.SDFV_MAGIC + hdr + self.data.astype("<f4").tobytes()
+        """volume.rs:119-137 `.sdfv` cache format (the library's writer)."""
+        from .scene_io import serialize_sdfv
+        return serialize_sdfv(self)
 
     @staticmethod
     def from_sdfv_bytes(b):
-        """volume.rs:140-176."""
-        if len(b) < 44:
-            raise ValueError("sdfv buffer is shorter than the header")
-        if b[:8] != SdfVolume.SDFV_MAGIC:
-            raise ValueError("sdfv magic/version mismatch")
-        nx, ny, nz = np.frombuffer(b[8:20], dtype="<u4")
-        vals = np.frombuffer(b[20:44], dtype="<f4")
-        n = int(nx) * int(ny) * int(nz)
-        if len(b) != 44 + 4 * n:
-            raise ValueError("sdfv byte length does not match expected")
-        if not np.all(np.isfinite(vals)):
-            raise ValueError("sdfv non-finite header")
-        data = np.frombuffer(b[44:], dtype="<f4").astype(F32)
-        if not np.all(np.isfinite(data)):
-            raise ValueError("sdfv non-finite sample")
-        return SdfVolume((nx, ny, nz), vals[:3], vals[3:], data)
+        """volume.rs:140-176 (the library's parser); SceneFormatError (a ValueError) on bad input."""
+        from .scene_io import parse_sdfv
+        return parse_sdfv(b)
 
 
 class GiVolume:

@@ -1,9 +1,12 @@
-"""`.mm3e` text scenes (mm3e-orchestrator/src/scene_io.rs) through the library's parser and writer."""
+"""`.mm3e` text scenes (mm3e-orchestrator/src/scene_io.rs) and `.sdfv` volumes
+(mm3e-kit/src/volume.rs:115-187) through the library's parsers and writers."""
 import ctypes as C
+
+import numpy as np
 
 from . import abi
 from .native import lib
-from .scene import Light, Material, Object, Prim, Scene, Transform
+from .scene import Light, Material, Object, Prim, Scene, SdfVolume, Transform
 
 
 class SceneFormatError(ValueError):
@@ -69,3 +72,42 @@ def serialize(scene, camera):
     buf = C.create_string_buffer(n.value + 1)
     lib().mm3e_scene_write_mm3e(h.ptr, C.byref(camera), buf, n.value + 1, C.byref(n), err, 512)
     return buf.value.decode()
+
+
+def parse_sdfv(data):
+    """SdfVolume::from_sdfv_bytes: an SdfVolume. Raises SceneFormatError with the reference's message."""
+    b = np.frombuffer(bytes(data), np.uint8)
+    P = C.POINTER
+    ptr = b.ctypes.data_as(P(C.c_uint8))
+    v = abi.Volume()
+    n = C.c_size_t()
+    err = C.create_string_buffer(512)
+    rc = lib().mm3e_volume_parse_sdfv(ptr, len(b), C.byref(v), None, 0, C.byref(n), err, 512)
+    if rc != abi.OK:
+        raise SceneFormatError(err.value.decode(errors="replace"))
+    out = np.empty(n.value, np.float32)
+    rc = lib().mm3e_volume_parse_sdfv(ptr, len(b), C.byref(v), out.ctypes.data_as(P(C.c_float)), n.value, None,
+                                      err, 512)
+    if rc != abi.OK:
+        raise SceneFormatError(err.value.decode(errors="replace"))
+    return SdfVolume((v.nx, v.ny, v.nz), tuple(v.min), tuple(v.cell), out)
+
+
+def serialize_sdfv(vol):
+    """SdfVolume::to_sdfv_bytes: the `.sdfv` bytes."""
+    data = np.ascontiguousarray(vol.data, np.float32)
+    v = abi.Volume()
+    v.nx, v.ny, v.nz = (int(d) for d in vol.dims)
+    v.min[:] = [float(x) for x in vol.min]
+    v.cell[:] = [float(x) for x in vol.cell]
+    v.data = data.ctypes.data_as(C.POINTER(C.c_float))
+    n = C.c_size_t()
+    err = C.create_string_buffer(512)
+    rc = lib().mm3e_volume_write_sdfv(C.byref(v), None, 0, C.byref(n), err, 512)
+    if rc != abi.OK:
+        raise SceneFormatError(err.value.decode(errors="replace"))
+    out = (C.c_uint8 * n.value)()
+    rc = lib().mm3e_volume_write_sdfv(C.byref(v), out, n.value, C.byref(n), err, 512)
+    if rc != abi.OK:
+        raise SceneFormatError(err.value.decode(errors="replace"))
+    return bytes(out)

@@ -291,6 +291,19 @@ void mm3e_parsed_scene_free(mm3e_parsed_scene* parsed);
 int mm3e_scene_write_mm3e(const mm3e_scene_desc* desc, const mm3e_camera* camera, char* out, size_t cap, size_t* len,
                           char* err, size_t err_len);
 
+/* SdfVolume::from_sdfv_bytes (mm3e-kit/src/volume.rs:140-176): decodes an `.sdfv` buffer
+ * ("MM3ESDF1", u32 nx ny nz, f32 min xyz, f32 cell xyz, then nx*ny*nz f32 samples, all
+ * little-endian) into `out` (dims, min, cell; out->data = data) and, when `data` is not NULL,
+ * its samples (capacity data_cap floats); *n_samples (may be NULL) receives nx*ny*nz. Errors:
+ * MM3E_ERR_INVALID with the reference's message in err (truncation, magic, non-finite values,
+ * overflow, length mismatch, SdfVolume::new's dims / cell rules). Host only; no GPU needed. */
+int mm3e_volume_parse_sdfv(const uint8_t* bytes, size_t n, mm3e_volume* out, float* data, size_t data_cap,
+                           size_t* n_samples, char* err, size_t err_len);
+/* SdfVolume::to_sdfv_bytes (volume.rs:119-137): validates the volume (volume.rs:33-87) and
+ * encodes it into out (capacity cap bytes; NULL: only *len). *len receives the encoded size. */
+int mm3e_volume_write_sdfv(const mm3e_volume* volume, uint8_t* out, size_t cap, size_t* len, char* err,
+                           size_t err_len);
+
 /* ---- context ----------------------------------------------------------------------------- */
 int mm3e_ctx_create(int device, mm3e_ctx** out);
 /* Destroys the context and every scene still compiled on it (their handles become invalid). */
