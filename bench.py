@@ -24,6 +24,7 @@ each rank renders its own frames (scaling "weak").
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -120,6 +121,62 @@ def bench_cornell(ctx, stream, torch):
             "frame_ms_median": statistics.median(ms), "gi_probes": "32^3 ambient cubes, 5 rays per face",
             "gi_bake_ms_host_wall": bake_s * 1000.0, "gi_bake_rays": 32 ** 3 * 6 * 5,
             "field": "scene-specialised (NVRTC)" if specialized else "tape interpreter"}
+
+
+def bench_preview(ctx, torch, with_cpu):
+    """Preview path at 1920x1080 on the gallery scene: render_gbuffer, then the camera moved 0.2
+    along its right axis and the frame reprojected (row fill) and hybrid-reprojected (holes
+    re-rendered). Host buffers in and out, host wall time per call (median of 5 after a warm-up).
+    CPU leg: the oracle's G-buffer frame on all host cores and its hybrid reprojection."""
+    import numpy as np
+
+    from mm3e_cuda import scenes
+    from mm3e_cuda.scene import look_at
+
+    import mm3e_cuda
+
+    s, c0 = scenes.gallery_scene(1920, 1080)
+    eye, fwd, right = (np.array(c0.eye[:], np.float32), np.array(c0.forward[:], np.float32),
+                       np.array(c0.right[:], np.float32))
+    e1 = eye + np.float32(0.2) * right
+    c1 = look_at(tuple(float(x) for x in e1), tuple(float(x) for x in e1 + fwd), (0.0, 1.0, 0.0),
+                 2.0 * math.atan(c0.fov_scale))
+    cs = mm3e_cuda.CompiledScene(ctx, s)
+    cs.specialize(cs.SPEC_AUTO)
+
+    def wall(fn, k=5):
+        fn()
+        ts = []
+        for _ in range(k):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = fn()
+            ts.append((time.perf_counter() - t0) * 1000.0)
+        return statistics.median(ts), out
+
+    g_ms, g = wall(lambda: cs.render_gbuffer(c0))
+    r_ms, _ = wall(lambda: ctx.reproject(g, c1))
+    h_ms, hyb = wall(lambda: ctx.reproject(g, c1, hybrid_scene=cs))
+    full_ms, truth = wall(lambda: cs.render_gbuffer(c1))
+    cs.close()
+    out = {"workload": "gallery_1080p_preview", "camera_move": "0.2 along the camera's right axis",
+           "render_gbuffer_ms": g_ms, "reproject_ms": r_ms, "reproject_hybrid_ms": h_ms,
+           "hybrid_matches_full_view": float((hyb == truth["color"]).all(-1).mean()),
+           "timing": "host wall per call, host buffers (H2D / D2H inside)"}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = oracle_py.render_gbuffer(s.desc(), c0, threads=threads)
+        t_g = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        oracle_py.reproject(ref, c0, c1, hybrid_handle=s.desc(), threads=threads)
+        t_h = time.perf_counter() - t0
+        out["cpu_baseline"] = {"render_gbuffer_ms": t_g * 1000.0, "reproject_hybrid_ms": t_h * 1000.0,
+                               "cores": threads, "kind": "port", "sample": "one full 1920x1080 frame each"}
+    return out
 
 
 def bench_batched(ctx, stream, torch, n_scenes):
@@ -536,6 +593,7 @@ def run_ours(args):
     if not args.no_forms and world == 1:
         line["cornell"] = bench_cornell(ctx, stream, torch)
         line["batched"] = bench_batched(ctx, stream, torch, args.batch_scenes)
+        line["preview"] = bench_preview(ctx, torch, not args.no_cpu)
         ctx.set_stream(None)
         line["served"] = bench_served(lambda: mm3e_cuda.Context(local), args.served_seconds, args.served_max_requests)
     print(json.dumps(line))
