@@ -25,6 +25,15 @@
  *                             (appearance.rs:250-269, mm3e-gpu/src/wgsl.rs:41-47,
  *                             mm3e-gpu/src/lib.rs:139-141, csg.rs:154-236)
  *   mm3e_last_error        <- the `Err(String)` of every checked reference call
+ *   mm3e_render_film       <- film::render_film with a thin Lens (film.rs:63-224, camera.rs:25-102)
+ *   mm3e_render_gbuffer    <- render_gbuffer_checked (mm3e-orchestrator/src/lib.rs:951-1039)
+ *   mm3e_reproject         <- reproject::reproject (reproject.rs:118-146) and
+ *                             reproject_hybrid (lib.rs:1040-1080)
+ *   mm3e_bake_mesh_sdf     <- mesh::bake_sdf (mm3e-orchestrator/src/mesh.rs:262-336)
+ *   mm3e_scene_parse_mm3e  <- scene_io::parse (mm3e-orchestrator/src/scene_io.rs:196-281)
+ *   mm3e_scene_write_mm3e  <- scene_io::try_serialize (scene_io.rs:32-120)
+ *   mm3e_volume_parse_sdfv <- SdfVolume::from_sdfv_bytes (mm3e-kit/src/volume.rs:140-176)
+ *   mm3e_volume_write_sdfv <- SdfVolume::to_sdfv_bytes (volume.rs:119-137)
  *
  * Conventions: 0 = success, negative = error (message via mm3e_last_error). Contexts are not
  * thread-safe: use one context per host thread. All floats are IEEE binary32.
@@ -319,8 +328,9 @@ int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
 /* Launch shape of the march and soft-shadow passes: threads per CTA (128 or 256), pixel tile
  * of 32 pixels 2^tile_wlog wide (tile_wlog 0..5; 3 = 8x4), and field samples per lane between
  * work refills (unroll 1 or 2); min_blocks (0..16) asks the compiler of scene-specialised
- * kernels to fit that many CTAs per SM in the register file (0: its own choice). Results do not
- * depend on it. mm3e_autotune picks block / tile / unroll. */
+ * kernels to fit that many CTAs per SM in the register file (0: the compiler's choice for the
+ * shadow / AO kernels and 7 CTAs of 128 or 3 of 256 for the march kernel). Results do not depend
+ * on it. mm3e_autotune picks block / tile / unroll. */
 typedef struct mm3e_tuning {
     uint32_t block, tile_wlog, unroll, min_blocks;
 } mm3e_tuning;
