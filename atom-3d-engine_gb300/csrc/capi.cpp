@@ -527,6 +527,9 @@ int mm3e_ctx_create(int device, mm3e_ctx** out) {
     cudaEventCreate(&c->ev1);
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     cudaDeviceGetAttribute(&c->clock_khz, cudaDevAttrClockRate, device);
+    int ats = 0;
+    cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+    c->host_access = ats == 1;
     *out = c.release();
     return MM3E_OK;
 }
@@ -546,6 +549,13 @@ void mm3e_ctx_destroy(mm3e_ctx* ctx) {
 }
 
 const char* mm3e_last_error(const mm3e_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int mm3e_ctx_set_host_writes(mm3e_ctx* ctx, int enable, int* active) {
+    if (!ctx) return MM3E_ERR_INVALID;
+    ctx->host_writes = enable != 0;
+    if (active) *active = ctx->host_access && ctx->host_writes ? 1 : 0;
+    return MM3E_OK;
+}
 
 int mm3e_ctx_sync(mm3e_ctx* ctx) {
     if (!ctx) return MM3E_ERR_INVALID;
@@ -669,20 +679,23 @@ int mm3e_render(mm3e_scene* s, const mm3e_camera* camera, const mm3e_dyn_sphere*
     int rc = validate_dynamic(s->src.d, dyn, n_dyn, err);
     if (rc) return fail(c, rc, err);
     cudaSetDevice(c->device);
-    rc = ensure_frame_buffers(s, true);
+    // On a host whose page tables the device shares, the post kernel stores the frame straight
+    // into the caller's buffer over the coherent link: no staging copy, no host memcpy.
+    const bool direct = n && c->host_access && c->host_writes && ((uintptr_t)host_out % (px == 4 ? 4u : 16u)) == 0;
+    rc = ensure_frame_buffers(s, !direct);
     if (rc) return rc;
     LaunchLog log = c->prof.log();
     cudaEventRecord(c->ev0, c->stream);
-    rc = render_to_device(s, camera, dyn, n_dyn, format, (void*)s->d_out, false, &log);
+    rc = render_to_device(s, camera, dyn, n_dyn, format, direct ? host_out : (void*)s->d_out, false, &log);
     if (rc) return rc;
     cudaEventRecord(c->ev1, c->stream);
-    if (n) {
+    if (n && !direct) {
         cudaError_t e = cudaMemcpyAsync(s->h_stage, s->d_out, n * px, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(c, e, "framebuffer download");
     }
     rc = check_status(s);
     if (rc) return rc;
-    if (n) std::memcpy(host_out, s->h_stage, n * px);
+    if (n && !direct) std::memcpy(host_out, s->h_stage, n * px);
     if (stats) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, c->ev0, c->ev1);

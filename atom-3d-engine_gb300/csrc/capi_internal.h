@@ -23,6 +23,10 @@ struct mm3e_ctx {
     cudaStream_t own_stream = nullptr;  // the context's own stream
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int sm_count = 0, clock_khz = 0;
+    // The device reaches pageable host memory through the host's page tables (a coherent
+    // NVLink-C2C host such as Grace): kernels then write host framebuffers directly.
+    bool host_access = false;
+    bool host_writes = true;  // use that for host outputs (mm3e_ctx_set_host_writes)
     std::string err;
     std::set<mm3e_scene*> scenes;       // live scenes; destroyed with the context
     mm3e::TuneParams tune;              // launch shape of the march / shadow passes

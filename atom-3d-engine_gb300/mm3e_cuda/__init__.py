@@ -78,6 +78,13 @@ class Context:
     def set_profiling(self, on=True):
         self.check(lib().mm3e_ctx_set_profiling(self._ptr, 1 if on else 0))
 
+    def set_host_writes(self, on=True):
+        """Direct kernel writes into host framebuffers where the device shares the host's page
+        tables (default on); returns whether they are in use."""
+        active = C.c_int()
+        self.check(lib().mm3e_ctx_set_host_writes(self._ptr, 1 if on else 0, C.byref(active)))
+        return bool(active.value)
+
     def kernel_times(self):
         """{kind: (launches, ms)} of the passes run since the last call (profiling on)."""
         arr = (abi.KernelTime * 16)()
@@ -235,10 +242,15 @@ class CompiledScene:
         self.ctx.check(lib().mm3e_scene_device_bytes(self._ptr, C.byref(n)))
         return n.value
 
-    def render(self, camera, dyn_spheres=(), fmt=abi.FB_RGBA_F32, stats=False):
-        """Framebuffer of the frame: (h, w, 4) f32 RGBA, or (h, w, 4) u8 for FB_RGBA8."""
+    def render(self, camera, dyn_spheres=(), fmt=abi.FB_RGBA_F32, stats=False, out=None):
+        """Framebuffer of the frame: (h, w, 4) f32 RGBA, or (h, w, 4) u8 for FB_RGBA8; into `out`
+        (a C-contiguous array of that shape and type, reused across frames) when given."""
         h, w = self.height, self.width
-        out = np.empty((h, w, 4), dtype=np.float32 if fmt == abi.FB_RGBA_F32 else np.uint8)
+        dtype = np.float32 if fmt == abi.FB_RGBA_F32 else np.uint8
+        if out is None:
+            out = np.empty((h, w, 4), dtype=dtype)
+        elif out.shape != (h, w, 4) or out.dtype != dtype or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous ({h}, {w}, 4) {np.dtype(dtype).name} array")
         dyn = (abi.DynSphere * max(1, len(dyn_spheres)))(*[s.to_abi() for s in dyn_spheres])
         st = abi.RenderStats()
         rc = lib().mm3e_render(self._ptr, C.byref(camera), dyn, len(dyn_spheres), fmt,

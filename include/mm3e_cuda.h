@@ -348,6 +348,13 @@ typedef struct mm3e_kernel_time {
     double ms;
 } mm3e_kernel_time;
 int mm3e_ctx_set_profiling(mm3e_ctx* ctx, int enable);
+/* Host framebuffers of mm3e_render: where the device reaches pageable host memory through the
+ * host's page tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables, e.g. a Grace host on
+ * NVLink-C2C), the post kernel writes the caller's buffer directly (default on); otherwise, or
+ * with enable = 0 or an unaligned buffer (RGBA8: 4 bytes, RGBA f32: 16 bytes), the frame is
+ * staged through pinned memory. Frames are identical either way. *active (may be NULL) receives
+ * 1 when direct writes are in use. */
+int mm3e_ctx_set_host_writes(mm3e_ctx* ctx, int enable, int* active);
 int mm3e_ctx_kernel_times(mm3e_ctx* ctx, mm3e_kernel_time* out, uint32_t cap, uint32_t* n_out);
 
 /* ---- scenes ------------------------------------------------------------------------------- */

@@ -5,6 +5,7 @@
 (iii) final RGB8 within 1 LSB on >= 99.9% of pixels, PSNR >= 50 dB
 All calls go through the C ABI (libmm3e_cuda.so).
 """
+import ctypes as C
 import json
 
 import numpy as np
@@ -187,3 +188,28 @@ def test_unsupported_surface_rejected(gpu_ctx):
     with pytest.raises(mm3e_cuda.RenderError) as e:
         mm3e_cuda.CompiledScene(gpu_ctx, scene)
     assert e.value.code == abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("fmt", [abi.FB_RGBA8, abi.FB_RGBA_F32])
+def test_host_writes_equal_staged_frames(gpu_ctx, fmt):
+    """mm3e_render's direct stores into the caller's host buffer (where the device shares the
+    host's page tables) give the staged path's frame byte for byte, also for a buffer that is not
+    aligned for direct stores (which then stages)."""
+    scene, cam = scenes.gallery_scene(320, 180)
+    cs = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    try:
+        direct = gpu_ctx.set_host_writes(True)
+        a = cs.render(cam, fmt=fmt)
+        gpu_ctx.set_host_writes(False)
+        b = cs.render(cam, fmt=fmt)
+        print("direct host writes active:", direct)
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+        gpu_ctx.set_host_writes(True)
+        px = 4 if fmt == abi.FB_RGBA8 else 16
+        raw = np.zeros(scene.width * scene.height * px + 16, np.uint8)
+        off = raw[1:1 + scene.width * scene.height * px]  # misaligned by one byte
+        rc = mm3e_cuda.lib().mm3e_render(cs._ptr, C.byref(cam), None, 0, fmt, off.ctypes.data, off.nbytes, None)
+        assert rc == abi.OK
+        assert np.array_equal(off, a.view(np.uint8).reshape(-1))
+    finally:
+        gpu_ctx.set_host_writes(True)
