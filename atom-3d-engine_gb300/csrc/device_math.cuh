@@ -151,6 +151,17 @@ MD Field f_smooth_union(Field a, Field b, float k) {  // sdf.rs:152-160
 }
 MD float rep_axis(float v, float period) { return period > 0.0f ? v - period * roundf(v / period) : v; }
 
+// Cull pre-test of a bounded union member (accel.rs:98-100: a sphere whose lower bound exceeds the
+// best distance so far cannot win). With d2 = length_sq(p - c) computed exactly as length() does,
+// true only when fl(fl(sqrt(d2)) - r) > bd holds for certain: squared distances with a relative
+// margin of 2^-14, far wider than the few roundings on either side, and only for bd >= 0 (where
+// a margin proportional to bd + r also clears bd's own rounding step). Skips the square root of
+// members that the exact test would cull anyway; never culls one that it would keep.
+MD bool far_beyond(float d2, float bd, float r) {
+    float q = bd + r;
+    return bd >= 0.0f && d2 > q * q * 1.00006103515625f;
+}
+
 // ---- tape view ----
 struct Tape {
     const TapeHeader* h;

@@ -4,7 +4,9 @@
 #include <dlfcn.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -106,6 +108,54 @@ std::string lower_expr(const DevObject& o) {
     return "length(p - V{" + fbits(o.bc[0]) + ", " + fbits(o.bc[1]) + ", " + fbits(o.bc[2]) + "}) - " + fbits(o.br);
 }
 
+// Spatial groups of at most 4 union members (median splits on the longest axis of their bound
+// centres) with an enclosing sphere: for every member, |c - ci| + ri <= r holds in exact
+// arithmetic with a relative margin of 2^-20, so a member's own bound test never keeps a point
+// that the cluster's test culled.
+struct MemberCluster {
+    std::vector<uint32_t> members;
+    float c[3];
+    float r;
+};
+
+void cluster_members(const DevObject* obj, std::vector<uint32_t> m, std::vector<MemberCluster>& out) {
+    if (m.empty()) return;
+    if (m.size() <= 4) {
+        MemberCluster cl;
+        cl.members = m;
+        double mean[3] = {0.0, 0.0, 0.0};
+        for (uint32_t i : m)
+            for (int a = 0; a < 3; ++a) mean[a] += obj[i].bc[a];
+        for (int a = 0; a < 3; ++a) cl.c[a] = (float)(mean[a] / (double)m.size());
+        double r = 0.0;
+        for (uint32_t i : m) {
+            double dx = (double)obj[i].bc[0] - cl.c[0], dy = (double)obj[i].bc[1] - cl.c[1],
+                   dz = (double)obj[i].bc[2] - cl.c[2];
+            double e = std::sqrt(dx * dx + dy * dy + dz * dz) + (double)obj[i].br;
+            if (e > r) r = e;
+        }
+        r = r * (1.0 + 1.0 / 1048576.0) + 1e-30;
+        float rf = (float)r;
+        if ((double)rf < r) rf = std::nextafter(rf, INFINITY);
+        cl.r = rf;
+        out.push_back(std::move(cl));
+        return;
+    }
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i : m)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], obj[i].bc[a]);
+            hi[a] = std::max(hi[a], obj[i].bc[a]);
+        }
+    int axis = 0;
+    for (int a = 1; a < 3; ++a)
+        if (hi[a] - lo[a] > hi[axis] - lo[axis]) axis = a;
+    std::stable_sort(m.begin(), m.end(), [&](uint32_t x, uint32_t y) { return obj[x].bc[axis] < obj[y].bc[axis]; });
+    size_t half = m.size() / 2;
+    cluster_members(obj, std::vector<uint32_t>(m.begin(), m.begin() + half), out);
+    cluster_members(obj, std::vector<uint32_t>(m.begin() + half, m.end()), out);
+}
+
 }  // namespace
 
 std::string nvrtc_status() { return nvrtc().status; }
@@ -180,12 +230,16 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             if (comb_exact == sg.b) os << "        " << fold(sg.b) << "\n";
             else os << "        if (sub) { " << fold(sg.b) << " } else { " << fold(comb_exact) << " }\n";
         } else if (sg.kind == SEG_LINEAR) {
+            // The fold is an argmin with lowest-index ties (the seed, index -1, wins its ties), and
+            // a culled member cannot reach the minimum, so any member order gives the same
+            // result: members that are never culled go first, then the cullable ones in spatial
+            // clusters whose enclosing-sphere pre-test skips a whole cluster at once.
             bool any_noncons = false;
             os << "        float bd = " << (seeded ? "acc.d" : "INF") << ";\n        int32_t bi = "
                << (seeded ? "-1" : "0x7FFFFFFF") << ";\n        uint32_t bm = " << (seeded ? "acc.m" : "0u")
                << ";\n        bool bnc = false;\n";
-            for (uint32_t k = 0; k < sg.b; ++k) {
-                uint32_t i = unb[sg.a + k];
+            std::vector<uint32_t> cullable;
+            auto member = [&](uint32_t i, bool cull) {
                 const DevObject& o = obj[i];
                 bool nc = (o.flags & OF_NONCONS) != 0;
                 any_noncons = any_noncons || nc;
@@ -195,17 +249,39 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                                     (nc ? "true" : "false") + ";\n            }\n";
                 os << "        {  // member " << i << "\n";
                 if (o.flags & OF_BOUND) {
-                    os << "            float lower = " << lower_expr(o) << ";\n";
-                    if (!nc) os << "            if (!(lower > bd)) {\n";
+                    if (cull) {
+                        os << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
+                           << ", " << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, bd, " << fbits(o.br)
+                           << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n";
+                    } else {
+                        os << "            float lower = " << lower_expr(o) << ";\n";
+                    }
+                    if (cull) os << "            if (!(lower > bd)) {\n";
                     os << "            if (lower > " << slack << ") {\n                if (lower < bd || (lower == bd && "
                        << i << " < bi)) {\n                    bd = lower;\n                    bi = " << i
                        << ";\n                    bm = " << o.mat << "u;\n                    bnc = false;\n"
                        << "                }\n            } else {\n            " << exact << "            }\n";
-                    if (!nc) os << "            }\n";
+                    if (cull) os << "            }\n            }\n";
                 } else {
                     os << "            " << exact;
                 }
                 os << "        }\n";
+            };
+            for (uint32_t k = 0; k < sg.b; ++k) {
+                uint32_t i = unb[sg.a + k];
+                bool cull = (obj[i].flags & OF_BOUND) && !(obj[i].flags & OF_NONCONS);
+                if (cull) cullable.push_back(i);
+                else member(i, false);
+            }
+            std::vector<MemberCluster> clusters;
+            cluster_members(obj, cullable, clusters);
+            for (const MemberCluster& cl : clusters) {
+                if (cl.members.size() > 1)
+                    os << "        if (!far_beyond(length_sq(p - V{" << fbits(cl.c[0]) << ", " << fbits(cl.c[1]) << ", "
+                       << fbits(cl.c[2]) << "}), bd, " << fbits(cl.r) << ")) {  // cluster of "
+                       << cl.members.size() << "\n";
+                for (uint32_t i : cl.members) member(i, true);
+                if (cl.members.size() > 1) os << "        }  // end of cluster\n";
             }
             if (any_noncons)
                 os << "        if (bnc) acc = bvh_segment(T, " << s << "u, p, " << (seeded ? "true" : "false")

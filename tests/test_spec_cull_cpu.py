@@ -1,0 +1,112 @@
+"""The specialised field's cull pre-tests never cull a member that the exact bound test keeps.
+
+A LINEAR union member is skipped when its bound lower = |p - c| - r exceeds the best distance so
+far (accel.rs:98-100). The generated code first tests squared distances with a relative margin
+(far_beyond in device_math.cuh) for single members and for spatial clusters of members, skipping
+the square root. These tests replay that arithmetic in IEEE binary32 (numpy float32: correctly
+rounded, no contraction, as the device code compiled with --fmad=false) on adversarial points
+just outside the cull boundary, and check the clusters' enclosing spheres in exact arithmetic.
+"""
+import re
+from fractions import Fraction
+
+import numpy as np
+
+import mm3e_cuda
+from mm3e_cuda import scenes
+
+F = np.float32
+M = F(1.00006103515625)  # 1 + 2^-14
+
+
+def far_beyond(d2, bd, r):
+    q = F(bd + r)
+    return (bd >= F(0)) & (d2 > F(F(q * q) * M))
+
+
+def length_sq(e):
+    return F(F(F(e[..., 0] * e[..., 0]) + F(e[..., 1] * e[..., 1])) + F(e[..., 2] * e[..., 2]))
+
+
+def exact_lower(p, c, r):
+    e = (p - c).astype(F)
+    return F(np.sqrt(length_sq(e)).astype(F) - r)
+
+
+def _points_near(rng, c, radius, n):
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    scale = radius * (1.0 + rng.uniform(-2e-4, 2e-4, n))
+    return (c.astype(np.float64) + d * scale[:, None]).astype(F)
+
+
+def test_member_pretest_implies_exact_cull():
+    rng = np.random.default_rng(11)
+    for _ in range(40):
+        c = rng.uniform(-50, 50, 3).astype(F)
+        r = F(rng.choice([0.0, rng.uniform(1e-3, 8.0)]))
+        bd = F(rng.choice([0.0, rng.uniform(1e-6, 1e-2), rng.uniform(0.01, 30.0)]))
+        p = _points_near(rng, c, float(bd) + float(r), 20000)
+        d2 = length_sq((p - c).astype(F))
+        skip = far_beyond(d2, bd, r)
+        lower = exact_lower(p, c, r)
+        assert (lower[skip] > bd).all()
+        # the margin is narrow: most points the exact test culls are culled by the pre-test too
+        culled = lower > bd
+        if culled.sum() > 1000:
+            assert skip.sum() >= 0.5 * culled.sum()
+
+
+def test_negative_best_is_never_pretested():
+    d2 = np.array([1e6], F)
+    assert not far_beyond(d2, F(-0.5), F(1.0)).any()
+
+
+def _clusters(src):
+    """(centre, radius, [(member centre, member radius)]) of every cluster in generated source."""
+    hexf = lambda h: np.array([int(h, 16)], np.uint32).view(F)[0]
+    out, cur = [], None
+    lines = src.splitlines()
+    for k, line in enumerate(lines):
+        m = re.search(r"far_beyond\(length_sq\(p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
+                      r"__uint_as_float\(0x(\w+)u\)\}\), bd, __uint_as_float\(0x(\w+)u\)\)\) \{  // cluster", line)
+        if m:
+            cur = (np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(m.group(4)), [])
+            out.append(cur)
+            continue
+        m = re.search(r"const float d2 = length_sq\(p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
+                      r"__uint_as_float\(0x(\w+)u\)\}\);", line)
+        if m and cur is not None:
+            r = re.search(r"far_beyond\(d2, bd, __uint_as_float\(0x(\w+)u\)\)", lines[k + 1])
+            cur[2].append((np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(r.group(1))))
+        if "// end of cluster" in line:
+            cur = None
+    return out
+
+
+def _exact_norm_le(v, bound):
+    """|v| <= bound in exact rational arithmetic (v, bound: float32 values)."""
+    s = sum(Fraction(float(x)) ** 2 for x in v)
+    b = Fraction(float(bound))
+    return b >= 0 and s <= b * b
+
+
+def test_cluster_spheres_enclose_members_and_cull_safely():
+    rng = np.random.default_rng(5)
+    sources = [mm3e_cuda.spec_source(scenes.gallery_scene(64, 36)[0]),
+               mm3e_cuda.spec_source(scenes.procedural_scene(3, 64, 48)[0]),
+               mm3e_cuda.spec_source(scenes.canonical_asset_scene()[0])]
+    n_clusters = 0
+    for src in sources:
+        for C, R, members in _clusters(src):
+            assert len(members) >= 2
+            n_clusters += 1
+            for c, r in members:
+                # |C - c| + r <= R exactly
+                assert _exact_norm_le((C.astype(np.float64) - c.astype(np.float64)), Fraction(float(R)) - Fraction(float(r)))
+            for bd in (F(0.0), F(1e-4), F(0.3), F(4.0)):
+                p = _points_near(rng, C, float(bd) + float(R), 20000)
+                skip = far_beyond(length_sq((p - C).astype(F)), bd, R)
+                for c, r in members:
+                    assert (exact_lower(p[skip], c, r) > bd).all()
+    assert n_clusters >= 2
