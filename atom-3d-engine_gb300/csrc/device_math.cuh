@@ -328,6 +328,13 @@ struct NodeStack {
     }
 };
 
+// Whether an exactly evaluated OF_NONCONS member's field d may lie below its bounding sphere's
+// lower bound (lower, radius r) at this point, so that the BVH walk might prune the member while
+// the linear fold picks it. A winner clear of its bound by a relative margin of 2^-10 cannot be
+// pruned by the walk: every node on its path has a lower bound no larger than the member's
+// (their spheres enclose its sphere), so a pruning best would already be below the winner.
+MD bool noncons_undercut(float d, float lower, float r) { return !(d > lower + (r + fabsf(lower)) * 0.0009765625f); }
+
 // WorldPlan::eval (accel.rs:209-252) with Bvh::query (accel.rs:79-119) and
 // WorldPlan::contrib (accel.rs:187-207). The plan is walked as a generator so that the exact
 // object field has a single call site: each outer iteration advances the plan to the next
@@ -336,7 +343,8 @@ struct NodeStack {
 // exactly one outer iteration per object on every lane, so lanes stay in step and the object
 // (hence the primitive code) is warp-uniform. BVH runs walk per lane, near child first, with
 // the reference's `lower > best` pruning and `lower > slack` bounding-sphere substitute; a
-// LINEAR run whose winner is an exactly evaluated OF_NONCONS member falls back to that walk.
+// LINEAR run whose winner is an exactly evaluated OF_NONCONS member that may undercut its
+// bounding sphere here (noncons_undercut) falls back to that walk.
 __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
     const float INF = __int_as_float(0x7f800000);
     const float slack = T.h->slack;
@@ -347,7 +355,9 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
     float bd = INF;
     int32_t bi = 0x7FFFFFFF;
     uint32_t bm = 0u;
-    bool bex = false;  // the linear winner was evaluated exactly
+    bool bex = false;  // the linear winner is an OF_NONCONS field that may undercut its sphere
+    bool wnc = false;  // the member being evaluated is a bounded OF_NONCONS one (lower wl, radius wr)
+    float wl = 0.0f, wr = 0.0f;
     uint32_t s = 0, st = W_START, ucur = 0, uend = 0, one = 0;
     NodeStack stk;
     stk.clear();
@@ -397,7 +407,7 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
             }
             if (st == W_LIN) {
                 if (ucur >= uend) {
-                    if (bex && bi >= 0 && (T.obj[bi].flags & OF_NONCONS)) {
+                    if (bex) {
                         // the winner may be one the BVH walk prunes: redo this run as the walk
                         DevSegment sg = T.seg[s];
                         bd = seeded ? acc.d : INF;
@@ -420,8 +430,11 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
                 ucur += 1;
                 step = true;
                 const DevObject& o = T.obj[i];
+                wnc = (o.flags & OF_NONCONS) && (o.flags & OF_BOUND);
                 if (o.flags & OF_BOUND) {
                     float lower = length(p - ld3(o.bc)) - o.br;
+                    wl = lower;
+                    wr = o.br;
                     if (lower > bd && !(o.flags & OF_NONCONS)) break;  // cannot win
                     if (lower > slack) {
                         if (lower < bd || (lower == bd && i < bi)) {
@@ -491,7 +504,7 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
             bd = f.d;
             bi = want;
             bm = f.m;
-            bex = true;
+            bex = st == W_LIN && wnc && noncons_undercut(f.d, wl, wr);
         }
     }
     return acc;

@@ -242,11 +242,14 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             auto member = [&](uint32_t i, bool cull) {
                 const DevObject& o = obj[i];
                 bool nc = (o.flags & OF_NONCONS) != 0;
-                any_noncons = any_noncons || nc;
+                // a bounded OF_NONCONS winner needs the BVH walk only where it may undercut its sphere
+                const bool nc_bounded = nc && (o.flags & OF_BOUND);
+                const std::string undercut = nc_bounded ? "noncons_undercut(f.d, lower, " + fbits(o.br) + ")" : "false";
                 std::string exact = "Field f = obj_" + std::to_string(i) + "(T, p);\n            if (f.d < bd || (f.d == bd && " +
                                     std::to_string(i) + " < bi)) {\n                bd = f.d;\n                bi = " +
                                     std::to_string(i) + ";\n                bm = f.m;\n                bnc = " +
-                                    (nc ? "true" : "false") + ";\n            }\n";
+                                    undercut + ";\n            }\n";
+                any_noncons = any_noncons || nc_bounded;
                 os << "        {  // member " << i << "\n";
                 if (o.flags & OF_BOUND) {
                     if (cull) {

@@ -81,8 +81,9 @@ enum : uint32_t { SEG_ONE = 0, SEG_RUN = 1, SEG_LINEAR = 2 };
 //   rule gives the BVH query's result whenever the winner's field is not below its bounding
 //   sphere's distance (a subtree the BVH prunes can then never hold the minimum); the only
 //   members whose fields can undercut their spheres are exactly-evaluated ellipsoids and
-//   octahedra (OF_NONCONS), and a lane whose linear winner is one of those re-runs the BVH
-//   walk. The linear fold is warp-uniform.
+//   octahedra (OF_NONCONS), and a lane whose linear winner is one of those, at a point where
+//   its field is not clear of its sphere's bound, re-runs the BVH walk. The linear fold is
+//   warp-uniform.
 struct alignas(16) DevSegment {
     uint32_t kind, a, b, c;
     uint32_t ua, ub, pad0, pad1;
