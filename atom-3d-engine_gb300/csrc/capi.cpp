@@ -7,6 +7,7 @@
 // constructors is binary32 without contraction (this file is compiled with -ffp-contract=off).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -215,7 +216,7 @@ int upload_tape(mm3e_scene* s, const LoweredScene& low, unsigned char** dst, siz
 int ensure_frame_buffers(mm3e_scene* s, bool host) {
     mm3e_ctx* c = s->ctx;
     cudaError_t e;
-    uint32_t wlog = c->tune.tile_wlog;
+    uint32_t wlog = s->tuning().tile_wlog;
     size_t n = (size_t)s->low.width * s->low.height;
     size_t samples = slots_of(s->low.width, s->low.height, wlog) * s->low.aa * s->low.aa;
     if (n != s->pixels) {
@@ -320,7 +321,7 @@ int march_centers(mm3e_scene* s, const mm3e_camera* cam, const unsigned char* ta
     a.n_items = n;
     a.counter = s->buf.counters;
     const SpecKernels* sp = tape == s->d_tape ? s->spec_kernels() : nullptr;
-    CK(launch_march(a, c->tune, c->stream, c->sm_count, log, sp));
+    CK(launch_march(a, s->tuning(), c->stream, c->sm_count, log, sp));
     if (want_ao) CK(launch_ao(a, c->stream, log, sp));
     return MM3E_OK;
 }
@@ -353,7 +354,7 @@ int render_to_device(mm3e_scene* s, const mm3e_camera* cam, const mm3e_dyn_spher
         PassPlan p = scene_plan(s, tape, tape_bytes, *cam, format, dout);
         if (n_dyn == 0) p.spec = s->spec_kernels();  // the specialised field is the scene's own tape
         p.post = !linear_only;
-        CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, log));
+        CK(run_beauty(p, s->buf, s->tuning(), c->stream, c->sm_count, log));
         return MM3E_OK;
     }
     const TapeHeader* th = reinterpret_cast<const TapeHeader*>(s->low.blob.data());
@@ -967,8 +968,9 @@ int mm3e_scene_specialize(mm3e_scene* s, int mode, double* compile_ms) {
     if (mode == 0) return MM3E_OK;
     if (mode == 1 && spec_size(s->low.blob).objects > SPEC_AUTO_MAX_OBJECTS) return MM3E_OK;  // interpreter is faster
     bool smem = s->low.blob.size() <= 96 * 1024;
-    uint32_t block = c->tune.block, unroll = c->tune.unroll;
-    std::string src = spec_source(s->low.blob, block, unroll, smem, c->tune.min_blocks);
+    const TuneParams& t = s->tuning();
+    uint32_t block = t.block, unroll = t.unroll;
+    std::string src = spec_source(s->low.blob, block, unroll, smem, t.min_blocks);
     std::unique_ptr<SpecModule> m(new SpecModule());
     m->kernels.block = block;
     m->kernels.smem_tape = smem;
@@ -979,6 +981,74 @@ int mm3e_scene_specialize(mm3e_scene* s, int mode, double* compile_ms) {
 }
 
 int mm3e_scene_is_specialized(mm3e_scene* s) { return s && s->spec ? 1 : 0; }
+
+// Launch-shape search for one scene's plain frames: each candidate is applied to the scene
+// (specialised kernels recompiled for it), timed over `repeats` frames with CUDA events, and the
+// fastest is kept as the scene's own tuning.
+int mm3e_scene_autotune(mm3e_scene* s, const mm3e_camera* camera, int spec_mode, const mm3e_tuning* candidates,
+                        uint32_t n_candidates, uint32_t repeats, mm3e_tuning* best, mm3e_tune_entry* report,
+                        uint32_t report_cap, uint32_t* n_report) {
+    if (!s || !camera || (n_candidates && !candidates)) return MM3E_ERR_INVALID;
+    mm3e_ctx* c = s->ctx;
+    if (spec_mode < 0 || spec_mode > 2) return fail(c, MM3E_ERR_INVALID, "spec_mode must be 0, 1 or 2");
+    static const mm3e_tuning builtin[] = {{128, 3, 1, 0}, {128, 3, 1, 6}, {128, 3, 1, 8},
+                                          {256, 3, 1, 0}, {256, 3, 1, 4}, {256, 4, 1, 0}};
+    if (!n_candidates) {
+        candidates = builtin;
+        n_candidates = (uint32_t)(sizeof(builtin) / sizeof(builtin[0]));
+    }
+    for (uint32_t k = 0; k < n_candidates; ++k) {
+        const mm3e_tuning& t = candidates[k];
+        if ((t.block != 128 && t.block != 256) || t.tile_wlog > 5 || (t.unroll != 1 && t.unroll != 2) || t.min_blocks > 16)
+            return fail(c, MM3E_ERR_INVALID, "autotune candidate out of range (block 128/256, tile 0..5, unroll 1/2, min_blocks 0..16)");
+    }
+    if (repeats == 0) repeats = 5;
+    if (n_report) *n_report = 0;
+    cudaSetDevice(c->device);
+    const bool had = s->own_tune;
+    const TuneParams keep = s->tune;
+    double best_ms = INFINITY;
+    uint32_t best_k = 0;
+    for (uint32_t k = 0; k < n_candidates; ++k) {
+        const mm3e_tuning& t = candidates[k];
+        s->tune = TuneParams{t.block, t.tile_wlog, t.unroll, t.min_blocks};
+        s->own_tune = true;
+        int rc = mm3e_scene_specialize(s, spec_mode, nullptr);
+        if (rc == MM3E_OK) rc = ensure_frame_buffers(s, true);
+        std::vector<float> ms;
+        for (uint32_t r = 0; rc == MM3E_OK && r < repeats + 2; ++r) {
+            LaunchLog log;
+            cudaEventRecord(c->ev0, c->stream);
+            rc = render_to_device(s, camera, nullptr, 0, MM3E_FB_RGBA8, (void*)s->d_out, false, &log);
+            cudaEventRecord(c->ev1, c->stream);
+            if (rc == MM3E_OK) rc = check_status(s);
+            float f = 0.0f;
+            if (rc == MM3E_OK && cudaEventElapsedTime(&f, c->ev0, c->ev1) == cudaSuccess && r >= 2) ms.push_back(f);
+        }
+        if (rc != MM3E_OK) {
+            s->tune = keep;
+            s->own_tune = had;
+            mm3e_scene_specialize(s, spec_mode, nullptr);
+            return rc;
+        }
+        std::sort(ms.begin(), ms.end());
+        double med = ms.empty() ? INFINITY : ms[ms.size() / 2];
+        if (report && k < report_cap) {
+            report[k].tuning = t;
+            report[k].device_ms = med;
+            if (n_report) *n_report = k + 1;
+        }
+        if (med < best_ms) {
+            best_ms = med;
+            best_k = k;
+        }
+    }
+    const mm3e_tuning& b = candidates[best_k];
+    s->tune = TuneParams{b.block, b.tile_wlog, b.unroll, b.min_blocks};
+    s->own_tune = true;
+    if (best) *best = b;
+    return mm3e_scene_specialize(s, spec_mode, nullptr);
+}
 
 int mm3e_scene_spec_source(const mm3e_scene_desc* desc, char* out, size_t cap, size_t* len) {
     if (!desc) return MM3E_ERR_INVALID;
@@ -1035,7 +1105,7 @@ int mm3e_render_film(mm3e_scene* s, const mm3e_camera* camera, float aperture_ra
     p.film = true;
     p.job0.lens_radius = aperture_radius;
     p.job0.focus_distance = focus_distance;
-    CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, &log));
+    CK(run_beauty(p, s->buf, s->tuning(), c->stream, c->sm_count, &log));
     std::vector<float4> hdr(n), fg(n), hn(n), qd(n);
     std::vector<uint2> hm(n);
     CK(cudaMemcpyAsync(hdr.data(), s->buf.hdr, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
@@ -1102,7 +1172,7 @@ int mm3e_render_gbuffer(mm3e_scene* s, const mm3e_camera* camera, const float* m
     p.post = false;
     if (n_movers)
         CK(cudaMemcpyAsync(pv.mover, movers4, n_movers * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-    CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, &log));
+    CK(run_beauty(p, s->buf, s->tuning(), c->stream, c->sm_count, &log));
     WaveArgs a{};
     a.job0 = p.job0;
     a.tile_wlog = s->buf_wlog;
@@ -1160,7 +1230,7 @@ int mm3e_reproject(mm3e_ctx* c, uint32_t w, uint32_t h, const mm3e_camera* prev_
     p.n_samples = (uint32_t)n;  // capacity: every pixel a hole
     p.spec = s->spec_kernels();
     p.post = false;
-    CK(run_beauty(p, s->buf, c->tune, c->stream, c->sm_count, &log));
+    CK(run_beauty(p, s->buf, s->tuning(), c->stream, c->sm_count, &log));
     WaveArgs a{};
     a.job0 = p.job0;
     a.cap = (uint32_t)s->buf.cap;

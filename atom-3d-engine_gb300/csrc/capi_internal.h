@@ -82,6 +82,9 @@ struct mm3e_scene {
     mm3e::PassBuffers buf;                // frame ray queues, hit records, HDR / bloom, counters
     uint32_t buf_wlog = 3;                // tile shape the buffers were sized for
     std::unique_ptr<mm3e::SpecModule> spec;  // scene-specialised kernels (NVRTC), when built
+    mm3e::TuneParams tune;                // this scene's launch shape (mm3e_scene_autotune) ...
+    bool own_tune = false;                // ... used instead of the context's when set
+    const mm3e::TuneParams& tuning() const { return own_tune ? tune : ctx->tune; }
     const mm3e::SpecKernels* spec_kernels() const;
     ~mm3e_scene();
     uint32_t n_lights() const;

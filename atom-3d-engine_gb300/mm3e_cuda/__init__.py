@@ -304,6 +304,23 @@ class CompiledScene:
                                               out["material_ids"].ctypes.data_as(P(C.c_uint32))))
         return out
 
+    def autotune(self, camera, spec_mode=1, candidates=None, repeats=5):
+        """mm3e_scene_autotune: the fastest launch shape for this scene's frames at `camera` becomes
+        the scene's own; returns (best tuning dict, [(tuning dict, median ms)])."""
+        cand = None
+        n = 0
+        if candidates:
+            cand = (abi.Tuning * len(candidates))(*[abi.Tuning(c["block"], c["tile_wlog"], c["unroll"],
+                                                               c.get("min_blocks", 0)) for c in candidates])
+            n = len(candidates)
+        best = abi.Tuning()
+        rep = (abi.TuneEntry * 64)()
+        nr = C.c_uint32()
+        self.ctx.check(lib().mm3e_scene_autotune(self._ptr, C.byref(camera), spec_mode, cand, n, repeats, C.byref(best),
+                                                 rep, 64, C.byref(nr)))
+        as_dict = lambda t: {"block": t.block, "tile_wlog": t.tile_wlog, "unroll": t.unroll, "min_blocks": t.min_blocks}
+        return as_dict(best), [(as_dict(rep[i].tuning), rep[i].device_ms) for i in range(nr.value)]
+
     def render_gbuffer(self, camera, movers=()):
         """render_gbuffer (lib.rs:951): a GFrame dict — color (h, w, 4) u8, depth (h, w) f32 (+inf on
         a miss), obj (h, w) i32 (-1: no mover), camera. `movers`: (centre xyz, radius) per mover."""

@@ -102,6 +102,8 @@ def _declare_extra(lib):
                                              P(C.c_size_t), C.c_char_p, C.c_size_t]),
         "mm3e_volume_write_sdfv": (C.c_int, [P(abi.Volume), P(C.c_uint8), C.c_size_t, P(C.c_size_t), C.c_char_p,
                                              C.c_size_t]),
+        "mm3e_scene_autotune": (C.c_int, [C.c_void_p, P(abi.Camera), C.c_int, P(abi.Tuning), C.c_uint32, C.c_uint32,
+                                          P(abi.Tuning), P(abi.TuneEntry), C.c_uint32, P(C.c_uint32)]),
         "mm3e_autotune": (C.c_int, [C.c_void_p, P(abi.Job), C.c_size_t, C.c_uint32, P(abi.Tuning),
                                     P(abi.TuneEntry), C.c_uint32, P(C.c_uint32)]),
     }

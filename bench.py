@@ -493,8 +493,15 @@ def run_ours(args):
         frame()
     interp_ms = timed(frame, max(3, args.steps // 2))
     spec_compile_ms = None
+    tuning = None
     if not args.no_spec:
         spec_compile_ms = compiled.specialize(compiled.SPEC_AUTO)
+        # the library's own launch-shape search for this scene (specialised kernels recompiled
+        # per candidate), before the timed region
+        t0 = time.perf_counter()
+        best, table = compiled.autotune(cam, spec_mode=compiled.SPEC_AUTO)
+        tuning = {"best": best, "table": [[t, round(ms, 3)] for t, ms in table],
+                  "search_s": round(time.perf_counter() - t0, 2)}
     specialized = compiled.specialized
     for _ in range(max(3, args.warmup)):
         frame()
@@ -581,7 +588,7 @@ def run_ours(args):
                    "max_steps": scene.marcher.max_steps, "parallelism": f"replicas x{world}",
                    "l2": "flushed between timed frames (256 MB write)",
                    "field": "scene-specialised (NVRTC)" if specialized else "tape interpreter",
-                   "spec_compile_ms": spec_compile_ms},
+                   "spec_compile_ms": spec_compile_ms, "launch_tuning": tuning},
         "interpreter": {"frames_per_s": 1000.0 / statistics.median(interp_ms),
                         "frame_ms_median": statistics.median(interp_ms)},
         "mrays_per_s": mrays, "frame_ms": {"min": min(frame_ms), "median": statistics.median(frame_ms),

@@ -511,6 +511,15 @@ typedef struct mm3e_tune_entry {
 } mm3e_tune_entry;
 int mm3e_autotune(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, uint32_t repeats, mm3e_tuning* best,
                   mm3e_tune_entry* report, uint32_t report_cap, uint32_t* n_report);
+/* Launch-shape autotuning of one scene's plain frames (no reference counterpart: the tuning is
+ * this library's). Each candidate (NULL / 0: a built-in set of block 128/256, tile and register
+ * budgets) is applied to the scene, the scene re-specialised as `spec_mode` asks
+ * (mm3e_scene_specialize modes), and `repeats` frames at `camera` timed with CUDA events (median);
+ * the fastest becomes the scene's own tuning, used by its later frames instead of the context's,
+ * and the scene is left specialised with it. Frames do not depend on the tuning. Blocking. */
+int mm3e_scene_autotune(mm3e_scene* scene, const mm3e_camera* camera, int spec_mode, const mm3e_tuning* candidates,
+                        uint32_t n_candidates, uint32_t repeats, mm3e_tuning* best, mm3e_tune_entry* report,
+                        uint32_t report_cap, uint32_t* n_report);
 
 /* ---- served form ----------------------------------------------------------------------------- */
 /* A request loop with continuous batching: client threads submit requests, one worker thread

@@ -62,3 +62,20 @@ def test_auto_mode_keeps_the_interpreter_for_large_fields(gpu_ctx):
     cs2 = mm3e_cuda.CompiledScene(gpu_ctx, small)
     cs2.specialize(cs2.SPEC_AUTO)
     assert cs2.specialized
+
+
+def test_scene_autotune_keeps_frames(gpu_ctx):
+    """mm3e_scene_autotune times candidate launch shapes and keeps the fastest as the scene's own;
+    frames are identical under every shape."""
+    scene, cam = scenes.gallery_scene(192, 108)
+    cs = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    ref = cs.render(cam, fmt=abi.FB_RGBA8)
+    cands = [{"block": 128, "tile_wlog": 3, "unroll": 1, "min_blocks": 0},
+             {"block": 256, "tile_wlog": 4, "unroll": 1, "min_blocks": 0},
+             {"block": 128, "tile_wlog": 2, "unroll": 2, "min_blocks": 8}]
+    best, table = cs.autotune(cam, spec_mode=cs.SPEC_ALWAYS, candidates=cands, repeats=2)
+    print("autotune", best, table)
+    assert len(table) == 3 and best in [t for t, _ in table]
+    assert cs.specialized
+    assert np.array_equal(cs.render(cam, fmt=abi.FB_RGBA8), ref)
+    assert gpu_ctx.get_tuning()["block"] == 128  # the context's own tuning is untouched
