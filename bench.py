@@ -80,6 +80,8 @@ def parse():
                     help="cap on requests per rate (the arrival window shrinks to fit)")
     ap.add_argument("--no-forms", action="store_true", help="skip the Cornell / batched / served measurements")
     ap.add_argument("--no-spec", action="store_true", help="time the tape interpreter (no NVRTC specialisation)")
+    ap.add_argument("--tuning", default=None,
+                    help="block,tile_wlog,unroll,min_blocks launch shape for the workload scene instead of the search")
     return ap.parse_args()
 
 
@@ -317,6 +319,11 @@ def bench_served(ctx_factory, seconds, max_requests, rates=(200, 1000, 5000), se
             "arrival_window_s": seconds, "max_requests_per_rate": max_requests, "by_rate": results}
 
 
+def _tuning(text):
+    b, t, u, m = (int(v) for v in text.split(","))
+    return {"block": b, "tile_wlog": t, "unroll": u, "min_blocks": m}
+
+
 def run_profile_frames(args):
     """Renders N frames of the workload through mm3e_render_device and exits (for ncu)."""
     import torch
@@ -330,6 +337,9 @@ def run_profile_frames(args):
     compiled = mm3e_cuda.CompiledScene(ctx, scene)
     if not args.no_spec:
         compiled.specialize(compiled.SPEC_AUTO)
+    if args.tuning:
+        compiled.autotune(cam, spec_mode=0 if args.no_spec else compiled.SPEC_AUTO, candidates=[_tuning(args.tuning)],
+                          repeats=1)
     out = torch.empty(scene.width * scene.height * 4, dtype=torch.uint8, device="cuda")
     for _ in range(args.profile_frames):
         compiled.render_device(cam, abi.FB_RGBA8, out.data_ptr(), out.numel())
@@ -499,7 +509,8 @@ def run_ours(args):
         # the library's own launch-shape search for this scene (specialised kernels recompiled
         # per candidate), before the timed region
         t0 = time.perf_counter()
-        best, table = compiled.autotune(cam, spec_mode=compiled.SPEC_AUTO)
+        best, table = compiled.autotune(cam, spec_mode=compiled.SPEC_AUTO,
+                                        candidates=[_tuning(args.tuning)] if args.tuning else None)
         tuning = {"best": best, "table": [[t, round(ms, 3)] for t, ms in table],
                   "search_s": round(time.perf_counter() - t0, 2)}
     specialized = compiled.specialized
