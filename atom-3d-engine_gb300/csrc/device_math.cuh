@@ -162,6 +162,18 @@ MD bool far_beyond(float d2, float bd, float r) {
     return bd >= 0.0f && d2 > q * q * 1.00006103515625f;
 }
 
+// Weak-bound cull of a union member whose exact sphere test does not apply (an unbounded
+// object, or one whose field can undercut its sphere): with l its local point, the field is at
+// least c * (n - R) * scale - post, n the norm of l over the axes that do not repeat (the
+// generator derives R, c and post per object). True only when that bound clears bd >= 0 by a
+// relative margin of 2^-10, far beyond the rounding of either side; such a member cannot win.
+MD bool weak_beyond(V l, bool ax, bool ay, bool az, float R, float c, float scl, float post, float bd) {
+    float n2 = (ax ? l.x * l.x : 0.0f) + (ay ? l.y * l.y : 0.0f) + (az ? l.z * l.z : 0.0f);
+    float n = sqrtf(n2);
+    float lb = (n - R) * c * scl - post;
+    return bd >= 0.0f && lb - (n + R) * scl * 0.0009765625f > bd;
+}
+
 // ---- tape view ----
 struct Tape {
     const TapeHeader* h;

@@ -654,7 +654,11 @@ int lower_scene(const mm3e_scene_desc& d0, const mm3e_dyn_sphere* dyn, size_t n_
         if (o.round != 0.0f) f |= OF_ROUND;
         if (o.onion != 0.0f) f |= OF_ONION;
         if (has_bound[i]) f |= OF_BOUND;
-        if (o.prim == MM3E_PRIM_ELLIPSOID || o.prim == MM3E_PRIM_OCTAHEDRON) f |= OF_NONCONS;
+        // Fields that can lie below their bounding sphere's distance: the ellipsoid and octahedron
+        // bound fields, and the hexagonal prism, whose Prim::local_bound radius (lib.rs:264-292)
+        // takes the hexagon's apothem where its corners reach 2/sqrt(3) times as far.
+        if (o.prim == MM3E_PRIM_ELLIPSOID || o.prim == MM3E_PRIM_OCTAHEDRON || o.prim == MM3E_PRIM_HEX_PRISM)
+            f |= OF_NONCONS;
         f |= (o.combine & 3u) << 16;  // combine mode, read by the dual-number normal
         g.flags = f;
         g.aux = o.prim == MM3E_PRIM_CSG ? csg_offset[o.id] : (d.n_volumes ? o.id % d.n_volumes : 0);

@@ -104,6 +104,89 @@ std::string object_fn(uint32_t i, const DevObject& o) {
     return os.str();
 }
 
+// A lower bound of an object's field that holds wherever it is positive: with l the local point
+// (rotation and 1/scale applied; before mirror, elongate, repeat, twist and bend),
+//   field(p) >= c * (n - R) * scale - post,   n = |l| over the axes that do not repeat,
+// because mirror, twist and bend preserve |l|, elongate by h moves it by at most |h| (added to
+// R), a periodic axis can only lower the norm the primitive sees, and each primitive's field is
+// at least c * (|q| - R) outside the ball of radius R about its local origin: c = 1 for the
+// exact distances, 0.577 for the octahedron's bound field ((|x|+|y|+|z| - s) * 0.5773503 with
+// |x|+|y|+|z| >= |q|), r_min / r_max for the ellipsoid's (k0 (k0 - 1) / k1 with k1 <= k0 / r_min
+// and k0 >= |q| / r_max). post = round (any sign) + onion (>= 0 only).
+struct WeakBound {
+    bool ok = false;
+    float R = 0.0f, c = 0.0f, post = 0.0f;
+    bool axis[3] = {true, true, true};
+};
+
+WeakBound weak_bound(const DevObject& o) {
+    WeakBound w;
+    const float* q = o.params;
+    double R = 0.0, c = 0.999;
+    switch (o.prim) {
+        case 0: R = q[0]; break;
+        case 1:
+        case 2: R = std::sqrt((double)q[0] * q[0] + (double)q[1] * q[1] + (double)q[2] * q[2]); break;
+        case 3: R = (double)q[0] + q[1]; break;
+        case 4: R = std::sqrt((double)q[0] * q[0] + (double)q[1] * q[1]); break;
+        case 5: {
+            double a = std::sqrt((double)q[0] * q[0] + (double)q[1] * q[1] + (double)q[2] * q[2]);
+            double b = std::sqrt((double)q[3] * q[3] + (double)q[4] * q[4] + (double)q[5] * q[5]);
+            R = std::max(a, b) + q[6];
+            break;
+        }
+        case 6: R = std::max((double)q[0], (double)q[2] + q[1]); break;
+        case 7: {
+            double rmax = std::max(std::max(q[0], q[1]), q[2]), rmin = std::min(std::min(q[0], q[1]), q[2]);
+            if (!(rmin > 0.0)) return w;
+            R = rmax;
+            c = 0.999 * rmin / rmax;
+            break;
+        }
+        case 8: R = q[0]; c = 0.577; break;
+        case 9: {
+            double circ = 2.0 * q[0] / std::sqrt(3.0);
+            R = std::sqrt(circ * circ + (double)q[1] * q[1]);
+            break;
+        }
+        default: return w;  // plane, CSG, volume
+    }
+    if (!(R >= 0.0) || !std::isfinite(R)) return w;
+    if (o.flags & OF_ELONGATE)
+        R += std::sqrt((double)o.elongate[0] * o.elongate[0] + (double)o.elongate[1] * o.elongate[1] +
+                       (double)o.elongate[2] * o.elongate[2]);
+    int kept = 3;
+    if (o.flags & OF_REPEAT)
+        for (int a = 0; a < 3; ++a)
+            if (o.repeat[a] > 0.0f) {
+                w.axis[a] = false;
+                kept -= 1;
+            }
+    if (kept == 0) return w;
+    double post = 0.0;
+    if (o.flags & OF_ROUND) post += o.round;
+    if (o.flags & OF_ONION) {
+        if (!(o.onion >= 0.0f)) return w;
+        post += o.onion;
+    }
+    R = R * (1.0 + 1.0 / 4096.0) + 1e-6;
+    w.R = (float)R;
+    w.c = (float)c;
+    w.post = (float)(post + std::fabs(post) / 4096.0 + 1e-6);
+    w.ok = std::isfinite(w.R) && std::isfinite(w.post) && o.scale > 0.0f;
+    return w;
+}
+
+// The weak-bound cull of a member: true when its field cannot reach down to bd.
+std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
+    std::ostringstream os;
+    os << "weak_beyond(scale(rot_t(RO, p - V{" << fbits(o.pos[0]) << ", " << fbits(o.pos[1]) << ", " << fbits(o.pos[2])
+       << "}), " << fbits(o.inv) << "), " << (w.axis[0] ? "true" : "false") << ", " << (w.axis[1] ? "true" : "false")
+       << ", " << (w.axis[2] ? "true" : "false") << ", " << fbits(w.R) << ", " << fbits(w.c) << ", " << fbits(o.scale)
+       << ", " << fbits(w.post) << ", bd)";
+    return os.str();
+}
+
 std::string lower_expr(const DevObject& o) {
     return "length(p - V{" + fbits(o.bc[0]) + ", " + fbits(o.bc[1]) + ", " + fbits(o.bc[2]) + "}) - " + fbits(o.br);
 }
@@ -251,6 +334,13 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                                     undercut + ";\n            }\n";
                 any_noncons = any_noncons || nc_bounded;
                 os << "        {  // member " << i << "\n";
+                // members the exact sphere test never culls (the reference's unbounded members, and
+                // the non-conservative ones) skip their exact field where their weak bound clears bd
+                const WeakBound wb = cull ? WeakBound{} : weak_bound(o);
+                if (wb.ok) {
+                    os << "            const float RO[9] = " << farr(o.rot, 9) << ";\n";
+                    exact = "if (!" + weak_cull_expr(o, wb) + ") {\n            " + exact + "            }\n";
+                }
                 if (o.flags & OF_BOUND) {
                     if (cull) {
                         os << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])

@@ -35,7 +35,7 @@ enum : uint32_t {
     OF_ROUND = 1u << 7,
     OF_ONION = 1u << 8,
     OF_BOUND = 1u << 9,
-    OF_NONCONS = 1u << 10,  // ellipsoid / octahedron: field can undercut the bounding sphere
+    OF_NONCONS = 1u << 10,  // ellipsoid / octahedron / hex prism: field can undercut the bounding sphere
     OF_ANY_MIRROR = OF_MIRROR_X | OF_MIRROR_Y | OF_MIRROR_Z,
     OF_POINT_OPS = OF_ANY_MIRROR | OF_ELONGATE | OF_REPEAT | OF_TWIST | OF_BEND,
 };
@@ -80,8 +80,8 @@ enum : uint32_t { SEG_ONE = 0, SEG_RUN = 1, SEG_LINEAR = 2 };
 //   fallback. A linear fold of every member with the reference's (distance, object index)
 //   rule gives the BVH query's result whenever the winner's field is not below its bounding
 //   sphere's distance (a subtree the BVH prunes can then never hold the minimum); the only
-//   members whose fields can undercut their spheres are exactly-evaluated ellipsoids and
-//   octahedra (OF_NONCONS), and a lane whose linear winner is one of those, at a point where
+//   members whose fields can undercut their spheres are exactly-evaluated ellipsoids,
+//   octahedra and hexagonal prisms (OF_NONCONS), and a lane whose linear winner is one of those, at a point where
 //   its field is not clear of its sphere's bound, re-runs the BVH walk. The linear fold is
 //   warp-uniform.
 struct alignas(16) DevSegment {
