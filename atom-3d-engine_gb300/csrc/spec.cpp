@@ -360,10 +360,14 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 }
                 os << "        }\n";
             };
+            // order: members that are always evaluated (they set an early best), the sphere-tested
+            // clusters, then the weak-bound members, whose looser bound needs the smallest best
+            std::vector<uint32_t> weak;
             for (uint32_t k = 0; k < sg.b; ++k) {
                 uint32_t i = unb[sg.a + k];
                 bool cull = (obj[i].flags & OF_BOUND) && !(obj[i].flags & OF_NONCONS);
                 if (cull) cullable.push_back(i);
+                else if (weak_bound(obj[i]).ok) weak.push_back(i);
                 else member(i, false);
             }
             std::vector<MemberCluster> clusters;
@@ -376,6 +380,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 for (uint32_t i : cl.members) member(i, true);
                 if (cl.members.size() > 1) os << "        }  // end of cluster\n";
             }
+            for (uint32_t i : weak) member(i, false);
             if (any_noncons)
                 os << "        if (bnc) acc = bvh_segment(T, " << s << "u, p, " << (seeded ? "true" : "false")
                    << ", acc);\n        else acc = Field{bd, bm};\n";
