@@ -284,6 +284,16 @@ def hero_scene(width=960, height=540, aa=2, bounces=2):
     return s, cam
 
 
+def gpu_render_scene(width=960, height=540, yaw=0.55):
+    """mm3e-gpu/examples/gpu_render.rs:11-49 (and gpu_resolution.rs): the hero scene at aa 2 with 3
+    bounces and a soft sun (radius 0.04), the scene of the reference's published GPU frame rates;
+    orbit camera at `yaw` (the benchmark loop turns it by 0.01 per frame from 0.55)."""
+    s, _ = hero_scene(width, height, 2, 3)
+    s.lights[0] = s.lights[0].soft(0.04)
+    cam = orbit_camera((0.2, 0.85, 0.4), 8.5, yaw, 0.32, radians(50.0))
+    return s, cam
+
+
 def demo_scene():
     """mm3e-orchestrator/tests/engine.rs:11-27 with its camera (engine.rs:29-31)."""
     s = Scene(96, 64)

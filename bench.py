@@ -184,6 +184,64 @@ def bench_preview(ctx, torch, with_cpu):
     return out
 
 
+# The reference's published GPU numbers for its own benchmark scene (mm3e-gpu examples, RTX 5070 Ti
+# over wgpu; README.md:15 and CHANGELOG.md:75-76), quoted beside ours on the same scene and loop.
+PUBLISHED_GPU_RENDER_FPS = 698.9
+PUBLISHED_RESOLUTION_FPS = {"960x540": 606.0, "1920x1080": 167.0, "2560x1440": 96.0, "3840x2160": 43.0}
+
+
+def bench_published(ctx, stream, torch):
+    """The reference's own GPU benchmarks re-run here: gpu_render.rs (960x540, aa 2, 3 bounces,
+    120 frames of an orbiting camera, each rendered and read back as RGBA8: e2e through
+    mm3e_render into one host framebuffer) and gpu_resolution.rs (the same scene at 540p to 4K,
+    render only: device time per frame with CUDA events)."""
+    import numpy as np
+
+    from mm3e_cuda import abi, scenes
+
+    import mm3e_cuda
+
+    s, cam = scenes.gpu_render_scene(960, 540)
+    cs = mm3e_cuda.CompiledScene(ctx, s)
+    best, _ = cs.autotune(cam, spec_mode=cs.SPEC_AUTO)
+    host = np.zeros((s.height, s.width, 4), np.uint8)
+    cams = [scenes.gpu_render_scene(960, 540, 0.55 + i * 0.01)[1] for i in range(120)]
+    for c in cams[:5]:
+        cs.render(c, fmt=abi.FB_RGBA8, out=host)
+    t0 = time.perf_counter()
+    for c in cams:
+        cs.render(c, fmt=abi.FB_RGBA8, out=host)
+    loop_s = time.perf_counter() - t0
+    cs.close()
+    out = {"scene": "mm3e-gpu gpu_render.rs: hero scene, aa 2, 3 bounces, soft sun", "tuning": best,
+           "gpu_render_960x540": {"frames_per_s": 120 / loop_s, "frames": 120,
+                                  "timing": "host wall of the 120-frame orbit loop, render + RGBA8 readback per frame",
+                                  "reference_published_fps": PUBLISHED_GPU_RENDER_FPS,
+                                  "reference_hardware": "RTX 5070 Ti, wgpu (README.md:15)"}}
+    sweep = {}
+    for key in PUBLISHED_RESOLUTION_FPS:
+        w, h = (int(v) for v in key.split("x"))
+        s, cam = scenes.gpu_render_scene(w, h)
+        cs = mm3e_cuda.CompiledScene(ctx, s)
+        cs.autotune(cam, spec_mode=cs.SPEC_AUTO, candidates=[best], repeats=1)
+        dev = torch.empty(w * h * 4, dtype=torch.uint8, device="cuda")
+        for _ in range(3):
+            cs.render_device(cam, abi.FB_RGBA8, dev.data_ptr(), dev.numel())
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        with torch.cuda.stream(stream):
+            for a, b in ev:
+                a.record(stream)
+                cs.render_device(cam, abi.FB_RGBA8, dev.data_ptr(), dev.numel())
+                b.record(stream)
+        stream.synchronize()
+        ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+        sweep[key] = {"frames_per_s": 1000.0 / ms, "reference_published_fps": PUBLISHED_RESOLUTION_FPS[key]}
+        cs.close()
+    out["gpu_resolution_render_only"] = sweep
+    out["gpu_resolution_note"] = "reference: RTX 5070 Ti, wgpu, render-only (CHANGELOG.md:75-76)"
+    return out
+
+
 def bench_batched(ctx, stream, torch, n_scenes):
     """Batched form: n seeded procedural scenes (8-64 primitives, random CSG, mixed resolutions
     256^2 / 512^2 / 1280x720 / 1920x1080, orbit cameras) rendered as one batch (autotuned launch
@@ -617,6 +675,7 @@ def run_ours(args):
         line["cornell"] = bench_cornell(ctx, stream, torch)
         line["batched"] = bench_batched(ctx, stream, torch, args.batch_scenes)
         line["preview"] = bench_preview(ctx, torch, not args.no_cpu)
+        line["published_scene"] = bench_published(ctx, stream, torch)
         ctx.set_stream(None)
         line["served"] = bench_served(lambda: mm3e_cuda.Context(local), args.served_seconds, args.served_max_requests)
     print(json.dumps(line))

@@ -57,6 +57,7 @@ SCENES = {
     "hero_aa2_b2": lambda: scenes.hero_scene(240, 135, 2, 2),
     "demo": scenes.demo_scene,
     "canonical_assets": scenes.canonical_asset_scene,
+    "gpu_render_aa2_b3": lambda: scenes.gpu_render_scene(240, 135),
 }
 
 
