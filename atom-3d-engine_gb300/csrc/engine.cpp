@@ -12,18 +12,22 @@ template <class T> cudaError_t grow(T** p, size_t n) {
 }  // namespace
 
 void PassBuffers::release() {
-    void* ps[] = {qa_o, qa_d, qb_o, qb_d, qc_o, qc_d, h_n, h_m, occ, shadow, h_n1, h_m1, occ1, shadow1,
-                  lvl, term, hdr, bright, blur, counters};
+    void* ps[] = {qa_o, qa_d, qb_o, qb_d, qc_o, qc_d, qd_o, qd_d, h_n, h_m, occ, shadow, h_n1, h_m1, occ1, shadow1,
+                  h_n2, h_m2, occ2, shadow2, lvl, term, hdr, bright, blur, counters};
     for (void* p : ps) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
+    for (int i = 0; i < MAX_LEVELS; ++i) {
+        if (ev_marched[i]) cudaEventDestroy(ev_marched[i]);
+        if (ev_shaded[i]) cudaEventDestroy(ev_shaded[i]);
+    }
     if (aux) cudaStreamDestroy(aux);
+    if (aux2) cudaStreamDestroy(aux2);
     *this = PassBuffers();
 }
 
 size_t PassBuffers::bytes_for(size_t cap, size_t lights, size_t levels, size_t pixels) {
     size_t l = lights ? lights : 1, v = levels ? levels : 1;
-    size_t queues = v >= 3 ? 6 : 4, hit_sets = v >= 2 ? 2 : 1;
+    size_t queues = v >= 4 ? 8 : (v >= 3 ? 6 : 4), hit_sets = v >= 3 ? 3 : (v >= 2 ? 2 : 1);
     return cap * (queues * sizeof(float4) + hit_sets * (sizeof(float4) + sizeof(uint2) + sizeof(float) +
                                                          l * sizeof(float)) +
                   2 * v * sizeof(float4) + sizeof(float4)) +
@@ -52,12 +56,23 @@ cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need
     if (v >= 2 && ((e = grow(&h_n1, c)) || (e = grow(&h_m1, c)) || (e = grow(&occ1, c)) ||
                    (e = grow(&shadow1, c * (l ? l : 1))) ||
                    (e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) ||
-                   (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)) ||
-                   (e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming)))) {
+                   (e = cudaStreamCreateWithFlags(&aux2, cudaStreamNonBlocking)) ||
+                   (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)))) {
         release();
         return e;
     }
-    if (v >= 3 && ((e = grow(&qc_o, c)) || (e = grow(&qc_d, c)))) {
+    for (size_t i = 1; i < v && i < (size_t)MAX_LEVELS; ++i)
+        if ((e = cudaEventCreateWithFlags(&ev_marched[i], cudaEventDisableTiming)) ||
+            (e = cudaEventCreateWithFlags(&ev_shaded[i], cudaEventDisableTiming))) {
+            release();
+            return e;
+        }
+    if (v >= 3 && ((e = grow(&qc_o, c)) || (e = grow(&qc_d, c)) || (e = grow(&h_n2, c)) || (e = grow(&h_m2, c)) ||
+                   (e = grow(&occ2, c)) || (e = grow(&shadow2, c * (l ? l : 1))))) {
+        release();
+        return e;
+    }
+    if (v >= 4 && ((e = grow(&qd_o, c)) || (e = grow(&qd_d, c)))) {
         release();
         return e;
     }
@@ -250,7 +265,7 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
     if (levels <= 1) {
         if ((e = level_passes(plan, a, buf, tune, s, sm_count, log, 0, false)) != cudaSuccess) return e;
     } else {
-        // primary level on `s`; its reflection rays fork the deeper levels onto the aux stream
+        // primary level on `s`; its reflection rays fork the deeper levels onto the aux streams
         WaveArgs a0 = a;
         a0.b.nq_o = buf.qb_o;
         a0.b.nq_d = buf.qb_d;
@@ -264,21 +279,42 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
         if ((e = launch_reflect(a0, s, log)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(buf.ev_fork, s)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(buf.aux, buf.ev_fork, 0)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(buf.aux2, buf.ev_fork, 0)) != cudaSuccess) return e;
+        float4* q_o[3] = {buf.qb_o, buf.qc_o, buf.qd_o};
+        float4* q_d[3] = {buf.qb_d, buf.qc_d, buf.qd_d};
         for (uint32_t level = 1; level < levels; ++level) {
             WaveArgs ak = a;
-            bool odd = (level & 1u) != 0;
-            ak.b.q_o = odd ? buf.qb_o : buf.qc_o;
-            ak.b.q_d = odd ? buf.qb_d : buf.qc_d;
-            ak.b.nq_o = odd ? buf.qc_o : buf.qb_o;
-            ak.b.nq_d = odd ? buf.qc_d : buf.qb_d;
-            ak.b.h_n = buf.h_n1;
-            ak.b.h_m = buf.h_m1;
-            ak.b.occ = buf.occ1;
-            ak.b.shadow = buf.shadow1;
-            if ((e = level_passes(plan, ak, buf, tune, buf.aux, sm_count, log, level, level + 1 < levels)) != cudaSuccess)
-                return e;
+            const uint32_t qi = (level - 1) % 3, ni = level % 3;
+            const bool odd = (level & 1u) != 0;
+            ak.b.q_o = q_o[qi];
+            ak.b.q_d = q_d[qi];
+            ak.b.nq_o = q_o[ni];
+            ak.b.nq_d = q_d[ni];
+            ak.b.h_n = odd ? buf.h_n1 : buf.h_n2;
+            ak.b.h_m = odd ? buf.h_m1 : buf.h_m2;
+            ak.b.occ = odd ? buf.occ1 : buf.occ2;
+            ak.b.shadow = odd ? buf.shadow1 : buf.shadow2;
+            ak.level = level;
+            ak.src = SRC_QUEUE;
+            ak.n_items = plan.n_samples;
+            ak.n_items_dev = buf.counters + 4 * (level - 1) + 2;
+            ak.b.nq_count = buf.counters + 4 * level + 2;
+            // this level's hits overwrite those of level - 2, and its reflection rays the queue
+            // level - 2 read: both wait for that level's shading
+            if (level >= 3 && (e = cudaStreamWaitEvent(buf.aux, buf.ev_shaded[level - 2], 0)) != cudaSuccess) return e;
+            ak.counter = buf.counters + 4 * level;
+            if ((e = launch_march(ak, tune, buf.aux, sm_count, log, plan.spec)) != cudaSuccess) return e;
+            if (level + 1 < levels && (e = launch_reflect(ak, buf.aux, log)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(buf.ev_marched[level], buf.aux)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(buf.aux2, buf.ev_marched[level], 0)) != cudaSuccess) return e;
+            if (plan.ao && (e = launch_ao(ak, buf.aux2, log, plan.spec)) != cudaSuccess) return e;
+            if (plan.shadows && plan.lights_max > 0) {
+                ak.counter = buf.counters + 4 * level + 1;
+                if ((e = launch_shadow(ak, tune, buf.aux2, sm_count, log, plan.spec)) != cudaSuccess) return e;
+            }
+            if ((e = launch_shade(ak, buf.aux2, log)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(buf.ev_shaded[level], buf.aux2)) != cudaSuccess) return e;
         }
-        if ((e = cudaEventRecord(buf.ev_join, buf.aux)) != cudaSuccess) return e;
         // the primary level's AO, shadows and shading overlap the reflection levels
         a0.counter = buf.counters;
         if (plan.ao && (e = launch_ao(a0, s, log, plan.spec)) != cudaSuccess) return e;
@@ -287,7 +323,9 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
             if ((e = launch_shadow(a0, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
         }
         if ((e = launch_shade(a0, s, log)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(s, buf.ev_join, 0)) != cudaSuccess) return e;
+        // join: every reflection level's shading (in order on aux2) and the last march (aux)
+        if ((e = cudaStreamWaitEvent(s, buf.ev_shaded[levels - 1], 0)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s, buf.ev_marched[levels - 1], 0)) != cudaSuccess) return e;
     }
     if (plan.queue0) return cudaSuccess;
     if ((e = launch_resolve(a, plan.n_slots, s, log)) != cudaSuccess) return e;
