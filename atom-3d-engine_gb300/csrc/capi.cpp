@@ -583,7 +583,7 @@ int mm3e_ctx_set_tuning(mm3e_ctx* ctx, const mm3e_tuning* t) {
     if (!ctx || !t) return MM3E_ERR_INVALID;
     if (t->block != 128 && t->block != 256) return fail(ctx, MM3E_ERR_INVALID, "block must be 128 or 256");
     if (t->tile_wlog > 5) return fail(ctx, MM3E_ERR_INVALID, "tile_wlog must be 0..5");
-    if (t->unroll != 1 && t->unroll != 2) return fail(ctx, MM3E_ERR_INVALID, "unroll must be 1 or 2");
+    if (t->unroll < 1 || t->unroll > 4) return fail(ctx, MM3E_ERR_INVALID, "unroll must be 1..4");
     if (t->min_blocks > 16) return fail(ctx, MM3E_ERR_INVALID, "min_blocks must be 0..16");
     cudaError_t e = cudaStreamSynchronize(ctx->stream);  // frames in flight keep their buffers
     if (e != cudaSuccess) return cuda_fail(ctx, e, "set tuning");
@@ -999,8 +999,8 @@ int mm3e_scene_autotune(mm3e_scene* s, const mm3e_camera* camera, int spec_mode,
     }
     for (uint32_t k = 0; k < n_candidates; ++k) {
         const mm3e_tuning& t = candidates[k];
-        if ((t.block != 128 && t.block != 256) || t.tile_wlog > 5 || (t.unroll != 1 && t.unroll != 2) || t.min_blocks > 16)
-            return fail(c, MM3E_ERR_INVALID, "autotune candidate out of range (block 128/256, tile 0..5, unroll 1/2, min_blocks 0..16)");
+        if ((t.block != 128 && t.block != 256) || t.tile_wlog > 5 || t.unroll < 1 || t.unroll > 4 || t.min_blocks > 16)
+            return fail(c, MM3E_ERR_INVALID, "autotune candidate out of range (block 128/256, tile 0..5, unroll 1..4, min_blocks 0..16)");
     }
     if (repeats == 0) repeats = 5;
     if (n_report) *n_report = 0;

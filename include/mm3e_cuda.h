@@ -327,7 +327,8 @@ int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
 
 /* Launch shape of the march and soft-shadow passes: threads per CTA (128 or 256), pixel tile
  * of 32 pixels 2^tile_wlog wide (tile_wlog 0..5; 3 = 8x4), and field samples per lane between
- * work refills (unroll 1 or 2); min_blocks (0..16) asks the compiler of scene-specialised
+ * work refills (unroll 1..4; the tape interpreter's kernels take 1 or 2, larger values act as 2);
+ * min_blocks (0..16) asks the compiler of scene-specialised
  * kernels to fit that many CTAs per SM in the register file (0: the compiler's choice for the
  * shadow / AO kernels and 7 CTAs of 128 or 3 of 256 for the march kernel). Results do not depend
  * on it. mm3e_autotune picks block / tile / unroll. */
