@@ -99,55 +99,23 @@ __device__ __forceinline__ bool stage_tape(unsigned char* smem, const unsigned c
     return ok;
 }
 
-// Items a warp has claimed from the pass's work counter and not yet handed out: [next, end),
-// the same in every lane of the warp. `chunk` is the size of the next claim.
-struct WorkRange {
-    uint32_t next, end, chunk;
-};
-
-__device__ __forceinline__ WorkRange work_range(uint32_t n) {
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    uint32_t c = n / (warps * 4u + 1u);
-    return WorkRange{0u, 0u, c < 32u ? 32u : (c > 256u ? 256u : c)};
-}
-
-// Warp-aggregated refill of idle lanes; a lane retires once the items run out. Lanes take
-// items from the warp's claimed range; only when it runs short does one lane claim a new chunk
-// with an atomic on the global counter (guided sizes: about a quarter of the remaining items per
-// warp, 32 to 256), so most refills cost no global round trip.
-__device__ __forceinline__ void refill(uint32_t& item, bool& retired, uint32_t n, uint32_t* counter, bool& fresh,
-                                       WorkRange& wr) {
+// Warp-aggregated refill of idle lanes; a lane retires once the items run out.
+__device__ __forceinline__ void refill(uint32_t& item, bool& retired, uint32_t n, uint32_t* counter, bool& fresh) {
     fresh = false;
     const uint32_t lane = threadIdx.x & 31u;
     unsigned want = __ballot_sync(0xFFFFFFFFu, item == NIL && !retired);
     if (!want) return;
-    const uint32_t cnt = (uint32_t)__popc(want);
-    const uint32_t have = wr.end - wr.next;
-    uint32_t claimed = 0;
-    if (have < cnt) {  // chunk >= 32 >= cnt: the new chunk covers the shortfall
-        int leader = __ffs(want) - 1;
-        if ((int)lane == leader) claimed = atomicAdd(counter, wr.chunk);
-        claimed = __shfl_sync(0xFFFFFFFFu, claimed, leader);
-    }
+    uint32_t base = 0;
+    int leader = __ffs(want) - 1;
+    if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(want));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
     if (item == NIL && !retired) {
-        uint32_t rank = (uint32_t)__popc(want & ((1u << lane) - 1u));
-        uint32_t it = rank < have ? wr.next + rank : claimed + (rank - have);
+        uint32_t it = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
         if (it >= n) retired = true;
         else {
             item = it;
             fresh = true;
         }
-    }
-    if (have >= cnt) {
-        wr.next += cnt;
-    } else {
-        const uint32_t got = wr.chunk;
-        wr.next = claimed + (cnt - have);
-        wr.end = claimed + got;
-        const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-        uint32_t left = n > wr.end ? n - wr.end : 0u;
-        uint32_t c = left / (warps * 4u + 1u);
-        wr.chunk = c < 32u ? 32u : (c > 256u ? 256u : c);
     }
 }
 
@@ -447,10 +415,9 @@ __device__ __forceinline__ void march_body(const WaveArgs& a) {
     L.item = NIL;
     L.phase = M_IDLE;
     bool retired = false;
-    WorkRange wr = work_range(n);
     for (;;) {
         bool fresh;
-        refill(L.item, retired, n, a.counter, fresh, wr);
+        refill(L.item, retired, n, a.counter, fresh);
         if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
         if (fresh && !m_start(L, LT, a)) continue;
 #pragma unroll 1
@@ -580,10 +547,9 @@ __device__ __forceinline__ void shadow_body(const WaveArgs& a) {
     SLane S;
     S.item = NIL;
     bool retired = false;
-    WorkRange wr = work_range(n);
     for (;;) {
         bool fresh;
-        refill(S.item, retired, n, a.counter, fresh, wr);
+        refill(S.item, retired, n, a.counter, fresh);
         if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
         if (fresh && !s_start(S, LT, a)) continue;
 #pragma unroll 1
