@@ -583,7 +583,7 @@ int mm3e_ctx_set_tuning(mm3e_ctx* ctx, const mm3e_tuning* t) {
     if (!ctx || !t) return MM3E_ERR_INVALID;
     if (t->block != 128 && t->block != 256) return fail(ctx, MM3E_ERR_INVALID, "block must be 128 or 256");
     if (t->tile_wlog > 5) return fail(ctx, MM3E_ERR_INVALID, "tile_wlog must be 0..5");
-    if (t->unroll < 1 || t->unroll > 4) return fail(ctx, MM3E_ERR_INVALID, "unroll must be 1..4");
+    if (t->unroll < 1 || t->unroll > 64) return fail(ctx, MM3E_ERR_INVALID, "unroll must be 1..64");
     if (t->min_blocks > 16) return fail(ctx, MM3E_ERR_INVALID, "min_blocks must be 0..16");
     cudaError_t e = cudaStreamSynchronize(ctx->stream);  // frames in flight keep their buffers
     if (e != cudaSuccess) return cuda_fail(ctx, e, "set tuning");
@@ -991,16 +991,16 @@ int mm3e_scene_autotune(mm3e_scene* s, const mm3e_camera* camera, int spec_mode,
     if (!s || !camera || (n_candidates && !candidates)) return MM3E_ERR_INVALID;
     mm3e_ctx* c = s->ctx;
     if (spec_mode < 0 || spec_mode > 2) return fail(c, MM3E_ERR_INVALID, "spec_mode must be 0, 1 or 2");
-    static const mm3e_tuning builtin[] = {{128, 3, 1, 0}, {128, 3, 1, 6}, {128, 3, 1, 8},
-                                          {256, 3, 1, 0}, {256, 3, 1, 4}, {256, 4, 1, 0}};
+    static const mm3e_tuning builtin[] = {{128, 4, 32, 0}, {128, 2, 32, 0}, {128, 3, 32, 0}, {128, 4, 16, 0},
+                                          {256, 4, 32, 0}, {256, 1, 32, 0}, {128, 4, 64, 0}, {128, 2, 64, 0}};
     if (!n_candidates) {
         candidates = builtin;
         n_candidates = (uint32_t)(sizeof(builtin) / sizeof(builtin[0]));
     }
     for (uint32_t k = 0; k < n_candidates; ++k) {
         const mm3e_tuning& t = candidates[k];
-        if ((t.block != 128 && t.block != 256) || t.tile_wlog > 5 || t.unroll < 1 || t.unroll > 4 || t.min_blocks > 16)
-            return fail(c, MM3E_ERR_INVALID, "autotune candidate out of range (block 128/256, tile 0..5, unroll 1..4, min_blocks 0..16)");
+        if ((t.block != 128 && t.block != 256) || t.tile_wlog > 5 || t.unroll < 1 || t.unroll > 64 || t.min_blocks > 16)
+            return fail(c, MM3E_ERR_INVALID, "autotune candidate out of range (block 128/256, tile 0..5, unroll 1..64, min_blocks 0..16)");
     }
     if (repeats == 0) repeats = 5;
     if (n_report) *n_report = 0;

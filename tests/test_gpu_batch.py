@@ -94,7 +94,7 @@ def test_batch_f32_output_and_tile_shapes():
     try:
         items = _mixed(ctx, [(50, 30), (37, 21), (64, 40), (45, 45)])
         refs = [cs.render(cam, fmt=abi.FB_RGBA_F32) for cs, cam, _, _ in items]
-        for block, wlog, unroll in ((128, 3, 1), (256, 2, 2), (128, 4, 2), (256, 5, 1)):
+        for block, wlog, unroll in ((128, 3, 1), (256, 2, 4), (128, 4, 16), (256, 5, 1)):
             ctx.set_tuning(block, wlog, unroll)
             outs = [np.zeros((h, w, 4), np.float32) for _, _, w, h in items]
             jobs = ctx.make_jobs([(cs, cam, 0, 0, abi.FB_RGBA_F32, None, o) for (cs, cam, _, _), o in zip(items, outs)])
