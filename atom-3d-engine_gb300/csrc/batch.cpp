@@ -377,7 +377,7 @@ int mm3e_autotune(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, uint32_t repeat
     cudaSetDevice(ctx->device);
     if (!ctx->batch) ctx->batch.reset(new BatchEngine(ctx));
     TuneParams keep = ctx->tune;
-    const uint32_t blocks[2] = {128, 256}, wlogs[3] = {2, 3, 4}, unrolls[3] = {1, 4, 16};
+    const uint32_t blocks[2] = {128, 256}, wlogs[3] = {2, 3, 4}, unrolls[3] = {1, 16, 64};
     double best_ms = -1.0;
     TuneParams best_t = keep;
     uint32_t k = 0;

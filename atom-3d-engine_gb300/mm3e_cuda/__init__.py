@@ -67,7 +67,7 @@ class Context:
         return {"sm_count": sm.value, "clock_khz": clk.value}
 
     # ---- launch shape, profiling -------------------------------------------------------------
-    def set_tuning(self, block=128, tile_wlog=3, unroll=16, min_blocks=0):
+    def set_tuning(self, block=128, tile_wlog=3, unroll=64, min_blocks=0):
         self.check(lib().mm3e_ctx_set_tuning(self._ptr, C.byref(abi.Tuning(block, tile_wlog, unroll, min_blocks))))
 
     def get_tuning(self):

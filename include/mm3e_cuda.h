@@ -327,8 +327,8 @@ int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
 
 /* Launch shape of the march and soft-shadow passes: threads per CTA (128 or 256), pixel tile
  * of 32 pixels 2^tile_wlog wide (tile_wlog 0..5; 3 = 8x4), and field samples per lane between
- * work refills (unroll 1..64, default 16; the tape interpreter's kernels round it down to 1, 4
- * or 16);
+ * work refills (unroll 1..64, default 64; the tape interpreter's kernels round it down to 1, 16
+ * or 64);
  * min_blocks (0..16) asks the compiler of scene-specialised
  * kernels to fit that many CTAs per SM in the register file (0: the compiler's choice for the
  * shadow / AO kernels and 7 CTAs of 128 or 3 of 256 for the march kernel). Results do not depend
@@ -504,7 +504,7 @@ int mm3e_batch_configure(mm3e_ctx* ctx, const mm3e_batch_config* cfg);
  * max_samples samples; each pass of a sequence is one launch over all its jobs. Blocking. */
 int mm3e_render_batch(mm3e_ctx* ctx, const mm3e_job* jobs, size_t n, mm3e_batch_stats* stats);
 
-/* Times every launch shape (block 128/256 x tile_wlog 2/3/4 x unroll 1/4/16) on `jobs` (each
+/* Times every launch shape (block 128/256 x tile_wlog 2/3/4 x unroll 1/16/64) on `jobs` (each
  * rendered `repeats` times after a warm-up), keeps the fastest as the context's tuning and
  * reports the timings. */
 typedef struct mm3e_tune_entry {

@@ -94,7 +94,7 @@ def test_batch_f32_output_and_tile_shapes():
     try:
         items = _mixed(ctx, [(50, 30), (37, 21), (64, 40), (45, 45)])
         refs = [cs.render(cam, fmt=abi.FB_RGBA_F32) for cs, cam, _, _ in items]
-        for block, wlog, unroll in ((128, 3, 1), (256, 2, 4), (128, 4, 16), (256, 5, 1)):
+        for block, wlog, unroll in ((128, 3, 1), (256, 2, 16), (128, 4, 64), (256, 5, 1)):
             ctx.set_tuning(block, wlog, unroll)
             outs = [np.zeros((h, w, 4), np.float32) for _, _, w, h in items]
             jobs = ctx.make_jobs([(cs, cam, 0, 0, abi.FB_RGBA_F32, None, o) for (cs, cam, _, _), o in zip(items, outs)])
@@ -114,7 +114,7 @@ def test_autotune_picks_a_listed_shape():
         outs = [np.zeros((h, w, 4), np.uint8) for _, _, w, h in items]
         jobs = ctx.make_jobs([(cs, cam, 0, 0, abi.FB_RGBA8, None, o) for (cs, cam, _, _), o in zip(items, outs)])
         best, table = ctx.autotune(jobs, repeats=1)
-        assert len(table) == 18  # block 128 / 256 x tile 2 / 3 / 4 x unroll 1 / 4 / 16
+        assert len(table) == 18  # block 128 / 256 x tile 2 / 3 / 4 x unroll 1 / 16 / 64
         assert best in [t for t, _ in table]
         assert ctx.get_tuning() == best
         assert all(ms > 0 for _, ms in table)
