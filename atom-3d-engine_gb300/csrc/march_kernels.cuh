@@ -524,7 +524,11 @@ __device__ __forceinline__ void s_step(SLane& S, const LaneTape<TM>& LT, const W
         S.item = NIL;
         return;
     }
-    S.sres = fminf(S.sres, S.sk * hh / S.st);
+    // res = min(res, k*h/t) (march.rs:246). All terms are positive here (h >= 8e-4, k, t > 0), so
+    // where k*h exceeds res*t by a relative 2^-20 the quotient cannot undercut res and the
+    // division (several instructions in IEEE binary32) is skipped; elsewhere it is taken exactly.
+    const float kh = S.sk * hh;
+    if (!(kh > S.sres * S.st * 1.00000095f)) S.sres = fminf(S.sres, kh / S.st);
     S.st = S.st + clampf(hh, 0.06f, 0.5f + 0.7f * S.st);
     S.si += 1;
     if (S.st > S.smax || S.si >= T.h->shadow_steps) {
