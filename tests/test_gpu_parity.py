@@ -247,3 +247,26 @@ def test_noncons_scene_parity(gpu_ctx):
     compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
     _check_image("noncons", gpu, ref)
     _check_hits("noncons", compiled, scene, cam)
+
+
+def test_deep_reflection_chain_parity(gpu_ctx):
+    """Seven bounces between two facing mirrors: every reflection level of the pipeline (queues
+    b / c / d and hit sets 1 / 2 rotating, each level's march waiting for the shading two levels
+    back) against the oracle's recursion."""
+    from mm3e_cuda.scene import Material, Object, Prim, Scene, Transform, directional, look_at, radians
+
+    s = Scene(160, 90)
+    s.bounces = 7
+    floor = s.material(Material.solid((0.8, 0.8, 0.8), checker=True))
+    mirror = s.material(Material.solid((0.9, 0.9, 0.95), metallic=1.0, roughness=0.05, reflectivity=0.9))
+    red = s.material(Material.solid((0.8, 0.2, 0.2), roughness=0.4, reflectivity=0.3))
+    s.add(Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, floor))
+    s.add(Object(Prim.box((0.1, 2.0, 3.0)), Transform.at((-2.5, 2.0, 0.0)), mirror))
+    s.add(Object(Prim.box((0.1, 2.0, 3.0)), Transform.at((2.5, 2.0, 0.0)), mirror))
+    s.add(Object(Prim.sphere(0.6), Transform.at((0.0, 0.8, 0.5)), red))
+    s.light(directional((0.4, 0.8, -0.3), (1.2, 1.1, 1.0)))
+    cam = look_at((0.3, 1.6, -5.5), (0.0, 1.2, 0.0), (0.0, 1.0, 0.0), radians(55.0))
+    compiled, gpu, ref = _render_pair(gpu_ctx, s, cam)
+    _check_image("mirrors_b7", gpu, ref)
+    compiled.specialize(compiled.SPEC_ALWAYS)
+    assert np.array_equal(compiled.render(cam, fmt=abi.FB_RGBA8), gpu)
