@@ -249,14 +249,12 @@ def test_noncons_scene_parity(gpu_ctx):
     _check_hits("noncons", compiled, scene, cam)
 
 
-def test_deep_reflection_chain_parity(gpu_ctx):
-    """Seven bounces between two facing mirrors: every reflection level of the pipeline (queues
-    b / c / d and hit sets 1 / 2 rotating, each level's march waiting for the shading two levels
-    back) against the oracle's recursion."""
+def _mirror_scene(bounces, shadows=True):
     from mm3e_cuda.scene import Material, Object, Prim, Scene, Transform, directional, look_at, radians
 
     s = Scene(160, 90)
-    s.bounces = 7
+    s.bounces = bounces
+    s.shadows = shadows
     floor = s.material(Material.solid((0.8, 0.8, 0.8), checker=True))
     mirror = s.material(Material.solid((0.9, 0.9, 0.95), metallic=1.0, roughness=0.05, reflectivity=0.9))
     red = s.material(Material.solid((0.8, 0.2, 0.2), roughness=0.4, reflectivity=0.3))
@@ -266,7 +264,25 @@ def test_deep_reflection_chain_parity(gpu_ctx):
     s.add(Object(Prim.sphere(0.6), Transform.at((0.0, 0.8, 0.5)), red))
     s.light(directional((0.4, 0.8, -0.3), (1.2, 1.1, 1.0)))
     cam = look_at((0.3, 1.6, -5.5), (0.0, 1.2, 0.0), (0.0, 1.0, 0.0), radians(55.0))
+    return s, cam
+
+
+def test_deep_reflection_chain_parity(gpu_ctx):
+    """Seven bounces between two facing mirrors (~2.6 reflection rays per pixel): every level of
+    the reflection pipeline (queues b / c / d and hit sets 1 / 2 rotating, each level's march
+    waiting for the shading two levels back) against the oracle's recursion. Without shadows the
+    frame is bit-exact. With shadows, the reference's position hash for the shadow start
+    (fract(sin(hb) * 43758.547), march.rs:236) turns the 1-ulp differences between CUDA's and the
+    C library's sinf into different start offsets on about 0.7% of shadow rays; on this
+    high-contrast scene 0.14% of pixels then differ by more than 1 LSB (PSNR stays near 68 dB)."""
+    s, cam = _mirror_scene(7, shadows=False)
     compiled, gpu, ref = _render_pair(gpu_ctx, s, cam)
-    _check_image("mirrors_b7", gpu, ref)
+    m = _check_image("mirrors_b7_noshadow", gpu, ref)
+    assert m["exact_px"] == 1.0
     compiled.specialize(compiled.SPEC_ALWAYS)
     assert np.array_equal(compiled.render(cam, fmt=abi.FB_RGBA8), gpu)
+    s, cam = _mirror_scene(7)
+    compiled, gpu, ref = _render_pair(gpu_ctx, s, cam)
+    m = image_metrics(gpu, ref)
+    print("mirrors_b7", json.dumps(m))
+    assert m["psnr"] >= PSNR_MIN and m["within1_px"] >= 0.998, m
