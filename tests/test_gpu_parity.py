@@ -273,7 +273,7 @@ def test_deep_reflection_chain_parity(gpu_ctx):
     waiting for the shading two levels back) against the oracle's recursion. Without shadows the
     frame is bit-exact. With shadows, the reference's position hash for the shadow start
     (fract(sin(hb) * 43758.547), march.rs:236) turns the 1-ulp differences between CUDA's and the
-    C library's sinf into different start offsets on about 0.7% of shadow rays; on this
+    C library's sinf into different start offsets on some shadow rays; on this
     high-contrast scene 0.14% of pixels then differ by more than 1 LSB (PSNR stays near 68 dB)."""
     s, cam = _mirror_scene(7, shadows=False)
     compiled, gpu, ref = _render_pair(gpu_ctx, s, cam)
