@@ -12,22 +12,24 @@ template <class T> cudaError_t grow(T** p, size_t n) {
 }  // namespace
 
 void PassBuffers::release() {
-    void* ps[] = {qa_o, qa_d, h_n, h_m, occ, shadow, lvl, term, hdr, bright, blur, counters};
+    void* ps[] = {qa_o, qa_d, qb_o, qb_d, qc_o, qc_d, qd_o, qd_d, h_n, h_m, occ, shadow, h_n1, h_m1, occ1, shadow1,
+                  h_n2, h_m2, occ2, shadow2, lvl, term, hdr, bright, blur, counters};
     for (void* p : ps) cudaFree(p);
-    for (int v = 0; v < MAX_LEVELS; ++v) {
-        void* lp[] = {lq_o[v], lq_d[v], lh_n[v], lh_m[v], locc[v], lshadow[v]};
-        for (void* p : lp) cudaFree(p);
-    }
     if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
+    for (int i = 0; i < MAX_LEVELS; ++i) {
+        if (ev_marched[i]) cudaEventDestroy(ev_marched[i]);
+        if (ev_shaded[i]) cudaEventDestroy(ev_shaded[i]);
+    }
     if (aux) cudaStreamDestroy(aux);
+    if (aux2) cudaStreamDestroy(aux2);
     *this = PassBuffers();
 }
 
 size_t PassBuffers::bytes_for(size_t cap, size_t lights, size_t levels, size_t pixels) {
     size_t l = lights ? lights : 1, v = levels ? levels : 1;
-    // per level: a ray queue (2 float4) and a hit set (float4 + uint2 + AO + a shadow per light)
-    return cap * (v * (2 * sizeof(float4) + sizeof(float4) + sizeof(uint2) + sizeof(float) + l * sizeof(float)) +
+    size_t queues = v >= 4 ? 8 : (v >= 3 ? 6 : 4), hit_sets = v >= 3 ? 3 : (v >= 2 ? 2 : 1);
+    return cap * (queues * sizeof(float4) + hit_sets * (sizeof(float4) + sizeof(uint2) + sizeof(float) +
+                                                         l * sizeof(float)) +
                   2 * v * sizeof(float4) + sizeof(float4)) +
            pixels * 3 * sizeof(float4) + N_COUNTERS * sizeof(uint32_t);
 }
@@ -41,28 +43,36 @@ cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need
     size_t l = need_lights > lights ? need_lights : lights;
     size_t v = need_levels > levels ? need_levels : levels;
     size_t px = need_pixels > pixels ? need_pixels : pixels;
-    if (v > (size_t)MAX_LEVELS) v = MAX_LEVELS;
     release();
     c = c ? c : 1;
-    l = l ? l : 1;
-    v = v ? v : 1;
     cudaError_t e;
-    if ((e = grow(&qa_o, c)) || (e = grow(&qa_d, c)) || (e = grow(&h_n, c)) || (e = grow(&h_m, c)) ||
-        (e = grow(&occ, c)) || (e = grow(&shadow, c * l)) || (e = grow(&lvl, c * 2 * v)) || (e = grow(&term, c)) ||
-        (e = grow(&hdr, px)) || (e = grow(&bright, px)) || (e = grow(&blur, px)) ||
-        (e = grow(&counters, (size_t)N_COUNTERS))) {
+    if ((e = grow(&qa_o, c)) || (e = grow(&qa_d, c)) || (e = grow(&qb_o, c)) || (e = grow(&qb_d, c)) ||
+        (e = grow(&h_n, c)) || (e = grow(&h_m, c)) || (e = grow(&occ, c)) || (e = grow(&shadow, c * (l ? l : 1))) ||
+        (e = grow(&lvl, c * 2 * (v ? v : 1))) || (e = grow(&term, c)) || (e = grow(&hdr, px)) ||
+        (e = grow(&bright, px)) || (e = grow(&blur, px)) || (e = grow(&counters, (size_t)N_COUNTERS))) {
         release();
         return e;
     }
-    for (size_t k = 1; k < v; ++k)
-        if ((e = grow(&lq_o[k], c)) || (e = grow(&lq_d[k], c)) || (e = grow(&lh_n[k], c)) || (e = grow(&lh_m[k], c)) ||
-            (e = grow(&locc[k], c)) || (e = grow(&lshadow[k], c * l))) {
+    if (v >= 2 && ((e = grow(&h_n1, c)) || (e = grow(&h_m1, c)) || (e = grow(&occ1, c)) ||
+                   (e = grow(&shadow1, c * (l ? l : 1))) ||
+                   (e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) ||
+                   (e = cudaStreamCreateWithFlags(&aux2, cudaStreamNonBlocking)) ||
+                   (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)))) {
+        release();
+        return e;
+    }
+    for (size_t i = 1; i < v && i < (size_t)MAX_LEVELS; ++i)
+        if ((e = cudaEventCreateWithFlags(&ev_marched[i], cudaEventDisableTiming)) ||
+            (e = cudaEventCreateWithFlags(&ev_shaded[i], cudaEventDisableTiming))) {
             release();
             return e;
         }
-    if (v >= 2 && ((e = cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking)) ||
-                   (e = cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming)) ||
-                   (e = cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming)))) {
+    if (v >= 3 && ((e = grow(&qc_o, c)) || (e = grow(&qc_d, c)) || (e = grow(&h_n2, c)) || (e = grow(&h_m2, c)) ||
+                   (e = grow(&occ2, c)) || (e = grow(&shadow2, c * (l ? l : 1))))) {
+        release();
+        return e;
+    }
+    if (v >= 4 && ((e = grow(&qd_o, c)) || (e = grow(&qd_d, c)))) {
         release();
         return e;
     }
@@ -207,18 +217,13 @@ WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tun
     a.b.h_m = buf.h_m;
     a.b.occ = buf.occ;
     a.b.shadow = buf.shadow;
+    a.b.nq_o = buf.qb_o;
+    a.b.nq_d = buf.qb_d;
     a.b.lvl = buf.lvl;
     a.b.term = buf.term;
     a.b.hdr = buf.hdr;
     a.b.fg = buf.bright;
     a.film = plan.film ? 1u : 0u;
-    for (int k = 1; k < MAX_LEVELS && k < (int)buf.levels; ++k) {
-        a.lq_o[k] = buf.lq_o[k];
-        a.lq_d[k] = buf.lq_d[k];
-        a.lh_n[k] = buf.lh_n[k];
-        a.lh_m[k] = buf.lh_m[k];
-        a.lq_count[k] = buf.counters + 4 * (k - 1) + 2;
-    }
     return a;
 }
 }  // namespace
@@ -229,35 +234,24 @@ const uint32_t* primary_count(const PassPlan& plan) {
     return plan.jobs ? &plan.totals->n_samples : nullptr;
 }
 
-// The AO, shadow and shading passes of one level whose hits exist (queue / hit set in a.b).
-cudaError_t shade_passes(const PassPlan& plan, WaveArgs& a, PassBuffers& buf, const TuneParams& tune, cudaStream_t s,
-                         int sm_count, LaunchLog* log, uint32_t level) {
+// The passes of one level: march, AO, shadows, (reflection rays of the next level), shading.
+cudaError_t level_passes(const PassPlan& plan, WaveArgs& a, PassBuffers& buf, const TuneParams& tune, cudaStream_t s,
+                         int sm_count, LaunchLog* log, uint32_t level, bool reflect_next) {
     cudaError_t e;
     a.level = level;
     a.src = level == 0 && !plan.queue0 ? SRC_SAMPLES : SRC_QUEUE;
     a.n_items = plan.n_samples;
     a.n_items_dev = level == 0 ? primary_count(plan) : buf.counters + 4 * (level - 1) + 2;
-    a.chain_levels = 0;
+    a.b.nq_count = buf.counters + 4 * level + 2;
+    a.counter = buf.counters + 4 * level;
+    if ((e = launch_march(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+    if (reflect_next && (e = launch_reflect(a, s, log)) != cudaSuccess) return e;
     if (plan.ao && (e = launch_ao(a, s, log, plan.spec)) != cudaSuccess) return e;
     if (plan.shadows && plan.lights_max > 0) {
         a.counter = buf.counters + 4 * level + 1;
         if ((e = launch_shadow(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
     }
     return launch_shade(a, s, log);
-}
-
-// One level on its own (no reflections): march, then AO, shadows and shading.
-cudaError_t level_passes(const PassPlan& plan, WaveArgs& a, PassBuffers& buf, const TuneParams& tune, cudaStream_t s,
-                         int sm_count, LaunchLog* log, uint32_t level) {
-    cudaError_t e;
-    a.level = level;
-    a.src = level == 0 && !plan.queue0 ? SRC_SAMPLES : SRC_QUEUE;
-    a.n_items = plan.n_samples;
-    a.n_items_dev = level == 0 ? primary_count(plan) : buf.counters + 4 * (level - 1) + 2;
-    a.counter = buf.counters + 4 * level;
-    a.chain_levels = 0;
-    if ((e = launch_march(a, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
-    return shade_passes(plan, a, buf, tune, s, sm_count, log, level);
 }
 }  // namespace
 
@@ -266,34 +260,72 @@ cudaError_t run_beauty(const PassPlan& plan, PassBuffers& buf, const TuneParams&
     cudaError_t e = cudaMemsetAsync(buf.counters, 0, (N_COUNTERS - (plan.clear_status ? 0 : 1)) * sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     WaveArgs a = wave_args(plan, buf, tune, sm_count);
+    a.emit = 0;  // reflection rays come from the reflect pass, right after each level's march
     const uint32_t levels = plan.levels > buf.levels ? (uint32_t)buf.levels : plan.levels;
     if (levels <= 1) {
-        if ((e = level_passes(plan, a, buf, tune, s, sm_count, log, 0)) != cudaSuccess) return e;
+        if ((e = level_passes(plan, a, buf, tune, s, sm_count, log, 0, false)) != cudaSuccess) return e;
     } else {
-        // the primary march runs every reflection chain too; then the levels shade side by side
+        // primary level on `s`; its reflection rays fork the deeper levels onto the aux streams
         WaveArgs a0 = a;
+        a0.b.nq_o = buf.qb_o;
+        a0.b.nq_d = buf.qb_d;
         a0.level = 0;
         a0.src = plan.queue0 ? SRC_QUEUE : SRC_SAMPLES;
         a0.n_items = plan.n_samples;
         a0.n_items_dev = primary_count(plan);
+        a0.b.nq_count = buf.counters + 2;
         a0.counter = buf.counters;
-        a0.chain_levels = levels;
         if ((e = launch_march(a0, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+        if ((e = launch_reflect(a0, s, log)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(buf.ev_fork, s)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(buf.aux, buf.ev_fork, 0)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(buf.aux2, buf.ev_fork, 0)) != cudaSuccess) return e;
+        float4* q_o[3] = {buf.qb_o, buf.qc_o, buf.qd_o};
+        float4* q_d[3] = {buf.qb_d, buf.qc_d, buf.qd_d};
         for (uint32_t level = 1; level < levels; ++level) {
             WaveArgs ak = a;
-            ak.b.q_o = buf.lq_o[level];
-            ak.b.q_d = buf.lq_d[level];
-            ak.b.h_n = buf.lh_n[level];
-            ak.b.h_m = buf.lh_m[level];
-            ak.b.occ = buf.locc[level];
-            ak.b.shadow = buf.lshadow[level];
-            if ((e = shade_passes(plan, ak, buf, tune, buf.aux, sm_count, log, level)) != cudaSuccess) return e;
+            const uint32_t qi = (level - 1) % 3, ni = level % 3;
+            const bool odd = (level & 1u) != 0;
+            ak.b.q_o = q_o[qi];
+            ak.b.q_d = q_d[qi];
+            ak.b.nq_o = q_o[ni];
+            ak.b.nq_d = q_d[ni];
+            ak.b.h_n = odd ? buf.h_n1 : buf.h_n2;
+            ak.b.h_m = odd ? buf.h_m1 : buf.h_m2;
+            ak.b.occ = odd ? buf.occ1 : buf.occ2;
+            ak.b.shadow = odd ? buf.shadow1 : buf.shadow2;
+            ak.level = level;
+            ak.src = SRC_QUEUE;
+            ak.n_items = plan.n_samples;
+            ak.n_items_dev = buf.counters + 4 * (level - 1) + 2;
+            ak.b.nq_count = buf.counters + 4 * level + 2;
+            // this level's hits overwrite those of level - 2, and its reflection rays the queue
+            // level - 2 read: both wait for that level's shading
+            if (level >= 3 && (e = cudaStreamWaitEvent(buf.aux, buf.ev_shaded[level - 2], 0)) != cudaSuccess) return e;
+            ak.counter = buf.counters + 4 * level;
+            if ((e = launch_march(ak, tune, buf.aux, sm_count, log, plan.spec)) != cudaSuccess) return e;
+            if (level + 1 < levels && (e = launch_reflect(ak, buf.aux, log)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(buf.ev_marched[level], buf.aux)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(buf.aux2, buf.ev_marched[level], 0)) != cudaSuccess) return e;
+            if (plan.ao && (e = launch_ao(ak, buf.aux2, log, plan.spec)) != cudaSuccess) return e;
+            if (plan.shadows && plan.lights_max > 0) {
+                ak.counter = buf.counters + 4 * level + 1;
+                if ((e = launch_shadow(ak, tune, buf.aux2, sm_count, log, plan.spec)) != cudaSuccess) return e;
+            }
+            if ((e = launch_shade(ak, buf.aux2, log)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(buf.ev_shaded[level], buf.aux2)) != cudaSuccess) return e;
         }
-        if ((e = cudaEventRecord(buf.ev_join, buf.aux)) != cudaSuccess) return e;
-        if ((e = shade_passes(plan, a0, buf, tune, s, sm_count, log, 0)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(s, buf.ev_join, 0)) != cudaSuccess) return e;
+        // the primary level's AO, shadows and shading overlap the reflection levels
+        a0.counter = buf.counters;
+        if (plan.ao && (e = launch_ao(a0, s, log, plan.spec)) != cudaSuccess) return e;
+        if (plan.shadows && plan.lights_max > 0) {
+            a0.counter = buf.counters + 1;
+            if ((e = launch_shadow(a0, tune, s, sm_count, log, plan.spec)) != cudaSuccess) return e;
+        }
+        if ((e = launch_shade(a0, s, log)) != cudaSuccess) return e;
+        // join: every reflection level's shading (in order on aux2) and the last march (aux)
+        if ((e = cudaStreamWaitEvent(s, buf.ev_shaded[levels - 1], 0)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s, buf.ev_marched[levels - 1], 0)) != cudaSuccess) return e;
     }
     if (plan.queue0) return cudaSuccess;
     if ((e = launch_resolve(a, plan.n_slots, s, log)) != cudaSuccess) return e;

@@ -26,27 +26,37 @@ inline uint64_t slots_of(uint32_t w, uint32_t h, uint32_t wlog) {
 
 constexpr int N_COUNTERS = 64;  // [4L] march, [4L+1] shadow, [4L+2] next queue length; [63] status
 
+constexpr int MAX_LEVELS = 8;  // bounces + 1 (MAX_BOUNCES = 7)
+
 // Device buffers of a pass sequence: ray queues and per-sample records for `cap` samples,
 // HDR / bloom arrays for `pixels` output pixels, and the work counters.
-// Level 0 (camera samples) has queue a and hit set 0, indexed by sample. Every reflection level L
-// has its own ray queue and hit set (lq_* / lh_*[L], indexed by queue slot): the primary march
-// continues each lane's ray into its reflection rays (so the reflection levels march inside the
-// primary level's launch), and the levels' AO / shadow / shading passes then run independently.
+// The levels run as a pipeline: level 0 on the caller's stream; the reflection levels' marches
+// (each emitting the next level's rays) in order on one auxiliary stream, forked as soon as the
+// primary hits exist; and each reflection level's AO / shadows / shading on a second auxiliary
+// stream as soon as its hits exist, beside the next level's march. So level 0 has queue a and hit
+// set 0, and reflection level L reads queue b, c, d (rotating from L = 1) and writes hit set 1
+// (odd L) or 2 (even L); a level's march waits for the shading of the level two before it, the
+// last reader of the queue and hit set it overwrites.
 struct PassBuffers {
     size_t cap = 0, lights = 0, levels = 0, pixels = 0;
-    float4 *qa_o = nullptr, *qa_d = nullptr;
+    float4 *qa_o = nullptr, *qa_d = nullptr, *qb_o = nullptr, *qb_d = nullptr, *qc_o = nullptr, *qc_d = nullptr;
+    float4 *qd_o = nullptr, *qd_d = nullptr;
     float4* h_n = nullptr;
     uint2* h_m = nullptr;
     float *occ = nullptr, *shadow = nullptr;
-    float4 *lq_o[MAX_LEVELS] = {}, *lq_d[MAX_LEVELS] = {};  // reflection level L's rays (L >= 1)
-    float4* lh_n[MAX_LEVELS] = {};                          // its hit records
-    uint2* lh_m[MAX_LEVELS] = {};
-    float *locc[MAX_LEVELS] = {}, *lshadow[MAX_LEVELS] = {};
+    float4* h_n1 = nullptr;  // hit set 1 (odd reflection levels)
+    uint2* h_m1 = nullptr;
+    float *occ1 = nullptr, *shadow1 = nullptr;
+    float4* h_n2 = nullptr;  // hit set 2 (even reflection levels)
+    uint2* h_m2 = nullptr;
+    float *occ2 = nullptr, *shadow2 = nullptr;
     float4 *lvl = nullptr, *term = nullptr;
     float4 *hdr = nullptr, *bright = nullptr, *blur = nullptr;
     uint32_t* counters = nullptr;
-    cudaStream_t aux = nullptr;  // reflection levels' AO / shadows / shading
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t aux = nullptr;   // reflection levels' marches
+    cudaStream_t aux2 = nullptr;  // reflection levels' AO / shadows / shading
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_marched[MAX_LEVELS] = {}, ev_shaded[MAX_LEVELS] = {};
     void release();
     // Grows the buffers to hold at least the given sizes (contents are not kept).
     cudaError_t ensure(size_t cap, size_t lights, size_t levels, size_t pixels);

@@ -2,12 +2,10 @@
 //
 // A beauty frame is rendered as a sequence of small kernels over ray queues (one per
 // reflection level), each with a compact code footprint:
-//   march   persistent tape interpreter: enhanced sphere tracing + hit normal per ray; a lane
-//           whose ray hits a reflective surface marches the reflection ray next, appending it
-//           to the next level's queue (all levels' rays march in the primary launch)
+//   march   persistent tape interpreter: enhanced sphere tracing + hit normal per ray
 //   ao      5-tap ambient occlusion per hit
 //   shadow  persistent soft-shadow marches, one per (hit, light)
-//   shade   GGX / IBL / GI / fog shading of one level's hits
+//   shade   GGX / IBL / GI / fog shading; appends reflection rays to the next level's queue
 //   resolve folds the reflection levels of every AA sample and averages a pixel's samples
 // followed by the post kernels (bloom, exposure, ACES, gamma, pack).
 //
@@ -71,8 +69,6 @@ struct TuneParams {
     uint32_t min_blocks = 0; // specialised kernels: CTAs per SM the register budget must allow (0: free)
 };
 
-constexpr int MAX_LEVELS = 8;  // reflection levels + 1 (bounces <= 7)
-
 // Device buffers of one pass sequence.
 struct WaveBuffers {
     float4* q_o;         // ray origin xyz, w = sample slot (uint bits)
@@ -81,6 +77,9 @@ struct WaveBuffers {
     uint2* h_m;          // x = material id or NIL (miss), y = march steps
     float* occ;          // AO per queue slot
     float* shadow;       // per (slot * lights_max + light): < 0 light skipped, else shadow factor
+    float4* nq_o;        // next level's queue
+    float4* nq_d;
+    uint32_t* nq_count;  // next level's queue length (device counter)
     float4* lvl;         // per sample and level: [(level * cap + sample) * 2 + {0, 1}]
     float4* term;        // per sample: terminal radiance xyz, w = level it ended at (uint bits)
     float4* hdr;         // per output pixel (job.pixel_base + y * w + x)
@@ -109,16 +108,8 @@ struct WaveArgs {
     uint32_t gi_nx, gi_ny, gi_nz, dirs_per_face;
     const float4* gather_dirs;
     uint32_t aov_mode;          // RenderMode for the AOV resolve
+    uint32_t emit;              // shade appends reflection rays (else a reflect pass did)
     uint32_t film;              // resolve also writes coverage (hdr.w) and the foreground (b.fg)
-    // Reflection chain of the primary march (chain_levels > 1): a lane whose ray hits a reflective
-    // surface below the bounce limit appends the reflection ray to level L+1's queue (lq_o / lq_d,
-    // length lq_count) and marches it next, writing its hit to lh_n / lh_m [L+1] at that slot.
-    uint32_t chain_levels;
-    float4* lq_o[MAX_LEVELS];
-    float4* lq_d[MAX_LEVELS];
-    float4* lh_n[MAX_LEVELS];
-    uint2* lh_m[MAX_LEVELS];
-    uint32_t* lq_count[MAX_LEVELS];
 };
 
 // Status bits written by kernels.
@@ -174,6 +165,7 @@ cudaError_t launch_shadow(const WaveArgs& a, const TuneParams& t, cudaStream_t s
                           const SpecKernels* spec = nullptr);
 cudaError_t launch_shade(const WaveArgs& a, cudaStream_t s, LaunchLog* log);
 // Reflection rays of the level's hits (the rays shade would append), into the next queue.
+cudaError_t launch_reflect(const WaveArgs& a, cudaStream_t s, LaunchLog* log);
 // Pixel slots of the jobs (n_slots when known on the host, else capacity + a.totals).
 cudaError_t launch_resolve(const WaveArgs& a, uint32_t n_slots, cudaStream_t s, LaunchLog* log);
 // AOV modes: display value per pixel-centre hit of job 0 (lib.rs:1185-1217), written as RGBA f32.

@@ -209,7 +209,6 @@ constexpr uint32_t BOOST_OMEGA = 0, BOOST_LEAP = 1, BOOST_SECANT = 2;
 
 struct MLane {
     uint32_t item, phase;
-    uint32_t level, sample, job;  // reflection depth of the current ray, its root sample and job
     V ro, rd;
     float t, prev_r, step, t_prev, d_prev, omega, subz;
     uint32_t i, secant_on, boost;
@@ -221,56 +220,10 @@ struct MLane {
 
 __device__ __forceinline__ V m_at(const MLane& L, float t) { return L.ro + scale(L.rd, t); }
 
-// Ray state at t = 0 (march.rs:132-141).
-__device__ __forceinline__ void m_init(MLane& L, const TapeHeader& h) {
-    L.t = 0.0f;
-    L.prev_r = 0.0f;
-    L.step = 0.0f;
-    L.t_prev = 0.0f;
-    L.d_prev = __int_as_float(0x7f800000);
-    bool lip = h.step_scale >= 1.0f;
-    L.omega = lip ? 1.4f : h.step_scale;
-    L.subz = lip ? h.subitize : 0.0f;
-    L.secant_on = ((h.flags & SF_SECANT) && lip) ? 1u : 0u;
-    L.boost = BOOST_OMEGA;
-    L.i = 0;
-    L.phase = M_MARCH;
-}
-
-// Finish a ray: write the hit record (normal, t, material or NIL, steps) into its level's hit
-// set. On a reflective hit below the bounce limit, with the pass's reflection chain on, the lane
-// goes on with the reflection ray shade_hit recurses into (lib.rs:1336-1343): appended to the
-// next level's queue (origin lifted off the surface, root sample in o.w, job in d.w) and marched
-// next, so every level's rays march in this one launch. The level's shading pass later decides
-// reflective-or-terminal with the same test.
-template <int TM>
-__device__ __forceinline__ void m_write(MLane& L, const LaneTape<TM>& LT, const WaveArgs& a, bool hit, V n,
-                                        uint32_t steps) {
-    const bool own = L.level == a.level;
-    float4* hn = own ? a.b.h_n : a.lh_n[L.level];
-    uint2* hm = own ? a.b.h_m : a.lh_m[L.level];
-    hn[L.item] = make_float4(n.x, n.y, n.z, L.t);
-    hm[L.item] = make_uint2(hit ? L.hmat : NIL, steps);
-    if (hit && L.level + 1u < a.chain_levels) {
-        const Tape T = LT.get();
-        const TapeHeader& h = *T.h;
-        const DevMaterial& m = T.mat[L.hmat % h.n_materials];
-        if (L.level < h.bounces && m.reflectivity > 0.0f) {
-            V hp = L.ro + scale(L.rd, L.t);
-            V rdir = normalize(reflect(L.rd, n));
-            V rorig = hp + scale(n, fmaxf(h.normal_h * 2.0f, 0.02f));
-            const uint32_t next = L.level + 1u;
-            const uint32_t q = atomicAdd(a.lq_count[next], 1u);
-            a.lq_o[next][q] = make_float4(rorig.x, rorig.y, rorig.z, __uint_as_float(L.sample));
-            a.lq_d[next][q] = make_float4(rdir.x, rdir.y, rdir.z, __uint_as_float(L.job));
-            L.item = q;
-            L.level = next;
-            L.ro = rorig;
-            L.rd = rdir;
-            m_init(L, h);  // max_steps > 0 here: this ray's parent marched to a hit
-            return;
-        }
-    }
+// Finish a ray: write the hit record (normal, t, material or NIL, steps).
+__device__ __forceinline__ void m_write(MLane& L, const WaveArgs& a, bool hit, V n, uint32_t steps) {
+    a.b.h_n[L.item] = make_float4(n.x, n.y, n.z, L.t);
+    a.b.h_m[L.item] = make_uint2(hit ? L.hmat : NIL, steps);
     L.item = NIL;
     L.phase = M_IDLE;
 }
@@ -295,12 +248,9 @@ __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveAr
         if (inside && aa > 1u && J.lens_radius > 0.0f) lens_ray(J, x, y, sx, sy, aa, L.ro, L.rd);
         a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
         a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, __uint_as_float(job));
-        L.level = a.level;
-        L.sample = L.item;
-        L.job = job;
         if (!inside) {  // padding pixel of the last tile row / column
             L.t = 0.0f;
-            m_write(L, LT, a, false, V{0.f, 0.f, 0.f}, 0u);
+            m_write(L, a, false, V{0.f, 0.f, 0.f}, 0u);
             return false;
         }
         LT.set(J.tape);
@@ -311,18 +261,12 @@ __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveAr
         L.rd = camera_dir(J.cam, (float)x + 0.5f, (float)y + 0.5f, J.width, J.height);
         a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
         a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, 0.0f);
-        L.level = a.level;
-        L.sample = L.item;
-        L.job = 0;
         LT.set(J.tape);
     } else if (a.src == SRC_QUEUE) {
         float4 o = a.b.q_o[L.item], d = a.b.q_d[L.item];
         L.ro = V{o.x, o.y, o.z};
         L.rd = V{d.x, d.y, d.z};
         job = a.jobs ? __float_as_uint(d.w) : 0u;
-        L.level = a.level;
-        L.sample = __float_as_uint(o.w);
-        L.job = job;
         LT.set(job_ref(a, job).tape);
     } else {  // SRC_GATHER (gi.rs:75-87)
         uint32_t dpf = a.dirs_per_face;
@@ -334,15 +278,24 @@ __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveAr
         L.rd = V{dw.x, dw.y, dw.z};
         a.b.q_o[L.item] = make_float4(L.ro.x, L.ro.y, L.ro.z, __uint_as_float(L.item));
         a.b.q_d[L.item] = make_float4(L.rd.x, L.rd.y, L.rd.z, 0.0f);
-        L.level = a.level;
-        L.sample = L.item;
-        L.job = 0;
         LT.set(a.job0.tape);
     }
     const TapeHeader& h = *LT.get().h;
-    m_init(L, h);
+    // march.rs:132-141
+    L.t = 0.0f;
+    L.prev_r = 0.0f;
+    L.step = 0.0f;
+    L.t_prev = 0.0f;
+    L.d_prev = __int_as_float(0x7f800000);
+    bool lip = h.step_scale >= 1.0f;
+    L.omega = lip ? 1.4f : h.step_scale;
+    L.subz = lip ? h.subitize : 0.0f;
+    L.secant_on = ((h.flags & SF_SECANT) && lip) ? 1u : 0u;
+    L.boost = BOOST_OMEGA;
+    L.i = 0;
+    L.phase = M_MARCH;
     if (h.max_steps == 0) {
-        m_write(L, LT, a, false, V{0.f, 0.f, 0.f}, 0u);
+        m_write(L, a, false, V{0.f, 0.f, 0.f}, 0u);
         return false;
     }
     return true;
@@ -363,7 +316,7 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         V kd = scale(tetra_k(L.tap), f.d);
         L.g = L.tap == 0 ? kd : L.g + kd;
         L.tap += 1;
-        if (L.tap == 4u) m_write(L, LT, a, true, normalize(L.g), L.i);
+        if (L.tap == 4u) m_write(L, a, true, normalize(L.g), L.i);
         return;
     }
     float d;
@@ -398,7 +351,7 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
     if (d < e) {
         L.hmat = m;
         if (h.flags & SF_DUAL_SAFE) {
-            m_write(L, LT, a, true, normal_dual(T.obj, h.n_objects, m_at(L, L.t)), L.i);
+            m_write(L, a, true, normal_dual(T.obj, h.n_objects, m_at(L, L.t)), L.i);
         } else {
             L.phase = M_TETRA;
             L.tap = 0;
@@ -427,11 +380,11 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         L.t_prev = L.t;
         L.t = L.t + step_len;
         if (L.t > h.max_dist) {
-            m_write(L, LT, a, false, V{0.f, 0.f, 0.f}, max_steps);
+            m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
             return;
         }
         L.i += 1;
-        if (L.i >= max_steps) m_write(L, LT, a, false, V{0.f, 0.f, 0.f}, max_steps);
+        if (L.i >= max_steps) m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
         return;
     }
 rollback:  // retreat to the last safe frontier (march.rs:155-170)
@@ -444,7 +397,7 @@ rollback:  // retreat to the last safe frontier (march.rs:155-170)
     L.step = 0.0f;
     L.d_prev = __int_as_float(0x7f800000);
     L.i += 1;
-    if (L.i >= max_steps) m_write(L, LT, a, false, V{0.f, 0.f, 0.f}, max_steps);
+    if (L.i >= max_steps) m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
 }
 
 template <int TM, int UNROLL, class FP>

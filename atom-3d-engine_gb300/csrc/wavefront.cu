@@ -30,14 +30,16 @@ __global__ void __launch_bounds__(BLOCK) k_shadow(const __grid_constant__ WaveAr
 __global__ void __launch_bounds__(SHADE_THREADS) k_ao(const __grid_constant__ WaveArgs a) { ao_body<InterpField>(a); }
 
 // ------------------------------------------------------------------------------------------
-// shade: shade_hit (lib.rs:1286-1360) / sky on a miss; a reflective hit leaves its level's
-// record for the resolve (its reflection ray was marched by the primary march's chain)
+// shade: shade_hit (lib.rs:1286-1360) / sky on a miss; reflection rays go to the next queue
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ void shade_slots(const WaveArgs& a, uint32_t slot, bool active) {
+    bool emit = false;
+    V rorig{0.f, 0.f, 0.f}, rdir{0.f, 0.f, 0.f};
+    uint32_t sample = 0, job = 0;
     if (active) {
         float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
-        const uint32_t sample = __float_as_uint(o4.w);
-        const uint32_t job = a.jobs ? __float_as_uint(d4.w) : 0u;
+        sample = __float_as_uint(o4.w);
+        job = a.jobs ? __float_as_uint(d4.w) : 0u;
         const Tape T = tape_view(job_ref(a, job).tape);
         const TapeHeader& h = *T.h;
         V rd{d4.x, d4.y, d4.z};
@@ -75,13 +77,31 @@ __device__ __forceinline__ void shade_slots(const WaveArgs& a, uint32_t slot, bo
             if (level < h.bounces && m.reflectivity > 0.0f) {
                 float cosv = fmaxf(dot(hn, view), 0.0f);
                 float fr = fresnel_schlick(cosv, m.reflectivity);
+                rdir = normalize(reflect(rd, hn));
+                rorig = hp + scale(hn, fmaxf(h.normal_h * 2.0f, 0.02f));
                 size_t li = ((size_t)level * a.cap + sample) * 2;
                 a.b.lvl[li] = make_float4(rad.x, rad.y, rad.z, fr);
                 a.b.lvl[li + 1] = make_float4(em.x, em.y, em.z, ht);
+                emit = true;
             } else {
                 V v = apply_fog(rad + em, ld3(h.fog), ht, h.fog_density);
                 a.b.term[sample] = make_float4(v.x, v.y, v.z, __uint_as_float(level));
             }
+        }
+    }
+    // append reflection rays to the next level's queue (one atomic per warp)
+    if (!a.emit) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned mask = __ballot_sync(0xFFFFFFFFu, emit);
+    if (mask) {
+        uint32_t base = 0;
+        int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(a.b.nq_count, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (emit) {
+            uint32_t q = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+            a.b.nq_o[q] = make_float4(rorig.x, rorig.y, rorig.z, __uint_as_float(sample));
+            a.b.nq_d[q] = make_float4(rdir.x, rdir.y, rdir.z, __uint_as_float(job));
         }
     }
 }
@@ -90,6 +110,53 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_shade(const __grid_constant__
     const uint32_t n = item_count(a);
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
         shade_slots(a, base + threadIdx.x, base + threadIdx.x < n);  // block-uniform trip count
+}
+
+// The reflection ray shade_hit recurses into (lib.rs:1336-1343), emitted as soon as the level's
+// hits exist so the next level can march while this level's AO / shadows / shading run.
+__device__ __forceinline__ void reflect_slots(const WaveArgs& a, uint32_t slot, bool active) {
+    bool emit = false;
+    V rorig{0.f, 0.f, 0.f}, rdir{0.f, 0.f, 0.f};
+    uint32_t sample = 0, job = 0;
+    if (active) {
+        uint2 hm = a.b.h_m[slot];
+        if (hm.x != NIL) {
+            float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
+            job = a.jobs ? __float_as_uint(d4.w) : 0u;
+            const Tape T = tape_view(job_ref(a, job).tape);
+            const TapeHeader& h = *T.h;
+            const DevMaterial& m = T.mat[hm.x % h.n_materials];
+            if (a.level < h.bounces && m.reflectivity > 0.0f) {
+                sample = __float_as_uint(o4.w);
+                float4 hn4 = a.b.h_n[slot];
+                V rd{d4.x, d4.y, d4.z};
+                V hp = V{o4.x, o4.y, o4.z} + scale(rd, hn4.w);
+                V hn{hn4.x, hn4.y, hn4.z};
+                rdir = normalize(reflect(rd, hn));
+                rorig = hp + scale(hn, fmaxf(h.normal_h * 2.0f, 0.02f));
+                emit = true;
+            }
+        }
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned mask = __ballot_sync(0xFFFFFFFFu, emit);
+    if (mask) {
+        uint32_t base = 0;
+        int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(a.b.nq_count, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (emit) {
+            uint32_t q = base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+            a.b.nq_o[q] = make_float4(rorig.x, rorig.y, rorig.z, __uint_as_float(sample));
+            a.b.nq_d[q] = make_float4(rdir.x, rdir.y, rdir.z, __uint_as_float(job));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SHADE_THREADS) k_reflect(const __grid_constant__ WaveArgs a) {
+    const uint32_t n = item_count(a);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
+        reflect_slots(a, base + threadIdx.x, base + threadIdx.x < n);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -440,6 +507,11 @@ cudaError_t launch_shade(const WaveArgs& a, cudaStream_t s, LaunchLog* log) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_reflect(const WaveArgs& a, cudaStream_t s, LaunchLog* log) {
+    LogScope sc(log, KK_SHADE, s, 1);
+    k_reflect<<<grid_for(a.n_items, SHADE_THREADS, a.grid_cap), SHADE_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_resolve(const WaveArgs& a, uint32_t n_slots, cudaStream_t s, LaunchLog* log) {
     LogScope sc(log, KK_RESOLVE, s, 1);
