@@ -27,14 +27,15 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                         uint32_t min_blocks);
 
 // Size of the generated field: objects it inlines and CSG program ops among them. Every inlined
-// object is its own code (the interpreter shares one copy per primitive kind), so past a few
-// dozen objects the specialised kernels outgrow the instruction cache and run slower.
+// object is its own code (the interpreter shares one copy per primitive kind), so a large enough
+// field outgrows the instruction cache. Measured with 64 field samples between refills: 1.3-2.6x
+// faster than the interpreter on seeded scenes of 13 to 63 objects (1280x720).
 struct SpecSize {
     uint32_t objects = 0, csg_ops = 0;
 };
 SpecSize spec_size(const std::vector<unsigned char>& blob);
 // The automatic policy's limit.
-constexpr uint32_t SPEC_AUTO_MAX_OBJECTS = 24;
+constexpr uint32_t SPEC_AUTO_MAX_OBJECTS = 64;
 
 // NVRTC compile of a specialised program to an sm_103a cubin (no device needed).
 std::string spec_compile(const std::string& source, std::vector<char>& cubin);

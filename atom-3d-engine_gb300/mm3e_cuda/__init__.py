@@ -227,7 +227,7 @@ class CompiledScene:
 
     def specialize(self, mode=2):
         """Scene-specialised march / shadow / AO kernels (NVRTC): mode 0 off, 1 auto (only
-        fields of at most 24 objects), 2 always (True/False map to 2/0). Returns compile ms."""
+        fields of at most 64 objects), 2 always (True/False map to 2/0). Returns compile ms."""
         mode = {True: 2, False: 0}.get(mode, mode) if isinstance(mode, bool) else mode
         ms = C.c_double()
         self.ctx.check(lib().mm3e_scene_specialize(self._ptr, int(mode), C.byref(ms)))

@@ -416,8 +416,8 @@ int mm3e_bake_mesh_sdf(mm3e_ctx* ctx, const mm3e_mesh* mesh, uint32_t resolution
  * mm3e_render_device / mm3e_render_linear / mm3e_render_hits calls of the scene use them (not
  * with dynamic spheres, not in batches). The launch shape is the context's tuning at this call.
  * mode 0 drops them; 2 always compiles; 1 (auto) compiles only scenes whose field inlines at
- * most 24 objects (larger fields outgrow the instruction cache and the shared-code interpreter
- * is faster) and otherwise returns MM3E_OK leaving the interpreter. MM3E_ERR_UNSUPPORTED when
+ * most 64 objects (the sizes measured faster than the shared-code interpreter; code size grows
+ * with every object) and otherwise returns MM3E_OK leaving the interpreter. MM3E_ERR_UNSUPPORTED when
  * NVRTC cannot be loaded or compile fails. A GI bake (re-lowering) drops them. compile_ms may be
  * NULL. Blocking. */
 int mm3e_scene_specialize(mm3e_scene* scene, int mode, double* compile_ms);

@@ -54,7 +54,11 @@ def test_specialised_scene_with_dynamic_spheres_uses_the_interpreter(gpu_ctx):
 
 
 def test_auto_mode_keeps_the_interpreter_for_large_fields(gpu_ctx):
-    big, cam = scenes.procedural_scene(4, 64, 48)  # 62 objects
+    from mm3e_cuda.scene import Object, Prim, Transform
+
+    big, cam = scenes.procedural_scene(4, 64, 48)  # 62 objects, plus spheres past the 64 limit
+    for k in range(8):
+        big.add(Object(Prim.sphere(0.2), Transform.at((8.0 + k, 0.5, 8.0)), 0))
     cs = mm3e_cuda.CompiledScene(gpu_ctx, big)
     cs.specialize(cs.SPEC_AUTO)
     assert not cs.specialized
