@@ -444,7 +444,10 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
                 const DevObject& o = T.obj[i];
                 wnc = (o.flags & OF_NONCONS) && (o.flags & OF_BOUND);
                 if (o.flags & OF_BOUND) {
-                    float lower = length(p - ld3(o.bc)) - o.br;
+                    const float d2 = length_sq(p - ld3(o.bc));
+                    // cannot win: the squared pre-test first, without the square root
+                    if (!(o.flags & OF_NONCONS) && far_beyond(d2, bd, o.br)) break;
+                    float lower = sqrtf(d2) - o.br;
                     wl = lower;
                     wr = o.br;
                     if (lower > bd && !(o.flags & OF_NONCONS)) break;  // cannot win
