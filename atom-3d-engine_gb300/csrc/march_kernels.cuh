@@ -212,10 +212,12 @@ struct MLane {
     V ro, rd;
     float t, prev_r, step, t_prev, d_prev, omega, subz;
     uint32_t i, secant_on, boost;
-    float sv_d, sv_r, sv_e;
-    uint32_t sv_m, hmat;
-    V g;
-    uint32_t tap;
+    uint32_t hmat;
+    // Phase scratch, never needed by two phases at once: M_COVER keeps the step's distance,
+    // radius and epsilon in x0..x2 and its material in xu; M_TETRA keeps the gradient sum in
+    // x0..x2 and the tap index in xu.
+    float x0, x1, x2;
+    uint32_t xu;
 };
 
 __device__ __forceinline__ V m_at(const MLane& L, float t) { return L.ro + scale(L.rd, t); }
@@ -309,14 +311,17 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
     const uint32_t max_steps = h.max_steps;
     V p;
     if (L.phase == M_MARCH) p = m_at(L, L.t);
-    else if (L.phase == M_COVER) p = m_at(L, 0.5f * ((L.t_prev + L.prev_r) + (L.t - L.sv_r)));
-    else p = m_at(L, L.t) + scale(tetra_k(L.tap), h.normal_h);
+    else if (L.phase == M_COVER) p = m_at(L, 0.5f * ((L.t_prev + L.prev_r) + (L.t - L.x1)));
+    else p = m_at(L, L.t) + scale(tetra_k(L.xu), h.normal_h);
     Field f = FP::eval(T, p);
     if (L.phase == M_TETRA) {
-        V kd = scale(tetra_k(L.tap), f.d);
-        L.g = L.tap == 0 ? kd : L.g + kd;
-        L.tap += 1;
-        if (L.tap == 4u) m_write(L, a, true, normalize(L.g), L.i);
+        V kd = scale(tetra_k(L.xu), f.d);
+        V g = L.xu == 0 ? kd : V{L.x0, L.x1, L.x2} + kd;
+        L.x0 = g.x;
+        L.x1 = g.y;
+        L.x2 = g.z;
+        L.xu += 1;
+        if (L.xu == 4u) m_write(L, a, true, normalize(g), L.i);
         return;
     }
     float d;
@@ -329,23 +334,23 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         e = h.eps * (1.0f + L.t * 0.5f) + h.lod_footprint * L.t;
         bool overlap_fail = (L.step > 0.0f && d < 0.0f) || L.step > radius + L.prev_r;
         if (overlap_fail && d > 0.0f) {  // check the gap midpoint first
-            L.sv_d = d;
-            L.sv_m = m;
-            L.sv_r = radius;
-            L.sv_e = e;
+            L.x0 = d;
+            L.xu = m;
+            L.x1 = radius;
+            L.x2 = e;
             L.phase = M_COVER;
             return;
         }
         if (overlap_fail) goto rollback;
     } else {  // M_COVER
         float gap_lo = L.t_prev + L.prev_r;
-        float gap_hi = L.t - L.sv_r;
+        float gap_hi = L.t - L.x1;
         L.phase = M_MARCH;
         if (!(f.d >= 0.5f * (gap_hi - gap_lo))) goto rollback;
-        d = L.sv_d;
-        m = L.sv_m;
-        radius = L.sv_r;
-        e = L.sv_e;
+        d = L.x0;
+        m = L.xu;
+        radius = L.x1;
+        e = L.x2;
     }
     // march.rs:173-206
     if (d < e) {
@@ -354,7 +359,7 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
             m_write(L, a, true, normal_dual(T.obj, h.n_objects, m_at(L, L.t)), L.i);
         } else {
             L.phase = M_TETRA;
-            L.tap = 0;
+            L.xu = 0;
         }
         return;
     }
