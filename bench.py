@@ -188,6 +188,7 @@ def bench_preview(ctx, torch, with_cpu):
 # over wgpu; README.md:15 and CHANGELOG.md:75-76), quoted beside ours on the same scene and loop.
 PUBLISHED_GPU_RENDER_FPS = 698.9
 PUBLISHED_RESOLUTION_FPS = {"960x540": 606.0, "1920x1080": 167.0, "2560x1440": 96.0, "3840x2160": 43.0}
+SWEEP_SHAPES = [{"block": 128, "tile_wlog": t, "unroll": 64, "min_blocks": 0} for t in (2, 3, 5)]
 
 
 def bench_published(ctx, stream, torch):
@@ -223,7 +224,9 @@ def bench_published(ctx, stream, torch):
         w, h = (int(v) for v in key.split("x"))
         s, cam = scenes.gpu_render_scene(w, h)
         cs = mm3e_cuda.CompiledScene(ctx, s)
-        cs.autotune(cam, spec_mode=cs.SPEC_AUTO, candidates=[best], repeats=1)
+        # per resolution: the 960x540 winner and the shapes that won at other sizes
+        cands = [best] + [c for c in SWEEP_SHAPES if c != best]
+        cs.autotune(cam, spec_mode=cs.SPEC_AUTO, candidates=cands, repeats=3)
         dev = torch.empty(w * h * 4, dtype=torch.uint8, device="cuda")
         for _ in range(3):
             cs.render_device(cam, abi.FB_RGBA8, dev.data_ptr(), dev.numel())
