@@ -483,9 +483,12 @@ struct SLane {
 };
 
 template <int TM>
-__device__ __forceinline__ bool s_start(SLane& S, LaneTape<TM>& LT, const WaveArgs& a) {
+__device__ __forceinline__ bool s_start(SLane& S, LaneTape<TM>& LT, const WaveArgs& a, uint32_t n_slots) {
+    // Work items run light-major (all hits' rays toward light 0, then light 1, ...), so a warp's
+    // rays share a direction and pass the same objects; results keep the slot-major layout.
     const uint32_t nl = a.lights_max;
-    uint32_t slot = S.item / nl, li = S.item % nl;
+    const uint32_t li = S.item / n_slots, slot = S.item - li * n_slots;
+    S.item = slot * nl + li;
     uint2 hm = a.b.h_m[slot];
     if (hm.x != NIL) {
         float4 hn4 = a.b.h_n[slot], o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
@@ -552,7 +555,8 @@ __device__ __forceinline__ void shadow_body(const WaveArgs& a) {
     } else {
         LT.p = a.job0.tape;
     }
-    const uint32_t n = item_count(a) * a.lights_max;
+    const uint32_t n_slots = item_count(a);
+    const uint32_t n = n_slots * a.lights_max;
     SLane S;
     S.item = NIL;
     bool retired = false;
@@ -560,7 +564,7 @@ __device__ __forceinline__ void shadow_body(const WaveArgs& a) {
         bool fresh;
         refill(S.item, retired, n, a.counter, fresh);
         if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
-        if (fresh && !s_start(S, LT, a)) continue;
+        if (fresh && !s_start(S, LT, a, n_slots)) continue;
 #pragma unroll 1
         for (int u = 0; u < UNROLL; ++u) {
             if (S.item == NIL) break;
