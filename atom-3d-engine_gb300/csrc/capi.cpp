@@ -1109,7 +1109,7 @@ int mm3e_render_film(mm3e_scene* s, const mm3e_camera* camera, float aperture_ra
     std::vector<float4> hdr(n), fg(n), hn(n), qd(n);
     std::vector<uint2> hm(n);
     CK(cudaMemcpyAsync(hdr.data(), s->buf.hdr, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(fg.data(), s->buf.bright, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(fg.data(), s->buf.fg, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
     // geometric AOVs: the centre pinhole ray of every pixel (film.rs:111-116)
     WaveArgs a;
     rc = march_centers(s, camera, s->d_tape, (uint32_t)s->low.blob.size(), false, &log, a);

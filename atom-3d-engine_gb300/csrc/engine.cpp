@@ -13,7 +13,7 @@ template <class T> cudaError_t grow(T** p, size_t n) {
 
 void PassBuffers::release() {
     void* ps[] = {qa_o, qa_d, qb_o, qb_d, qc_o, qc_d, qd_o, qd_d, h_n, h_m, occ, shadow, h_n1, h_m1, occ1, shadow1,
-                  h_n2, h_m2, occ2, shadow2, lvl, term, hdr, bright, blur, counters};
+                  h_n2, h_m2, occ2, shadow2, lvl, term, hdr, fg, blur, counters};
     for (void* p : ps) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
     for (int i = 0; i < MAX_LEVELS; ++i) {
@@ -49,7 +49,7 @@ cudaError_t PassBuffers::ensure(size_t need_cap, size_t need_lights, size_t need
     if ((e = grow(&qa_o, c)) || (e = grow(&qa_d, c)) || (e = grow(&qb_o, c)) || (e = grow(&qb_d, c)) ||
         (e = grow(&h_n, c)) || (e = grow(&h_m, c)) || (e = grow(&occ, c)) || (e = grow(&shadow, c * (l ? l : 1))) ||
         (e = grow(&lvl, c * 2 * (v ? v : 1))) || (e = grow(&term, c)) || (e = grow(&hdr, px)) ||
-        (e = grow(&bright, px)) || (e = grow(&blur, px)) || (e = grow(&counters, (size_t)N_COUNTERS))) {
+        (e = grow(&fg, px)) || (e = grow(&blur, px)) || (e = grow(&counters, (size_t)N_COUNTERS))) {
         release();
         return e;
     }
@@ -222,7 +222,7 @@ WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tun
     a.b.lvl = buf.lvl;
     a.b.term = buf.term;
     a.b.hdr = buf.hdr;
-    a.b.fg = buf.bright;
+    a.b.fg = buf.fg;
     a.film = plan.film ? 1u : 0u;
     return a;
 }
@@ -343,7 +343,6 @@ cudaError_t run_post(const PassPlan& plan, PassBuffers& buf, cudaStream_t s, int
     p.any_bloom = plan.bloom ? 1 : 0;
     p.grid_cap = (uint32_t)sm_count * 16u;
     p.hdr = buf.hdr;
-    p.bright = buf.bright;
     p.blur_h = buf.blur;
     return launch_post(p, s, log);
 }

@@ -51,7 +51,8 @@ struct PassBuffers {
     uint2* h_m2 = nullptr;
     float *occ2 = nullptr, *shadow2 = nullptr;
     float4 *lvl = nullptr, *term = nullptr;
-    float4 *hdr = nullptr, *bright = nullptr, *blur = nullptr;
+    float4 *hdr = nullptr, *blur = nullptr;
+    float4* fg = nullptr;  // film coverage / foreground per output pixel
     uint32_t* counters = nullptr;
     cudaStream_t aux = nullptr;   // reflection levels' marches
     cudaStream_t aux2 = nullptr;  // reflection levels' AO / shadows / shading
@@ -123,7 +124,7 @@ struct PassPlan {
     bool ao = false, shadows = false, bloom = false, post = true;
     bool clear_status = true;       // also clear the status word with the work counters
     const SpecKernels* spec = nullptr;  // scene-specialised march / shadow / AO (single job only)
-    bool film = false;              // resolve coverage + foreground (into buf.bright) too
+    bool film = false;              // resolve coverage + foreground (into buf.fg) too
     // Primary rays from queue a (count in this device word, outside buf.counters) instead of
     // the jobs' camera samples; sample k of the queue is queue entry k. The caller resolves.
     const uint32_t* queue0 = nullptr;

@@ -175,7 +175,8 @@ cudaError_t launch_gather_shade(const WaveArgs& a, float4* radiance, cudaStream_
 
 // Post stack (post.rs:36-115) over the output pixels of the jobs: bright-pass, separable
 // Gaussian (per-job weights), add, exposure, ACES, gamma, clamp; RGBA f32 or RGBA8 into
-// each job's `out`.
+// each job's `out`. With bloom it is two launches: bright-pass + horizontal blur into
+// `blur_h`, then vertical blur + resolve.
 struct PostArgs {
     FrameJob job0;
     const FrameJob* jobs;
@@ -185,8 +186,7 @@ struct PostArgs {
     int any_bloom;      // some job blooms
     uint32_t grid_cap;  // block limit of the grid-stride kernels (0: one thread per pixel)
     const float4* hdr;
-    float4* bright;
-    float4* blur_h;
+    float4* blur_h;  // horizontal blur of the bright-pass (one float4 per output pixel)
 };
 cudaError_t launch_post(const PostArgs& p, cudaStream_t s, LaunchLog* log);
 cudaError_t launch_pack_rgba8(const float4* src, uchar4* dst, size_t n, cudaStream_t s, LaunchLog* log);

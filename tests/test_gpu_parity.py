@@ -286,3 +286,33 @@ def test_deep_reflection_chain_parity(gpu_ctx):
     m = image_metrics(gpu, ref)
     print("mirrors_b7", json.dumps(m))
     assert m["psnr"] >= PSNR_MIN and m["within1_px"] >= 0.998, m
+
+
+# (width, height, aa, bloom radius): frames smaller than one launch tile (every tile shape leaves
+# padding lanes), one-pixel rows and columns, the widest frame the C ABI accepts, bloom kernels
+# wider than the frame (clamped borders on both sides of every tap) and radius 0 (the reference
+# blurs with radius 1 then, post.rs:78).
+EDGE_FRAMES = [(1, 1, 1, 12), (1, 9, 2, 12), (9, 1, 1, 12), (13, 7, 2, 40), (37, 21, 1, 0), (70, 3, 1, 1),
+               (16384, 1, 1, 12)]
+
+
+@pytest.mark.parametrize("w,h,aa,radius", EDGE_FRAMES)
+def test_edge_frame_sizes(gpu_ctx, w, h, aa, radius):
+    scene, cam = scenes.gallery_scene(w, h, aa=aa)
+    scene.post.bloom_radius = radius
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    gpu = compiled.render(cam, fmt=abi.FB_RGBA8)
+    ref = mm3e_cuda.to_rgba8(oracle_py.render(scene.desc(), cam))
+    assert gpu.shape == ref.shape == (h, w, 4)
+    diff = np.abs(gpu.astype(np.int16) - ref.astype(np.int16)).max(axis=-1)
+    print(w, h, aa, radius, "exact", float((diff == 0).mean()), "over 1 LSB", int((diff > 1).sum()))
+    assert int((diff > 1).sum()) <= max(1, int(0.001 * w * h))
+
+
+def test_empty_frames(gpu_ctx):
+    """A zero-width or zero-height frame renders to an empty framebuffer (no launch)."""
+    for w, h in ((0, 5), (5, 0), (0, 0)):
+        scene, cam = scenes.gallery_scene(w, h)
+        compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+        assert compiled.render(cam, fmt=abi.FB_RGBA8).shape == (h, w, 4)
+        assert compiled.render(cam).shape == (h, w, 4)
