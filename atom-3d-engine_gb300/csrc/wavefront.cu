@@ -324,6 +324,7 @@ __device__ __forceinline__ void blur4(const float* __restrict__ kw, int r, TAP t
     a1 = a1 + scale(v, k1);
     a2 = a2 + scale(v, k0);
     float c1 = k2, c2 = k1, c3 = k0;  // kw[j-1], kw[j-2], kw[j-3] at the top of step j
+#pragma unroll 4
     for (int j = 3; j <= 2 * r; ++j) {
         const float c0 = __ldg(kw + j);
         v = tap(j);

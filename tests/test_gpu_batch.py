@@ -74,6 +74,27 @@ def test_batch_device_outputs_graphs_and_small_waves():
         ctx.close()
 
 
+def test_batch_tiny_frames_and_wide_bloom():
+    """Jobs of one pixel, one row or one column, and bloom kernels wider than their frames, packed
+    next to each other: the post stack's blur windows then span several jobs, and every tap must
+    stay in its own job's row or column."""
+    ctx = mm3e_cuda.Context(0)
+    try:
+        items = []
+        for k, (w, h, r) in enumerate([(1, 1, 12), (9, 1, 40), (1, 9, 12), (13, 7, 1), (70, 3, 33), (5, 5, 0),
+                                       (2, 31, 32), (300, 2, 12)]):
+            s, cam = scenes.gallery_scene(w, h) if k % 2 == 0 else scenes.hero_scene(w, h, 2, 1)
+            s.post.bloom_radius = r
+            items.append((mm3e_cuda.CompiledScene(ctx, s), cam, w, h))
+        outs = [np.zeros((h, w, 4), np.uint8) for _, _, w, h in items]
+        jobs = ctx.make_jobs([(cs, cam, 0, 0, abi.FB_RGBA8, None, o) for (cs, cam, _, _), o in zip(items, outs)])
+        ctx.render_batch(jobs)
+        for (cs, cam, w, h), o in zip(items, outs):
+            assert np.array_equal(o, _plain(cs, cam)), f"batched frame differs from the plain frame ({w}x{h})"
+    finally:
+        ctx.close()
+
+
 def test_batch_resolution_override_matches_scene_compiled_at_that_size():
     ctx = mm3e_cuda.Context(0)
     try:
