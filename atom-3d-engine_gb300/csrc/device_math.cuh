@@ -64,6 +64,17 @@ MD V rot_t(const float* r, V v) {
     return V{r[0] * v.x + r[1] * v.y + r[2] * v.z, r[3] * v.x + r[4] * v.y + r[5] * v.z,
              r[6] * v.x + r[7] * v.y + r[8] * v.z};
 }
+// rot_t for r exactly the identity, with the same result bits for finite v. There x is
+// (1·vx + 0·vy) + 0·vz: the products 0·vy and 0·vz are zeros carrying the signs of vy and vz,
+// so x is vx except for the sign of a zero vx, which IEEE zero addition leaves negative only when
+// vy and vz are negative too. Adding the zero whose sign is that AND of signs reproduces it (and
+// likewise for y and z), one integer and one float operation a component instead of four.
+MD float zero_with_sign_and(float a, float b) {
+    return __int_as_float((__float_as_int(a) & __float_as_int(b)) & (int)0x80000000u);
+}
+MD V rot_t_identity(V v) {
+    return V{v.x + zero_with_sign_and(v.y, v.z), v.y + zero_with_sign_and(v.x, v.z), v.z + zero_with_sign_and(v.x, v.y)};
+}
 
 struct Field {
     float d;
@@ -276,7 +287,11 @@ static __device__ __noinline__ float csg_eval(const DevCsgOp* op, V p) {
 
 // Object::local_point (lib.rs:400-419)
 MD V local_point(const DevObject& o, V p) {
-    V l = scale(rot_t(o.rot, p - ld3(o.pos)), o.inv);
+    const V d = p - ld3(o.pos);
+    V r;
+    if (o.flags & OF_ROT_IDENTITY) r = rot_t_identity(d);  // folded away in a specialised field
+    else r = rot_t(o.rot, d);
+    V l = scale(r, o.inv);
     uint32_t f = o.flags;
     if (f & OF_POINT_OPS) {
         if (f & OF_ANY_MIRROR) {

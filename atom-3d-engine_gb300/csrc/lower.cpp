@@ -659,6 +659,10 @@ int lower_scene(const mm3e_scene_desc& d0, const mm3e_dyn_sphere* dyn, size_t n_
         // takes the hexagon's apothem where its corners reach 2/sqrt(3) times as far.
         if (o.prim == MM3E_PRIM_ELLIPSOID || o.prim == MM3E_PRIM_OCTAHEDRON || o.prim == MM3E_PRIM_HEX_PRISM)
             f |= OF_NONCONS;
+        {
+            static const float ident[9] = {1.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+            if (std::memcmp(o.rot, ident, sizeof(ident)) == 0) f |= OF_ROT_IDENTITY;  // bitwise: no -0 entries
+        }
         f |= (o.combine & 3u) << 16;  // combine mode, read by the dual-number normal
         g.flags = f;
         g.aux = o.prim == MM3E_PRIM_CSG ? csg_offset[o.id] : (d.n_volumes ? o.id % d.n_volumes : 0);

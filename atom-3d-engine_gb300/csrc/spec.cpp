@@ -178,10 +178,14 @@ WeakBound weak_bound(const DevObject& o) {
 }
 
 // The weak-bound cull of a member: true when its field cannot reach down to bd.
+// The bound only takes the norm of the local point, so an identity rotation is left out (the
+// skipped products could only change the signs of zero coordinates).
 std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
     std::ostringstream os;
-    os << "weak_beyond(scale(rot_t(RO, p - V{" << fbits(o.pos[0]) << ", " << fbits(o.pos[1]) << ", " << fbits(o.pos[2])
-       << "}), " << fbits(o.inv) << "), " << (w.axis[0] ? "true" : "false") << ", " << (w.axis[1] ? "true" : "false")
+    const std::string d =
+        "p - V{" + fbits(o.pos[0]) + ", " + fbits(o.pos[1]) + ", " + fbits(o.pos[2]) + "}";
+    os << "weak_beyond(scale(" << ((o.flags & OF_ROT_IDENTITY) ? d : "rot_t(RO, " + d + ")") << ", " << fbits(o.inv)
+       << "), " << (w.axis[0] ? "true" : "false") << ", " << (w.axis[1] ? "true" : "false")
        << ", " << (w.axis[2] ? "true" : "false") << ", " << fbits(w.R) << ", " << fbits(w.c) << ", " << fbits(o.scale)
        << ", " << fbits(w.post) << ", bd)";
     return os.str();
@@ -338,7 +342,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 // the non-conservative ones) skip their exact field where their weak bound clears bd
                 const WeakBound wb = cull ? WeakBound{} : weak_bound(o);
                 if (wb.ok) {
-                    os << "            const float RO[9] = " << farr(o.rot, 9) << ";\n";
+                    if (!(o.flags & OF_ROT_IDENTITY)) os << "            const float RO[9] = " << farr(o.rot, 9) << ";\n";
                     exact = "if (!" + weak_cull_expr(o, wb) + ") {\n            " + exact + "            }\n";
                 }
                 if (o.flags & OF_BOUND) {

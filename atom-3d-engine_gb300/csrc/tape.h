@@ -36,6 +36,7 @@ enum : uint32_t {
     OF_ONION = 1u << 8,
     OF_BOUND = 1u << 9,
     OF_NONCONS = 1u << 10,  // ellipsoid / octahedron / hex prism: field can undercut the bounding sphere
+    OF_ROT_IDENTITY = 1u << 11,  // rotation exactly the identity (1 on the diagonal, +0 elsewhere)
     OF_ANY_MIRROR = OF_MIRROR_X | OF_MIRROR_Y | OF_MIRROR_Z,
     OF_POINT_OPS = OF_ANY_MIRROR | OF_ELONGATE | OF_REPEAT | OF_TWIST | OF_BEND,
 };

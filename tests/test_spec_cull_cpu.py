@@ -110,3 +110,33 @@ def test_cluster_spheres_enclose_members_and_cull_safely():
                 for c, r in members:
                     assert (exact_lower(p[skip], c, r) > bd).all()
     assert n_clusters >= 2
+
+
+def _zero_with_sign_and(a, b):
+    bits = (a.view(np.uint32) & b.view(np.uint32)) & np.uint32(0x80000000)
+    return bits.view(np.float32)
+
+
+def test_identity_rotation_shortcut_is_bit_exact():
+    """An object whose rotation is exactly the identity skips the rotation's multiplications
+    (rot_t_identity in device_math.cuh): x = vx + (a zero with the sign of vy AND vz), and so on.
+    Checked bit for bit against the full product r[0]·vx + r[1]·vy + r[2]·vz of the identity in
+    binary32 (vec.rs:125-127 order) on signed zeros, subnormals and ordinary values."""
+    F = np.float32
+    special = np.array([0.0, -0.0, 1e-45, -1e-45, 1.5e-39, -2.5e-39, 1.0, -1.0, 3.25, -7.5e3, 6e37, -6e37], F)
+    rng = np.random.default_rng(5)
+    rand = (rng.standard_normal(4000) * 10.0 ** rng.integers(-6, 6, 4000)).astype(F)
+    vals = np.concatenate([special, rand])
+    g = np.array(np.meshgrid(special, special, special, indexing="ij")).reshape(3, -1)
+    v = np.concatenate([g, rng.choice(vals, (3, 20000))], axis=1).astype(F)
+    vx, vy, vz = v
+    one, zero = F(1.0), F(0.0)
+    full = [(one * vx + zero * vy) + zero * vz, (zero * vx + one * vy) + zero * vz, (zero * vx + zero * vy) + one * vz]
+    short = [vx + _zero_with_sign_and(vy, vz), vy + _zero_with_sign_and(vx, vz), vz + _zero_with_sign_and(vx, vy)]
+    for f, s in zip(full, short):
+        assert f.dtype == s.dtype == np.float32
+        assert np.array_equal(f.view(np.uint32), s.view(np.uint32))
+    # the generator drops the rotation from an identity member's weak-bound test and the RO table
+    scene, _ = scenes.gallery_scene(32, 18)
+    src = mm3e_cuda.spec_source(scene)
+    assert "weak_beyond(scale(p - V{" in src

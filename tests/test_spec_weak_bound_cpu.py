@@ -17,7 +17,7 @@ import pytest
 
 import mm3e_cuda
 import oracle_py
-from mm3e_cuda.scene import Material, Object, Prim, Scene, Transform, mat3_from_euler
+from mm3e_cuda.scene import IDENTITY_ROT, Material, Object, Prim, Scene, Transform, mat3_from_euler
 
 F = np.float32
 
@@ -60,9 +60,13 @@ def _scene(obj, with_anchor):
 
 def _weak_constants(src):
     m = re.search(r"const float RO\[9\] = \{([^}]*)\};\s*\n\s*(?:float lower = [^\n]*\n\s*if[^\n]*\n\s*)?", src)
-    assert m, "no weak-bound cull emitted"
-    rot = np.array([_f(h) for h in re.findall(r"0x([0-9a-f]+)u", m.group(1))], F)
-    call = re.search(r"weak_beyond\(scale\(rot_t\(RO, p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}\), " + _HEX +
+    if m:
+        rot = np.array([_f(h) for h in re.findall(r"0x([0-9a-f]+)u", m.group(1))], F)
+        local = r"rot_t\(RO, p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}\)"
+    else:  # an identity rotation is left out of the test
+        rot = np.eye(3, dtype=F).reshape(-1)
+        local = r"p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}"
+    call = re.search(r"weak_beyond\(scale\(" + local + ", " + _HEX +
                      r"\), (true|false), (true|false), (true|false), " + ", ".join([_HEX] * 4) + r", bd\)", src)
     assert call, "no weak_beyond call"
     g = call.groups()
@@ -87,11 +91,12 @@ def _bound(pts, rot, pos, inv, axes, R, c, scl, post):
     return F(lb - F(F(F(n + R) * scl) * F(0.0009765625)))
 
 
+@pytest.mark.parametrize("rotated", [True, False])
 @pytest.mark.parametrize("mod", list(MODS))
 @pytest.mark.parametrize("prim", list(PRIMS))
-def test_weak_bound_holds(prim, mod):
-    rng = np.random.default_rng(abs(hash((prim, mod))) % (1 << 32))
-    rot = mat3_from_euler(0.3, -0.7, 1.1)
+def test_weak_bound_holds(prim, mod, rotated):
+    rng = np.random.default_rng(abs(hash((prim, mod, rotated))) % (1 << 32))
+    rot = mat3_from_euler(0.3, -0.7, 1.1) if rotated else IDENTITY_ROT
     base = Object(PRIMS[prim], Transform((0.4, 1.2, -0.6), rot, 1.3), 0)
     obj = MODS[mod](base)
     src = mm3e_cuda.spec_source(_scene(obj, True))
