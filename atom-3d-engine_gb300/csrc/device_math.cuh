@@ -184,6 +184,15 @@ MD bool weak_beyond(V l, bool ax, bool ay, bool az, float R, float c, float scl,
     float lb = (n - R) * c * scl - post;
     return bd >= 0.0f && lb - (n + R) * scl * 0.0009765625f > bd;
 }
+// weak_beyond without the square root. In exact arithmetic its test is n > (bd + A) / K with
+// K = scl (c - 2^-10) > 0 and A = post + R scl (c + 2^-10) > 0; the generator passes A rounded up
+// and B = (1 + 2^-17) / K rounded up, so t = (bd + A) B exceeds the exact threshold by more than
+// the few binary32 roundings of t * t and n2 can take back, and n2 > t * t implies it.
+MD bool weak_beyond_sq(V l, bool ax, bool ay, bool az, float A, float B, float bd) {
+    float n2 = (ax ? l.x * l.x : 0.0f) + (ay ? l.y * l.y : 0.0f) + (az ? l.z * l.z : 0.0f);
+    float t = (bd + A) * B;
+    return bd >= 0.0f && n2 > t * t;
+}
 
 // ---- tape view ----
 struct Tape {

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <sstream>
 
@@ -177,17 +178,36 @@ WeakBound weak_bound(const DevObject& o) {
     return w;
 }
 
+// The nearest binary32 value at or above x.
+float float_at_or_above(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+
 // The weak-bound cull of a member: true when its field cannot reach down to bd.
 // The bound only takes the norm of the local point, so an identity rotation is left out (the
-// skipped products could only change the signs of zero coordinates).
+// skipped products could only change the signs of zero coordinates). With positive constants the
+// test compares squared norms (weak_beyond_sq); a trailing comment keeps the bound's R, c, scale
+// and post for the soundness tests.
 std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
     std::ostringstream os;
     const std::string d =
         "p - V{" + fbits(o.pos[0]) + ", " + fbits(o.pos[1]) + ", " + fbits(o.pos[2]) + "}";
-    os << "weak_beyond(scale(" << ((o.flags & OF_ROT_IDENTITY) ? d : "rot_t(RO, " + d + ")") << ", " << fbits(o.inv)
-       << "), " << (w.axis[0] ? "true" : "false") << ", " << (w.axis[1] ? "true" : "false")
-       << ", " << (w.axis[2] ? "true" : "false") << ", " << fbits(w.R) << ", " << fbits(w.c) << ", " << fbits(o.scale)
-       << ", " << fbits(w.post) << ", bd)";
+    const std::string local = "scale(" + ((o.flags & OF_ROT_IDENTITY) ? d : "rot_t(RO, " + d + ")") + ", " +
+                              fbits(o.inv) + "), " + (w.axis[0] ? "true" : "false") + ", " +
+                              (w.axis[1] ? "true" : "false") + ", " + (w.axis[2] ? "true" : "false");
+    const double eps = 1.0 / 1024.0;
+    const double K = (double)o.scale * ((double)w.c - eps);
+    const double A = (double)w.post + (double)w.R * (double)o.scale * ((double)w.c + eps);
+    const float Af = float_at_or_above(A), Bf = float_at_or_above((1.0 + 1.0 / 131072.0) / K);
+    if (K > 0.0 && A > 0.0 && std::isfinite(Af) && std::isfinite(Bf)) {
+        os << "weak_beyond_sq(" << local << ", " << fbits(Af) << ", " << fbits(Bf) << ", bd) /* weak bound R c scale post: "
+           << fbits(w.R) << " " << fbits(w.c) << " " << fbits(o.scale) << " " << fbits(w.post) << " */";
+    } else {
+        os << "weak_beyond(" << local << ", " << fbits(w.R) << ", " << fbits(w.c) << ", " << fbits(o.scale) << ", "
+           << fbits(w.post) << ", bd)";
+    }
     return os.str();
 }
 
@@ -299,9 +319,23 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
         os << "    {  // segment " << s << "\n";
         if (sg.kind == SEG_ONE) {
             const DevObject& o = obj[sg.a];
+            // A bounded union or smooth-union object whose sphere distance clears the slack and
+            // the accumulated field (by k more, with a 1% margin, for the smooth union, whose blend
+            // weight is then exactly 1) leaves the accumulator as it is: the squared pre-test
+            // skips the segment there. Not for a zero accumulator (the blend's result could carry
+            // the other sign of zero) or one that is not finite.
+            const bool smooth = sg.b == 1u && o.k > 0.0f;
+            const bool skip = seeded && (o.flags & OF_BOUND) && (sg.b == 0u || sg.b == 1u);
+            if (skip) {
+                const std::string thr = smooth ? "acc.d + " + fbits((float)((double)o.k * 1.01)) : std::string("acc.d");
+                os << "        const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
+                   << fbits(o.bc[2]) << "});\n        if (!(acc.d < INF" << (smooth ? " && acc.d != 0.0f" : "")
+                   << " && far_beyond(d2, fmaxf(" << thr << ", " << slack << "), " << fbits(o.br) << "))) {\n";
+            }
             os << "        Field f;\n        bool sub = false;\n";
             if (o.flags & OF_BOUND)
-                os << "        {\n            float lower = " << lower_expr(o) << ";\n"
+                os << "        {\n            float lower = "
+                   << (skip ? "sqrtf(d2) - " + fbits(o.br) : lower_expr(o)) << ";\n"
                    << "            if (lower > " << slack << ") {\n                f = Field{lower, " << o.mat
                    << "u};\n                sub = true;\n            }\n        }\n";
             os << "        if (!sub) f = obj_" << sg.a << "(T, p);\n";
@@ -316,6 +350,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             };
             if (comb_exact == sg.b) os << "        " << fold(sg.b) << "\n";
             else os << "        if (sub) { " << fold(sg.b) << " } else { " << fold(comb_exact) << " }\n";
+            if (skip) os << "        }\n";
         } else if (sg.kind == SEG_LINEAR) {
             // The fold is an argmin with lowest-index ties (the seed, index -1, wins its ties), and
             // a culled member cannot reach the minimum, so any member order gives the same
@@ -351,14 +386,18 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                            << ", " << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, bd, " << fbits(o.br)
                            << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n";
                     } else {
-                        os << "            float lower = " << lower_expr(o) << ";\n";
+                        // beyond both the slack and bd, the member's value is its sphere distance and
+                        // it cannot win: the squared pre-test skips the square root there
+                        os << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
+                           << ", " << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, fmaxf(bd, " << slack << "), "
+                           << fbits(o.br) << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n";
                     }
                     if (cull) os << "            if (!(lower > bd)) {\n";
                     os << "            if (lower > " << slack << ") {\n                if (lower < bd || (lower == bd && "
                        << i << " < bi)) {\n                    bd = lower;\n                    bi = " << i
                        << ";\n                    bm = " << o.mat << "u;\n                    bnc = false;\n"
                        << "                }\n            } else {\n            " << exact << "            }\n";
-                    if (cull) os << "            }\n            }\n";
+                    os << (cull ? "            }\n            }\n" : "            }\n");
                 } else {
                     os << "            " << exact;
                 }

@@ -139,4 +139,42 @@ def test_identity_rotation_shortcut_is_bit_exact():
     # the generator drops the rotation from an identity member's weak-bound test and the RO table
     scene, _ = scenes.gallery_scene(32, 18)
     src = mm3e_cuda.spec_source(scene)
-    assert "weak_beyond(scale(p - V{" in src
+    assert "weak_beyond_sq(scale(p - V{" in src
+
+
+def _smooth_union_d(a, b, k):
+    """sdf.rs:152-160 distance in binary32 (a, b arrays, k > 0)."""
+    h = F(F(0.5) + F(F(F(0.5) * F(b - a)) / k))
+    h = np.minimum(np.maximum(h, F(0)), F(1)).astype(F)
+    one_h = F(F(1) - h)
+    return F(F(F(b * one_h) + F(a * h)) - F(F(k * h) * one_h)), h
+
+
+def test_far_smooth_and_union_segments_leave_the_accumulator():
+    """A specialised smooth-union (or union) segment is skipped where its sphere distance clears
+    max(acc + 1.01 k, slack) by the squared pre-test (acc finite and non-zero): there the blend
+    weight is exactly 1, and the blend returns the accumulator's distance bit for bit with its
+    material (for a union, the accumulator wins outright)."""
+    rng = np.random.default_rng(23)
+    slack = F(0.4)
+    for _ in range(60):
+        c = rng.uniform(-20, 20, 3).astype(F)
+        r = F(rng.uniform(0.05, 3.0))
+        k = F(rng.choice([0.01, 0.3, 1.0, 2.5]))
+        acc = np.concatenate([rng.uniform(-5, 5, 8000), rng.uniform(-150, 150, 6000),
+                              rng.uniform(1e-6, 1e-3, 6000)]).astype(F)
+        acc[acc == 0] = F(1e-3)
+        thr = np.maximum(F(acc + F(k * 1.01)), slack).astype(F)
+        p = _points_near(rng, c, float(rng.uniform(0.5, 40.0)), 20000)
+        p = (c + (p - c) * rng.uniform(0.0, 3.0, (20000, 1))).astype(F)
+        d2 = length_sq((p - c).astype(F))
+        skip = far_beyond(d2, thr, r)
+        lower = exact_lower(p, c, r)
+        assert skip.mean() > 0.05
+        assert (lower[skip] > slack).all()  # the slack substitute is the member's value there
+        dist, h = _smooth_union_d(acc, lower, k)
+        assert (h[skip] == F(1)).all()
+        assert np.array_equal(dist[skip].view(np.uint32), acc[skip].view(np.uint32))
+        # the union's skip (threshold max(acc, slack)) keeps the accumulator: acc <= lower
+        uskip = far_beyond(d2, np.maximum(acc, slack).astype(F), r)
+        assert (acc[uskip] <= lower[uskip]).all()

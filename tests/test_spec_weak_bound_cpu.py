@@ -59,26 +59,35 @@ def _scene(obj, with_anchor):
 
 
 def _weak_constants(src):
-    m = re.search(r"const float RO\[9\] = \{([^}]*)\};\s*\n\s*(?:float lower = [^\n]*\n\s*if[^\n]*\n\s*)?", src)
+    """(rot, pos, inv, axes, R, c, scale, post, sq) of the one weak-bound cull in `src`; sq holds the
+    (A, B) constants of the square-root-free form, or None for the plain form."""
+    m = re.search(r"const float RO\[9\] = \{([^}]*)\};", src)
     if m:
         rot = np.array([_f(h) for h in re.findall(r"0x([0-9a-f]+)u", m.group(1))], F)
         local = r"rot_t\(RO, p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}\)"
     else:  # an identity rotation is left out of the test
         rot = np.eye(3, dtype=F).reshape(-1)
         local = r"p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}"
-    call = re.search(r"weak_beyond\(scale\(" + local + ", " + _HEX +
-                     r"\), (true|false), (true|false), (true|false), " + ", ".join([_HEX] * 4) + r", bd\)", src)
-    assert call, "no weak_beyond call"
-    g = call.groups()
+    head = r"\(scale\(" + local + ", " + _HEX + r"\), (true|false), (true|false), (true|false), "
+    sq = re.search(r"weak_beyond_sq" + head + _HEX + ", " + _HEX + r", bd\) /\* weak bound R c scale post: " +
+                   " ".join([_HEX] * 4), src)
+    if sq:
+        g = sq.groups()
+        consts = (_f(g[9]), _f(g[10]), _f(g[11]), _f(g[12]))
+        ab = (_f(g[7]), _f(g[8]))
+    else:
+        call = re.search(r"weak_beyond" + head + ", ".join([_HEX] * 4) + r", bd\)", src)
+        assert call, "no weak-bound cull emitted"
+        g = call.groups()
+        consts = tuple(_f(x) for x in g[7:11])
+        ab = None
     pos = np.array([_f(g[0]), _f(g[1]), _f(g[2])], F)
     inv = _f(g[3])
     axes = [g[4] == "true", g[5] == "true", g[6] == "true"]
-    R, c, scl, post = (_f(x) for x in g[7:11])
-    return rot, pos, inv, axes, R, c, scl, post
+    return (rot, pos, inv, axes) + consts + (ab,)
 
 
-def _bound(pts, rot, pos, inv, axes, R, c, scl, post):
-    """weak_beyond's bound minus its margin, in binary32 with the device's operation order."""
+def _local_n2(pts, rot, pos, inv, axes):
     d = (pts - pos).astype(F)
     l = np.stack([F(F(F(rot[3 * k] * d[:, 0]) + F(rot[3 * k + 1] * d[:, 1])) + F(rot[3 * k + 2] * d[:, 2]))
                   for k in range(3)], axis=1)
@@ -86,7 +95,12 @@ def _bound(pts, rot, pos, inv, axes, R, c, scl, post):
     n2 = np.zeros(len(pts), F)
     for a in range(3):
         n2 = F(n2 + (F(l[:, a] * l[:, a]) if axes[a] else F(0)))
-    n = np.sqrt(n2).astype(F)
+    return n2
+
+
+def _bound(pts, rot, pos, inv, axes, R, c, scl, post):
+    """weak_beyond's bound minus its margin, in binary32 with the device's operation order."""
+    n = np.sqrt(_local_n2(pts, rot, pos, inv, axes)).astype(F)
     lb = F(F(F(F(n - R) * c) * scl) - post)
     return F(lb - F(F(F(n + R) * scl) * F(0.0009765625)))
 
@@ -107,7 +121,7 @@ def test_weak_bound_holds(prim, mod, rotated):
         assert not weak  # the exact sphere test covers it
         return
     assert weak
-    consts = _weak_constants(src)
+    *consts, ab = _weak_constants(src)
     d = rng.standard_normal((40000, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     r = rng.uniform(0.0, 6.0, 40000) ** 1.5
@@ -118,3 +132,21 @@ def test_weak_bound_holds(prim, mod, rotated):
     assert live.mean() > 0.2  # the bound is not vacuous
     bad = live & ~(field >= lb)
     assert not bad.any(), (pts[bad][:3], field[bad][:3], lb[bad][:3])
+    if ab is None:
+        return
+    # the square-root-free form: constants no smaller than the exact ones, and on thresholds bd
+    # around the bound every cull it makes is one the plain form makes, with the field above bd
+    rot, pos, inv, axes, R, c, scl, post = consts
+    A, B = ab
+    K = float(scl) * (float(c) - 2.0 ** -10)
+    assert K > 0 and A >= float(post) + float(R) * float(scl) * (float(c) + 2.0 ** -10)
+    assert B >= (1.0 + 2.0 ** -17) / K
+    n2 = _local_n2(pts, rot, pos, inv, axes)
+    for scale_bd in (0.5, 0.9, 0.99, 0.999, 1.0, 1.001):
+        bd = np.maximum(lb * F(scale_bd), F(0)).astype(F)
+        t = F(F(bd + A) * B)
+        sq = n2 > F(t * t)
+        assert not (sq & ~(lb > bd)).any()
+        assert not (sq & ~(field > bd)).any()
+    bd = (lb * F(0.98)).astype(F)
+    assert (n2 > F(F(F(bd + A) * B) ** 2))[lb > 0.1].mean() > 0.5  # and it still culls
