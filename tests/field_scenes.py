@@ -26,3 +26,29 @@ def noncons_scene(seed, width=64, height=36):
         s.objects.append(Object(prim, Transform(pos, rot, float(rng.uniform(0.7, 1.3))), 1 + k % 2))
     cam = look_at((0.0, 3.5, -9.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), radians(50.0))
     return s, cam
+
+
+def smooth_chain_scene(seed, width=64, height=36):
+    """Plain-union runs interleaved with smooth-union objects of blend radii from 0 to 1.2 and a
+    subtraction, identity and rotated transforms mixed, on a plane: the specialised field's
+    segment skip (a far smooth-union object leaves the accumulator as it is) meets accumulators of
+    both signs, including points inside the union (AO and normal taps)."""
+    rng = np.random.default_rng(seed)
+    s = Scene(width, height)
+    s.materials = [Material((0.8, 0.8, 0.8)), Material((0.7, 0.3, 0.2)), Material((0.2, 0.5, 0.7))]
+    s.objects = [Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, 0)]
+    ks = [0.0, 0.05, 0.3, 0.7, 1.2]
+    for k in range(16):
+        pos = tuple(float(v) for v in rng.uniform([-4, 0.3, -3], [4, 2.0, 3]))
+        rot = mat3_from_euler(*rng.uniform(-1.2, 1.2, 3)) if k % 3 else (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
+        prim = Prim.sphere(float(rng.uniform(0.3, 0.9))) if k % 2 else Prim.box(tuple(float(v) for v in rng.uniform(0.2, 0.7, 3)))
+        o = Object(prim, Transform(pos, rot, 1.0), 1 + k % 2)
+        if k % 4 == 1:
+            o = o.smooth(ks[(k // 4) % len(ks)])
+        elif k == 10:
+            o = o.subtract()
+        elif k % 4 == 3:
+            o = o.smooth(ks[(k // 4 + 2) % len(ks)])
+        s.objects.append(o)
+    cam = look_at((0.5, 3.0, -8.5), (0.0, 0.8, 0.0), (0.0, 1.0, 0.0), radians(55.0))
+    return s, cam

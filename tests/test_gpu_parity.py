@@ -15,7 +15,7 @@ import mm3e_cuda
 import oracle_py
 from mm3e_cuda import abi, scenes
 from mm3e_cuda.scene import DynSphere, GiVolume
-from field_scenes import noncons_scene
+from field_scenes import noncons_scene, smooth_chain_scene
 from parity import hit_metrics, image_metrics
 
 pytestmark = pytest.mark.gpu
@@ -247,6 +247,17 @@ def test_noncons_scene_parity(gpu_ctx):
     compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
     _check_image("noncons", gpu, ref)
     _check_hits("noncons", compiled, scene, cam)
+
+
+def test_smooth_chain_scene_parity(gpu_ctx):
+    """Smooth-union objects of several blend radii between union runs: the interpreter and the
+    specialised field (whose far smooth segments are skipped) both against the oracle."""
+    scene, cam = smooth_chain_scene(5, 160, 90)
+    compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image("smooth_chain", gpu, ref)
+    _check_hits("smooth_chain", compiled, scene, cam)
+    compiled.specialize(compiled.SPEC_ALWAYS)
+    _check_image("smooth_chain_spec", compiled.render(cam, fmt=abi.FB_RGBA8), ref)
 
 
 def _mirror_scene(bounces, shadows=True):

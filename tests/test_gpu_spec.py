@@ -9,7 +9,7 @@ import pytest
 
 import mm3e_cuda
 from mm3e_cuda import abi, scenes
-from field_scenes import noncons_scene
+from field_scenes import noncons_scene, smooth_chain_scene
 from mm3e_cuda.scene import DynSphere
 
 pytestmark = pytest.mark.gpu
@@ -23,6 +23,7 @@ SCENES = {
     "procedural0": lambda: scenes.procedural_scene(0, 96, 64),
     "procedural4": lambda: scenes.procedural_scene(4, 96, 64),
     "noncons": lambda: noncons_scene(21, 160, 90),
+    "smooth_chain": lambda: smooth_chain_scene(5, 160, 90),
 }
 
 
