@@ -371,6 +371,26 @@ struct NodeStack {
 // (their spheres enclose its sphere), so a pruning best would already be below the winner.
 MD bool noncons_undercut(float d, float lower, float r) { return !(d > lower + (r + fabsf(lower)) * 0.0009765625f); }
 
+// Whether a bounded ONE segment leaves a finite accumulator `acc` exactly as it is, from its
+// object's squared sphere distance d2 alone: past the slack the object's value is its sphere
+// distance `lower`, and a union keeps acc when acc <= lower, a smooth union (k > 0) when
+// lower - acc >= k with a 1% margin (the blend weight is then exactly 1 and the blend returns acc
+// bit for bit, unless acc is a zero), a subtraction when -lower < acc. far_beyond proves
+// lower > max(threshold, slack) in binary32 without the square root.
+MD bool one_keeps_acc(uint32_t comb, float k, float acc, float d2, float r, float slack) {
+    if (!(acc < __int_as_float(0x7f800000) && acc > -__int_as_float(0x7f800000))) return false;
+    float thr;
+    if (comb == 1u && k > 0.0f) {
+        if (acc == 0.0f) return false;
+        thr = acc + k * 1.01f;
+    } else if (comb == 2u) {
+        thr = -acc;
+    } else {
+        thr = acc;
+    }
+    return far_beyond(d2, fmaxf(thr, slack), r);
+}
+
 // WorldPlan::eval (accel.rs:209-252) with Bvh::query (accel.rs:79-119) and
 // WorldPlan::contrib (accel.rs:187-207). The plan is walked as a generator so that the exact
 // object field has a single call site: each outer iteration advances the plan to the next
@@ -408,7 +428,13 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
                     const DevObject& o = T.obj[sg.a];
                     one = sg.a;
                     if (o.flags & OF_BOUND) {
-                        float lower = length(p - ld3(o.bc)) - o.br;
+                        const float d2 = length_sq(p - ld3(o.bc));
+                        if (seeded && one_keeps_acc(sg.b, o.k, acc.d, d2, o.br, slack)) {
+                            s += 1;
+                            step = true;
+                            break;
+                        }
+                        float lower = sqrtf(d2) - o.br;
                         if (lower > slack) {
                             Field f{lower, o.mat};
                             if (!seeded) acc = f;

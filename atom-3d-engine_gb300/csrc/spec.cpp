@@ -319,18 +319,22 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
         os << "    {  // segment " << s << "\n";
         if (sg.kind == SEG_ONE) {
             const DevObject& o = obj[sg.a];
-            // A bounded union or smooth-union object whose sphere distance clears the slack and
-            // the accumulated field (by k more, with a 1% margin, for the smooth union, whose blend
-            // weight is then exactly 1) leaves the accumulator as it is: the squared pre-test
-            // skips the segment there. Not for a zero accumulator (the blend's result could carry
-            // the other sign of zero) or one that is not finite.
+            // A bounded object whose sphere distance clears the slack and a threshold set by the
+            // accumulated field leaves the accumulator as it is (one_keeps_acc in device_math.cuh:
+            // the accumulator for a union, the accumulator plus k with a 1% margin for a smooth
+            // union, whose blend weight is then exactly 1, minus the accumulator for a
+            // subtraction): the squared pre-test skips the segment there. Never for an
+            // accumulator that is not finite, nor a zero one under a smooth union.
             const bool smooth = sg.b == 1u && o.k > 0.0f;
-            const bool skip = seeded && (o.flags & OF_BOUND) && (sg.b == 0u || sg.b == 1u);
+            const bool skip = seeded && (o.flags & OF_BOUND) && sg.b <= 2u;
             if (skip) {
-                const std::string thr = smooth ? "acc.d + " + fbits((float)((double)o.k * 1.01)) : std::string("acc.d");
+                const std::string thr = smooth      ? "acc.d + " + fbits((float)((double)o.k * 1.01))
+                                        : sg.b == 2u ? std::string("-acc.d")
+                                                     : std::string("acc.d");
                 os << "        const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
-                   << fbits(o.bc[2]) << "});\n        if (!(acc.d < INF" << (smooth ? " && acc.d != 0.0f" : "")
-                   << " && far_beyond(d2, fmaxf(" << thr << ", " << slack << "), " << fbits(o.br) << "))) {\n";
+                   << fbits(o.bc[2]) << "});\n        if (!(acc.d < INF && acc.d > -INF"
+                   << (smooth ? " && acc.d != 0.0f" : "") << " && far_beyond(d2, fmaxf(" << thr << ", " << slack
+                   << "), " << fbits(o.br) << "))) {\n";
             }
             os << "        Field f;\n        bool sub = false;\n";
             if (o.flags & OF_BOUND)

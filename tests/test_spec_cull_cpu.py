@@ -150,11 +150,12 @@ def _smooth_union_d(a, b, k):
     return F(F(F(b * one_h) + F(a * h)) - F(F(k * h) * one_h)), h
 
 
-def test_far_smooth_and_union_segments_leave_the_accumulator():
-    """A specialised smooth-union (or union) segment is skipped where its sphere distance clears
-    max(acc + 1.01 k, slack) by the squared pre-test (acc finite and non-zero): there the blend
-    weight is exactly 1, and the blend returns the accumulator's distance bit for bit with its
-    material (for a union, the accumulator wins outright)."""
+def test_far_one_segments_leave_the_accumulator():
+    """A smooth-union segment is skipped where its sphere distance clears max(acc + 1.01 k, slack)
+    by the squared pre-test (acc finite and non-zero): there the blend weight is exactly 1, and
+    the blend returns the accumulator's distance bit for bit with its material. A union segment
+    (threshold acc) keeps the accumulator outright, a subtraction (threshold -acc) keeps it as
+    max(acc, -lower). Both the specialised field and the interpreter (one_keeps_acc) apply it."""
     rng = np.random.default_rng(23)
     slack = F(0.4)
     for _ in range(60):
@@ -178,3 +179,8 @@ def test_far_smooth_and_union_segments_leave_the_accumulator():
         # the union's skip (threshold max(acc, slack)) keeps the accumulator: acc <= lower
         uskip = far_beyond(d2, np.maximum(acc, slack).astype(F), r)
         assert (acc[uskip] <= lower[uskip]).all()
+        # the subtraction's skip (threshold max(-acc, slack)): max(acc, -lower) is acc, bit for bit
+        sskip = far_beyond(d2, np.maximum(-acc, slack).astype(F), r)
+        assert sskip.mean() > 0.05
+        sub = np.fmax(acc, -lower).astype(F)
+        assert np.array_equal(sub[sskip].view(np.uint32), acc[sskip].view(np.uint32))
