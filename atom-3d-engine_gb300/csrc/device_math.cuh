@@ -373,16 +373,16 @@ MD bool noncons_undercut(float d, float lower, float r) { return !(d > lower + (
 
 // Whether a bounded ONE segment leaves a finite accumulator `acc` exactly as it is, from its
 // object's squared sphere distance d2 alone: past the slack the object's value is its sphere
-// distance `lower`, and a union keeps acc when acc <= lower, a smooth union (k > 0) when
-// lower - acc >= k with a 1% margin (the blend weight is then exactly 1 and the blend returns acc
-// bit for bit, unless acc is a zero), a subtraction when -lower < acc. far_beyond proves
-// lower > max(threshold, slack) in binary32 without the square root.
+// distance `lower`, and a union keeps acc when acc <= lower, a subtraction when -lower < acc,
+// and a smooth union (k > 0) when lower > acc + k rounded up: then lower - acc rounds to at least
+// k, the blend weight is exactly 1 and the blend returns acc bit for bit (unless acc is a zero).
+// far_beyond proves lower > max(threshold, slack) in binary32 without the square root.
 MD bool one_keeps_acc(uint32_t comb, float k, float acc, float d2, float r, float slack) {
     if (!(acc < __int_as_float(0x7f800000) && acc > -__int_as_float(0x7f800000))) return false;
     float thr;
     if (comb == 1u && k > 0.0f) {
         if (acc == 0.0f) return false;
-        thr = acc + k * 1.01f;
+        thr = __fadd_ru(acc, k);
     } else if (comb == 2u) {
         thr = -acc;
     } else {

@@ -321,14 +321,14 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             const DevObject& o = obj[sg.a];
             // A bounded object whose sphere distance clears the slack and a threshold set by the
             // accumulated field leaves the accumulator as it is (one_keeps_acc in device_math.cuh:
-            // the accumulator for a union, the accumulator plus k with a 1% margin for a smooth
-            // union, whose blend weight is then exactly 1, minus the accumulator for a
-            // subtraction): the squared pre-test skips the segment there. Never for an
-            // accumulator that is not finite, nor a zero one under a smooth union.
+            // the accumulator for a union, the accumulator plus k rounded up for a smooth union,
+            // whose blend weight is then exactly 1, minus the accumulator for a subtraction): the
+            // squared pre-test skips the segment there. Never for an accumulator that is not
+            // finite, nor a zero one under a smooth union.
             const bool smooth = sg.b == 1u && o.k > 0.0f;
             const bool skip = seeded && (o.flags & OF_BOUND) && sg.b <= 2u;
             if (skip) {
-                const std::string thr = smooth      ? "acc.d + " + fbits((float)((double)o.k * 1.01))
+                const std::string thr = smooth      ? "__fadd_ru(acc.d, " + fbits(o.k) + ")"
                                         : sg.b == 2u ? std::string("-acc.d")
                                                      : std::string("acc.d");
                 os << "        const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "

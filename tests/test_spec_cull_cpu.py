@@ -151,8 +151,8 @@ def _smooth_union_d(a, b, k):
 
 
 def test_far_one_segments_leave_the_accumulator():
-    """A smooth-union segment is skipped where its sphere distance clears max(acc + 1.01 k, slack)
-    by the squared pre-test (acc finite and non-zero): there the blend weight is exactly 1, and
+    """A smooth-union segment is skipped where its sphere distance clears max(acc + k rounded up,
+    slack) by the squared pre-test (acc finite and non-zero): there the blend weight is exactly 1, and
     the blend returns the accumulator's distance bit for bit with its material. A union segment
     (threshold acc) keeps the accumulator outright, a subtraction (threshold -acc) keeps it as
     max(acc, -lower). Both the specialised field and the interpreter (one_keeps_acc) apply it."""
@@ -165,7 +165,10 @@ def test_far_one_segments_leave_the_accumulator():
         acc = np.concatenate([rng.uniform(-5, 5, 8000), rng.uniform(-150, 150, 6000),
                               rng.uniform(1e-6, 1e-3, 6000)]).astype(F)
         acc[acc == 0] = F(1e-3)
-        thr = np.maximum(F(acc + F(k * 1.01)), slack).astype(F)
+        exact = acc.astype(np.float64) + np.float64(k)  # exact: the operands' exponents are close
+        up = exact.astype(F)
+        up = np.where(up.astype(np.float64) < exact, np.nextafter(up, F(np.inf)), up).astype(F)  # __fadd_ru
+        thr = np.maximum(up, slack).astype(F)
         p = _points_near(rng, c, float(rng.uniform(0.5, 40.0)), 20000)
         p = (c + (p - c) * rng.uniform(0.0, 3.0, (20000, 1))).astype(F)
         d2 = length_sq((p - c).astype(F))
@@ -184,3 +187,27 @@ def test_far_one_segments_leave_the_accumulator():
         assert sskip.mean() > 0.05
         sub = np.fmax(acc, -lower).astype(F)
         assert np.array_equal(sub[sskip].view(np.uint32), acc[sskip].view(np.uint32))
+
+
+def test_smooth_skip_holds_for_large_accumulators_and_small_blends():
+    """The smooth-union skip's threshold is acc + k rounded up, so it needs no bound on |acc|:
+    sphere distances within a few parts in 10^4 of the threshold (the pre-test keeps a 2^-14
+    margin on squared distances), accumulators up to 10^5, blend radii down to 10^-3."""
+    rng = np.random.default_rng(31)
+    slack = F(0.4)
+    for k in (0.001, 0.01, 0.3, 2.0):
+        k = F(k)
+        acc = np.concatenate([rng.uniform(1e2, 1e5, 20000), rng.uniform(0.4, 3.0, 20000)]).astype(F)
+        r = F(0.75)
+        exact = acc.astype(np.float64) + np.float64(k)
+        up = exact.astype(F)
+        up = np.where(up.astype(np.float64) < exact, np.nextafter(up, F(np.inf)), up).astype(F)
+        thr = np.maximum(up, slack).astype(F)
+        dist_c = (thr.astype(np.float64) + np.float64(r)) * (1.0 + rng.uniform(-1e-4, 2e-4, len(acc)))
+        d2 = F(dist_c * dist_c)
+        skip = far_beyond(d2, thr, r)
+        assert 0.2 < skip.mean() < 0.8
+        lower = F(np.sqrt(d2).astype(F) - r)
+        dist, h = _smooth_union_d(acc, lower, k)
+        assert (h[skip] == F(1)).all()
+        assert np.array_equal(dist[skip].view(np.uint32), acc[skip].view(np.uint32))
