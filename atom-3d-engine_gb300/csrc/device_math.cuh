@@ -495,8 +495,9 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
                 wnc = (o.flags & OF_NONCONS) && (o.flags & OF_BOUND);
                 if (o.flags & OF_BOUND) {
                     const float d2 = length_sq(p - ld3(o.bc));
-                    // cannot win: the squared pre-test first, without the square root
-                    if (!(o.flags & OF_NONCONS) && far_beyond(d2, bd, o.br)) break;
+                    // cannot win: the squared pre-test first, without the square root (a
+                    // non-conservative member past the slack as well, where its value is `lower`)
+                    if (far_beyond(d2, (o.flags & OF_NONCONS) ? fmaxf(bd, slack) : bd, o.br)) break;
                     float lower = sqrtf(d2) - o.br;
                     wl = lower;
                     wr = o.br;
@@ -531,7 +532,9 @@ __device__ __forceinline__ Field world_eval(const Tape& T, V p) {
                 continue;
             }
             const DevNode& nd = T.node[stk.pop()];
-            float lower = length(p - V{nd.cx, nd.cy, nd.cz}) - nd.r;
+            const float nd2 = length_sq(p - V{nd.cx, nd.cy, nd.cz});
+            if (far_beyond(nd2, bd, nd.r)) continue;  // lower > bd, without the square root
+            float lower = sqrtf(nd2) - nd.r;
             if (lower > bd) continue;
             if (nd.leaf >= 0) {
                 if (lower > slack) {
@@ -601,7 +604,9 @@ static __device__ __noinline__ Field bvh_segment(const Tape& T, uint32_t s, V p,
     if (sg.c != NIL) stk.push(sg.c);
     while (stk.n > 0) {
         const DevNode& nd = T.node[stk.pop()];
-        float lower = length(p - V{nd.cx, nd.cy, nd.cz}) - nd.r;
+        const float nd2 = length_sq(p - V{nd.cx, nd.cy, nd.cz});
+        if (far_beyond(nd2, bd, nd.r)) continue;  // lower > bd, without the square root
+        float lower = sqrtf(nd2) - nd.r;
         if (lower > bd) continue;
         if (nd.leaf >= 0) {
             int32_t i = nd.leaf;
