@@ -22,3 +22,22 @@ def test_generated_program_compiles(name):
     if not ok and "libnvrtc not found" in msg:
         pytest.skip("NVRTC is not installed")
     assert ok, msg
+
+
+@pytest.mark.parametrize("name", ["smooth_chain", "noncons", "procedural2"])
+def test_generated_program_compiles_with_every_cull(name):
+    """Programs that use the squared weak-bound test, the non-conservative pre-test, and the
+    union / smooth-union / subtraction segment skips compile too."""
+    from field_scenes import noncons_scene, smooth_chain_scene
+
+    s, _ = {"smooth_chain": lambda: smooth_chain_scene(5, 32, 18), "noncons": lambda: noncons_scene(21, 32, 18),
+            "procedural2": lambda: scenes.procedural_scene(2, 32, 18)}[name]()
+    src = mm3e_cuda.spec_source(s)
+    if name == "smooth_chain":
+        assert "__fadd_ru(acc.d, " in src and "fmaxf(-acc.d, " in src
+    if name == "noncons":
+        assert "far_beyond(d2, fmaxf(bd, " in src
+    ok, msg, ms = mm3e_cuda.spec_compile_check(s)
+    if not ok and "libnvrtc not found" in msg:
+        pytest.skip("NVRTC is not installed")
+    assert ok, msg
