@@ -211,6 +211,16 @@ std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
     return os.str();
 }
 
+// A sphere with the identity rotation, unit scale and no modifiers whose bounding sphere is
+// itself: its exact field, length(p - pos) - r (the identity rotation only changes the signs of
+// zero coordinates, which the squares drop), equals the bound distance sqrtf(|p - c|^2) - r bit for
+// bit, so a member needs no second evaluation.
+bool plain_sphere(const DevObject& o) {
+    return o.prim == 0u && (o.flags & OF_BOUND) && (o.flags & OF_ROT_IDENTITY) &&
+           !(o.flags & (OF_POINT_OPS | OF_ROUND | OF_ONION)) && o.scale == 1.0f && o.inv == 1.0f &&
+           o.bc[0] == o.pos[0] && o.bc[1] == o.pos[1] && o.bc[2] == o.pos[2] && o.br == o.params[0];
+}
+
 std::string lower_expr(const DevObject& o) {
     return "length(p - V{" + fbits(o.bc[0]) + ", " + fbits(o.bc[1]) + ", " + fbits(o.bc[2]) + "}) - " + fbits(o.br);
 }
@@ -367,6 +377,16 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             std::vector<uint32_t> cullable;
             auto member = [&](uint32_t i, bool cull) {
                 const DevObject& o = obj[i];
+                if (cull && plain_sphere(o)) {
+                    os << "        {  // member " << i << " (its exact field is its bound distance)\n"
+                       << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
+                       << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, bd, " << fbits(o.br)
+                       << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n"
+                       << "            if (lower < bd || (lower == bd && " << i << " < bi)) {\n                bd = lower;\n"
+                       << "                bi = " << i << ";\n                bm = " << o.mat
+                       << "u;\n                bnc = false;\n            }\n            }\n        }\n";
+                    return;
+                }
                 bool nc = (o.flags & OF_NONCONS) != 0;
                 // a bounded OF_NONCONS winner needs the BVH walk only where it may undercut its sphere
                 const bool nc_bounded = nc && (o.flags & OF_BOUND);
