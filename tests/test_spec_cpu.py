@@ -41,3 +41,23 @@ def test_generated_program_compiles_with_every_cull(name):
     if not ok and "libnvrtc not found" in msg:
         pytest.skip("NVRTC is not installed")
     assert ok, msg
+
+
+def test_plain_sphere_members_only_where_the_bound_is_the_field():
+    """Only a sphere with the identity rotation, unit scale and no modifiers takes its bound
+    distance as its exact field; scaled, rotated or rounded spheres keep their own evaluation."""
+    from mm3e_cuda.scene import Material, Object, Prim, Scene, Transform, mat3_from_euler
+
+    def count(obj):
+        s = Scene(16, 16)
+        s.materials = [Material((0.8, 0.8, 0.8))]
+        s.objects = [Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, 0), obj,
+                     Object(Prim.sphere(0.3), Transform((9.0, 1.0, 9.0)), 0)]
+        return mm3e_cuda.spec_source(s).count("its exact field is its bound distance")
+
+    plain = Object(Prim.sphere(0.7), Transform((0.5, 1.0, -0.25)), 0)
+    assert count(plain) == 2
+    assert count(Object(Prim.sphere(0.7), Transform((0.5, 1.0, -0.25), scale=2.0), 0)) == 1
+    assert count(Object(Prim.sphere(0.7), Transform((0.5, 1.0, -0.25), mat3_from_euler(0.1, 0.2, 0.3)), 0)) == 1
+    assert count(plain.round(0.05)) == 1
+    assert count(Object(Prim.box((0.5, 0.5, 0.5)), Transform((0.5, 1.0, -0.25)), 0)) == 1
