@@ -246,7 +246,9 @@ int ensure_frame_buffers(mm3e_scene* s, bool host) {
 }
 
 int upload_post_kernel(mm3e_scene* s) {
-    uint32_t r = s->src.d.post.bloom_radius;
+    const mm3e_post& post = s->src.d.post;
+    // the kernel is read only by blooming frames; without bloom a radius-1 kernel stands in
+    uint32_t r = (post.bloom && post.bloom_intensity > 0.0f) ? post.bloom_radius : 1u;
     std::vector<float> k = gaussian_kernel(r);
     cudaFree(s->d_kernel);
     s->d_kernel = nullptr;

@@ -463,6 +463,11 @@ int validate_scene(const mm3e_scene_desc& d, std::string& err) {
         err = "bounces must be at most 7";
         return MM3E_ERR_UNSUPPORTED;
     }
+    if (d.post.bloom && d.post.bloom_intensity > 0.0f && d.post.bloom_radius > MAX_BLOOM_RADIUS) {
+        // every output pixel sums 2r+1 taps per blur pass: a larger kernel would hold the GPU for minutes
+        err = "bloom radius must be at most 4096";
+        return MM3E_ERR_UNSUPPORTED;
+    }
     if (d.n_csgs && (!d.csg_roots || !d.csg_nodes)) {
         err = "null CSG arrays";
         return MM3E_ERR_INVALID;

@@ -22,6 +22,7 @@ constexpr uint32_t MAX_NODES = 65535;
 constexpr int MAX_CSG_STACK = 16;   // value / point stack of a CSG program
 constexpr int MAX_BOUNCES = 7;      // reflection recursion depth the kernels carry
 constexpr int MAX_AA = 16;
+constexpr uint32_t MAX_BLOOM_RADIUS = 4096;  // bloom kernels of at most 2 * 4096 + 1 taps
 
 // Object flags
 enum : uint32_t {

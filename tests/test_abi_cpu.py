@@ -109,6 +109,22 @@ def test_invalid_scenes_are_rejected():
     assert _validate(s)[0] == abi.ERR_INVALID
 
 
+def test_bloom_radius_limit():
+    """A blooming scene's blur radius is capped at 4096 (each pass sums 2r+1 taps per pixel); the
+    radius of a scene without bloom is not looked at."""
+    s, _ = scenes.gallery_scene(32, 18)
+    s.post.bloom_radius = 4096
+    assert _validate(s) == (abi.OK, "")
+    s.post.bloom_radius = 4097
+    code, msg = _validate(s)
+    assert code == abi.ERR_UNSUPPORTED and "bloom radius" in msg
+    s.post.bloom = False
+    assert _validate(s) == (abi.OK, "")
+    s.post.bloom = True
+    s.post.bloom_intensity = 0.0
+    assert _validate(s) == (abi.OK, "")
+
+
 @pytest.mark.parametrize("expr", [
     Expr.sphere(float("nan")),
     Expr.plane((0.0, 2.0, 0.0), 0.0),
