@@ -360,7 +360,10 @@ int mm3e_ctx_set_host_writes(mm3e_ctx* ctx, int enable, int* active);
 int mm3e_ctx_kernel_times(mm3e_ctx* ctx, mm3e_kernel_time* out, uint32_t cap, uint32_t* n_out);
 
 /* ---- scenes ------------------------------------------------------------------------------- */
-/* Validates and lowers `desc` into a device-resident scene tape; `desc` may be freed after. */
+/* Validates and lowers `desc` into a device-resident scene tape; `desc` may be freed after.
+ * Beyond the reference's own rules, this path gives MM3E_ERR_UNSUPPORTED for aa > 16,
+ * bounces > 7, a blooming scene's bloom_radius > 4096, CSG programs deeper than 16 values and
+ * plain-union runs too large for its traversal stack. */
 int mm3e_scene_compile(mm3e_ctx* ctx, const mm3e_scene_desc* desc, mm3e_scene** out);
 void mm3e_scene_destroy(mm3e_scene* scene);
 /* Device memory the compiled scene holds (tape, payloads, pass and frame buffers). */
