@@ -37,17 +37,52 @@ def normalize_f32(v):
 IDENTITY_ROT = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
 
 
+class _LibraryHostMath:
+    """The library's own host helpers (libmm3e_cuda.so): the default provider."""
+
+    @staticmethod
+    def camera_look_at(eye3, target3, up3, fov_y, cam_ref):
+        lib().mm3e_camera_look_at(eye3, target3, up3, fov_y, cam_ref)
+
+    @staticmethod
+    def orbit_camera(target3, radius, yaw, pitch, fov_y, cam_ref):
+        lib().mm3e_orbit_camera(target3, radius, yaw, pitch, fov_y, cam_ref)
+
+    @staticmethod
+    def mat3_from_euler(x, y, z, out9):
+        lib().mm3e_mat3_from_euler(x, y, z, out9)
+
+    @staticmethod
+    def quat_to_mat3(q4, out9):
+        lib().mm3e_quat_to_mat3(q4, out9)
+
+
+_host_math = _LibraryHostMath()
+
+
+def use_host_math(provider=None):
+    """Route the binary32 scene-building helpers (look_at, orbit_camera, mat3_from_euler,
+    quat_to_mat3) through `provider`, an object with the four functions of _LibraryHostMath
+    that writes the same values; None restores the library's helpers. A process that must not
+    load libmm3e_cuda.so (a CPU-only timing of the reference path) builds its scenes this way.
+    Returns the previous provider."""
+    global _host_math
+    prev = _host_math
+    _host_math = provider if provider is not None else _LibraryHostMath()
+    return prev
+
+
 def mat3_from_euler(x, y, z):
     """Mat3::from_euler (vec.rs:144-149): columns as a 9-tuple."""
     out = (C.c_float * 9)()
-    lib().mm3e_mat3_from_euler(x, y, z, out)
+    _host_math.mat3_from_euler(x, y, z, out)
     return tuple(out)
 
 
 def quat_to_mat3(q_xyzw):
     """Quat::to_mat3 (vec.rs:318-326)."""
     out = (C.c_float * 9)()
-    lib().mm3e_quat_to_mat3((C.c_float * 4)(*q_xyzw), out)
+    _host_math.quat_to_mat3((C.c_float * 4)(*q_xyzw), out)
     return tuple(out)
 
 
@@ -502,7 +537,7 @@ class Scene:
 def look_at(eye, target, up_hint, fov_y):
     """Camera::look_at (camera.rs:50-55)."""
     cam = abi.Camera()
-    lib().mm3e_camera_look_at((C.c_float * 3)(*eye), (C.c_float * 3)(*target), (C.c_float * 3)(*up_hint), fov_y,
+    _host_math.camera_look_at((C.c_float * 3)(*eye), (C.c_float * 3)(*target), (C.c_float * 3)(*up_hint), fov_y,
                               C.byref(cam))
     return cam
 
@@ -510,7 +545,7 @@ def look_at(eye, target, up_hint, fov_y):
 def orbit_camera(target, radius, yaw, pitch, fov_y):
     """orbit_camera (mm3e-orchestrator/src/lib.rs:1426-1435)."""
     cam = abi.Camera()
-    lib().mm3e_orbit_camera((C.c_float * 3)(*target), radius, yaw, pitch, fov_y, C.byref(cam))
+    _host_math.orbit_camera((C.c_float * 3)(*target), radius, yaw, pitch, fov_y, C.byref(cam))
     return cam
 
 

@@ -3,26 +3,27 @@
 
 Workload (default): the 1080p feature gallery (1920x1080, aa 1, one reflection bounce, soft
 shadows, AO, fog, sky IBL, bloom + ACES; 11 primitives, smooth union, twist/bend/onion/round/
-repeat/mirror; max 256 steps). A step = one frame rendered on the GPU from the resident
-scene tape to a device RGBA8 framebuffer (render kernel + post kernels).
+repeat/mirror; max 256 steps). A step = `--frames-per-step` frames (32 by default) of the same
+scene and camera, each rendered on the GPU from the resident scene tape to a device RGBA8
+framebuffer (render kernels + post kernels); the L2 is flushed between timed steps.
 
-  value      frames/s with the scene resident in HBM (CUDA events on the render stream,
-             L2 flushed between timed frames by writing a 256 MB buffer)
+  value      frames/s with the scene resident in HBM (CUDA events on the render stream)
   e2e        frames/s through the public C ABI call mm3e_render with a host framebuffer:
              per frame the camera goes host->device and the RGBA8 frame device->host (on a
              host whose page tables the GPU shares, the post kernel stores it straight into
              the caller's buffer over NVLink-C2C; elsewhere through a pinned staging copy)
-  roofline   FP32-pipe roofline of the dominant kernel (the march tape interpreter): the
-             algorithmic f32 operations of its phase per frame (oracle operation count split by
-             kernel, committed fixture) / its CUDA-event-timed device time per frame (events
-             around every pass, a second run of the same frames), against SMs x 128 lanes x 2 x
-             max SM clock
-  cpu_baseline  the CPU restatement of the reference render path on all host cores, timed on
-             a bounded row sample (rows scaled to a full frame) plus its single-thread post pass
+  roofline   FP32-pipe roofline of the dominant kernel: the algorithmic f32 operations of its
+             phase per frame (oracle operation count split by kernel, committed fixture) / its
+             CUDA-event-timed device time per frame (events around every pass, a second run of
+             the same frames), against SMs x 128 lanes x 2 x max SM clock
+  cpu_baseline  the CPU restatement of the reference render path on all host cores, whole frames
+  parity     the last timed frame against the oracle's frame of the cpu_baseline leg, and the
+             primary hits against the oracle's
 
 --impl reference times the CPU reference path (the oracle restatement: the Rust reference has no
-toolchain here) on the same workload and prints its own line. Multi-GPU runs are replicas:
-each rank renders its own frames (scaling "weak").
+toolchain here) on the same workload, one whole frame per step, and prints its own line with the
+same `config`; it builds its scene through the oracle's helpers and never loads the CUDA library.
+Multi-GPU runs are replicas: each rank renders its own frames (scaling "weak").
 """
 import argparse
 import json
@@ -65,6 +66,8 @@ def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--frames-per-step", type=int, default=32,
+                    help="frames of the workload (same scene and camera) rendered per timed step")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gallery_1080p")
@@ -463,56 +466,122 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(scene, cam, target_s):
-    """Oracle render of a bounded row sample on all host cores + its post pass, scaled to a frame."""
+def workload_config(args, scene, world):
+    """The `config` dict both arms print (the same workload, the same dict)."""
+    return {"workload": args.workload, "width": scene.width, "height": scene.height, "aa": scene.aa,
+            "bounces": scene.bounces, "max_steps": scene.marcher.max_steps, "parallelism": f"replicas x{world}",
+            "l2": "flushed between timed steps (256 MB write)"}
+
+
+def cpu_frames(scene, cam, target_s, threads):
+    """Whole frames of the workload through the oracle (render + post, all host threads): one
+    untimed frame, then frames until about `target_s` seconds are spent (at least one), each
+    after a 256 MB host write. Returns (frame seconds list, the last RGBA f32 frame)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
 
     import oracle_py
 
-    threads = os.cpu_count() or 1
     h = scene.desc()
-    probe_rows = max(4, scene.height // 64)
-    y0 = scene.height // 2 - probe_rows // 2
-    t_probe = oracle_py.time_rows(h, cam, y0, y0 + probe_rows, threads)
-    rows = int(min(scene.height, max(probe_rows, probe_rows * target_s / max(t_probe, 1e-3))))
-    y0 = max(0, scene.height // 2 - rows // 2)
-    # rows centred on the frame's middle band, where the scene content (and the cost) sits
-    t_rows = oracle_py.time_rows(h, cam, y0, y0 + rows, threads)
-    hdr = np.zeros((scene.height, scene.width, 3), np.float32)
-    hdr[y0:y0 + rows] = oracle_py.render_rows(h, cam, y0, y0 + rows, threads)
+    flush = np.empty(64 * 1024 * 1024, np.float32)
     t0 = time.perf_counter()
-    oracle_py.post(h, hdr)
-    t_post = time.perf_counter() - t0
-    frame_s = t_rows * scene.height / rows + t_post
-    return {"value": 1.0 / frame_s, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"rows {y0}-{y0 + rows} of {scene.height} ({t_rows:.2f} s on {threads} threads, scaled "
-                      f"to the frame) + full-frame post pass ({t_post:.2f} s, single thread as post::resolve)"}
+    frame = oracle_py.render(h, cam, threads=threads)
+    first = time.perf_counter() - t0
+    n = max(1, int(round(target_s / max(first, 1e-3))))
+    ts = []
+    for i in range(n):
+        flush.fill(float(i))
+        t0 = time.perf_counter()
+        frame = oracle_py.render(h, cam, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    return ts, frame
+
+
+def cpu_baseline(scene, cam, target_s):
+    """The oracle (CPU restatement of the reference render path) on all host cores, whole frames."""
+    threads = os.cpu_count() or 1
+    ts, frame = cpu_frames(scene, cam, target_s, threads)
+    v = len(ts) / sum(ts)
+    return {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{len(ts)} whole {scene.width}x{scene.height} frames after one untimed frame "
+                      f"(render + post; {sum(ts):.2f} s on {threads} threads)"}, frame
+
+
+def frame_parity(gpu_rgba8, ref_rgba8, gpu_hits, ref_hits):
+    """The parity bars on one frame: (iii) RGB8 within 1 LSB and PSNR; (i) hit/miss and material
+    mismatches (silhouettes: pixels with a different id in their 4-neighbourhood); (ii) hit
+    distance within 1e-4 relative on agreed hits."""
+    import numpy as np
+
+    a = np.asarray(gpu_rgba8)[..., :3].astype(np.int32)
+    b = np.asarray(ref_rgba8)[..., :3].astype(np.int32)
+    d = np.abs(a - b)
+    mse = float((d.astype(np.float64) ** 2).mean())
+    out = {"psnr": float("inf") if mse == 0 else 10.0 * math.log10(255.0 ** 2 / mse),
+           "within1_px": float((d.max(-1) <= 1).mean()), "exact_px": float((d.max(-1) == 0).mean()),
+           "max_lsb": int(d.max())}
+    gm, rm = gpu_hits["mat"], ref_hits["mat"]
+    diff = gm != rm
+
+    def edges(m):
+        e = np.zeros(m.shape, bool)
+        e[1:, :] |= m[1:, :] != m[:-1, :]
+        e[:-1, :] |= m[:-1, :] != m[1:, :]
+        e[:, 1:] |= m[:, 1:] != m[:, :-1]
+        e[:, :-1] |= m[:, :-1] != m[:, 1:]
+        return e
+
+    sil = edges(gm) | edges(rm)
+    agreed = (~diff) & (rm != 0xFFFFFFFF)
+    rel = np.abs(gpu_hits["t"][agreed].astype(np.float64) - ref_hits["t"][agreed]) / np.maximum(
+        np.abs(ref_hits["t"][agreed]), 1e-12)
+    out.update({"mismatch_frac": float(diff.mean()), "mismatch_off_silhouette": int((diff & ~sil).sum()),
+                "t_within_1e-4": float((rel <= 1e-4).mean()) if rel.size else 1.0,
+                "t_rel_max": float(rel.max()) if rel.size else 0.0})
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the CPU reference render path (the oracle restatement; the Rust reference
+    has no toolchain here) on all host threads, whole frames of the same workload. The scene and
+    camera are built through the oracle's own helpers, so libmm3e_cuda.so is never loaded."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle_py
+    from mm3e_cuda.scene import use_host_math
+
+    use_host_math(oracle_py.HostMath())
     scene, cam = workloads()[args.workload]()
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    threads = os.cpu_count() or 1
+    h = scene.desc()
+    flush = np.empty(64 * 1024 * 1024, np.float32)
     for _ in range(args.warmup):
-        cpu_baseline(scene, cam, per_step)
-    vals = [cpu_baseline(scene, cam, per_step) for _ in range(args.steps)]
-    v = statistics.median([x["value"] for x in vals])
-    cb = dict(vals[0])
-    cb["value"] = v
+        oracle_py.render(h, cam, threads=threads)
+    ts = []
+    for i in range(args.steps):
+        flush.fill(float(i))
+        t0 = time.perf_counter()
+        oracle_py.render(h, cam, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    v = len(ts) / sum(ts)
     counts = load_counts(args.workload)
     rays = None
     if counts:
         r = counts["render"]
         rays = (r["primary_rays"] + r["reflection_rays"] + r["shadow_rays"]) * v / 1e6
+    cb = {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+          "sample": f"one whole {scene.width}x{scene.height} frame per step (render + post), all {threads} host "
+                    "threads; the CPU restatement of the reference path (oracle/)"}
     print(json.dumps({
         "impl": "reference", "metric": f"frames/s ({args.workload})", "value": v, "unit": "frames/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(ts) / len(ts),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic seeded scene", "config": {"workload": args.workload, "width": scene.width,
-                                                     "height": scene.height, "aa": scene.aa},
+        "data": "synthetic seeded scene (no dataset)", "config": workload_config(args, scene, world),
         "mrays_per_s": rays, "cpu_baseline": cb,
         "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
@@ -545,8 +614,14 @@ def run_ours(args):
     out8 = torch.empty(h * w * 4, dtype=torch.uint8, device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
 
+    fps_step = max(1, args.frames_per_step)
+
     def frame():
         compiled.render_device(cam, abi.FB_RGBA8, out8.data_ptr(), out8.numel())
+
+    def step():
+        for _ in range(fps_step):
+            frame()
 
     def timed(fn, k):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
@@ -577,7 +652,7 @@ def run_ours(args):
                   "search_s": round(time.perf_counter() - t0, 2)}
     specialized = compiled.specialized
     for _ in range(max(3, args.warmup)):
-        frame()
+        step()
     stream.synchronize()
     if dist:
         tdist.barrier()
@@ -585,9 +660,11 @@ def run_ours(args):
 
     sampler = ClockSampler(local)
     t0 = time.perf_counter()
-    frame_ms = timed(frame, args.steps)
+    step_ms = timed(step, args.steps)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    gpu_frame = out8.view(h, w, 4).cpu().numpy()  # the last timed frame, for the parity check
+    frame_ms = [ms / fps_step for ms in step_ms]
     # per-kernel device time: the same frames again with CUDA events around every pass
     ctx.set_profiling(True)
     ctx.kernel_times()
@@ -601,7 +678,7 @@ def run_ours(args):
     _, st = compiled.render(cam, fmt=abi.FB_RGBA8, stats=True, out=host)
     launches_per_frame = st["kernel_launches"]
     t1 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(args.steps * fps_step):
         compiled.render(cam, fmt=abi.FB_RGBA8, out=host)
     e2e_s = time.perf_counter() - t1
     clocks = sampler.stop()
@@ -650,26 +727,33 @@ def run_ours(args):
         roofline["frame_fp32_per_s"] = (r["fp32"] + counts["post"]["fp32"]) * value / 1e12
         rays = r["primary_rays"] + r["reflection_rays"] + r["shadow_rays"]
         mrays = rays * value / 1e6
-    cpu = None
+    cpu, parity = None, None
     if not args.no_cpu:
-        cpu = cpu_baseline(scene, cam, args.cpu_seconds)
-    e2e_value = world * args.steps / e2e_s
+        cpu, ref_frame = cpu_baseline(scene, cam, args.cpu_seconds)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+
+        parity = frame_parity(gpu_frame, mm3e_cuda.to_rgba8(ref_frame), compiled.render_hits(cam),
+                              oracle_py.primary_hits(scene.desc(), cam))
+        parity["frame"] = ("the last timed frame (device RGBA8, the timed launch shape) against the oracle's frame "
+                           "of the cpu_baseline leg; hits: mm3e_render_hits against the oracle's primary hits")
+    e2e_value = world * args.steps * fps_step / e2e_s
     line = {
         "metric": f"frames/s ({args.workload})", "value": value, "unit": "frames/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean_ms * fps_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic seeded scene (no dataset)",
-        "config": {"workload": args.workload, "width": w, "height": h, "aa": scene.aa, "bounces": scene.bounces,
-                   "max_steps": scene.marcher.max_steps, "parallelism": f"replicas x{world}",
-                   "l2": "flushed between timed frames (256 MB write)",
-                   "field": "scene-specialised (NVRTC)" if specialized else "tape interpreter",
-                   "spec_compile_ms": spec_compile_ms, "launch_tuning": tuning},
+        "config": workload_config(args, scene, world),
+        "frames_per_step": fps_step,
+        "field": "scene-specialised (NVRTC)" if specialized else "tape interpreter",
+        "spec_compile_ms": spec_compile_ms, "launch_tuning": tuning,
         "interpreter": {"frames_per_s": 1000.0 / statistics.median(interp_ms),
                         "frame_ms_median": statistics.median(interp_ms)},
         "mrays_per_s": mrays, "frame_ms": {"min": min(frame_ms), "median": statistics.median(frame_ms),
                                            "max": max(frame_ms)},
-        "wall_s_timed_region": wall, "roofline": roofline, "cpu_baseline": cpu,
-        "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 52, "d2h_bytes_per_step": w * h * 4},
-        "gpu_launches": launches_per_frame * args.steps, "clocks": clocks,
+        "wall_s_timed_region": wall, "roofline": roofline, "cpu_baseline": cpu, "parity": parity,
+        "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 52 * fps_step,
+                "d2h_bytes_per_step": w * h * 4 * fps_step},
+        "gpu_launches": launches_per_frame * args.steps * fps_step, "clocks": clocks,
     }
     if cpu:
         line["speedup_vs_cpu"] = value / cpu["value"]

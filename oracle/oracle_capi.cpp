@@ -93,6 +93,28 @@ void oracle_mat3_from_euler(float x, float y, float z, float out_cols[9]) {
     }
 }
 
+// Quat::to_mat3 (vec.rs:318-326) after Quat::normalize (vec.rs:276-283; dot at :272-274):
+// columns of the rotation matrix of the normalised quaternion (x, y, z, w).
+void oracle_quat_to_mat3(const float q_xyzw[4], float out_cols[9]) {
+    float x = q_xyzw[0], y = q_xyzw[1], z = q_xyzw[2], w = q_xyzw[3];
+    float n = std::sqrt(x * x + y * y + z * z + w * w);
+    if (n > 1e-12f) {
+        x = x / n;
+        y = y / n;
+        z = z / n;
+        w = w / n;
+    } else {  // Quat::IDENTITY
+        x = 0.0f;
+        y = 0.0f;
+        z = 0.0f;
+        w = 1.0f;
+    }
+    const float c[9] = {1.0f - 2.0f * (y * y + z * z), 2.0f * (x * y + z * w), 2.0f * (x * z - y * w),
+                        2.0f * (x * y - z * w), 1.0f - 2.0f * (x * x + z * z), 2.0f * (y * z + x * w),
+                        2.0f * (x * z + y * w), 2.0f * (y * z - x * w), 1.0f - 2.0f * (x * x + y * y)};
+    for (int i = 0; i < 9; ++i) out_cols[i] = c[i];
+}
+
 // Full frame through the reference's render() semantics: beauty (with post) or a debug AOV.
 // rgba: w*h*4 floats (Framebuffer pixels). hdr3 (optional): beauty radiance before post.
 int oracle_render(const mm3e_scene_desc* d, const mm3e_camera* cam, unsigned threads, float* rgba, float* hdr3) {

@@ -63,6 +63,7 @@ def lib():
         l.oracle_camera_look_at.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), C.c_float, vp]
         l.oracle_orbit_camera.argtypes = [P(C.c_float), C.c_float, C.c_float, C.c_float, C.c_float, vp]
         l.oracle_mat3_from_euler.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        l.oracle_quat_to_mat3.argtypes = [P(C.c_float), P(C.c_float)]
         _lib = l
     return _lib
 
@@ -324,3 +325,26 @@ def reproject(g, prev_cam, new_cam, deltas=(), hybrid_handle=None, threads=None)
         lib().oracle_rerender_holes(C.addressof(hybrid_handle.desc), C.addressof(new_cam), threads or threads_default(),
                                     _u8(out), _u8(filled))
     return out
+
+
+class HostMath:
+    """The oracle's restatements of the reference's scene-building helpers (Camera::look_at,
+    orbit_camera, Mat3::from_euler, Quat::to_mat3), with the signatures of the CUDA library's
+    host helpers. `mm3e_cuda.scene.use_host_math(HostMath())` builds scenes and cameras through
+    them, so that a CPU-only process (the timed reference arm) never loads the CUDA library."""
+
+    @staticmethod
+    def camera_look_at(eye3, target3, up3, fov_y, cam_ref):
+        lib().oracle_camera_look_at(eye3, target3, up3, fov_y, cam_ref)
+
+    @staticmethod
+    def orbit_camera(target3, radius, yaw, pitch, fov_y, cam_ref):
+        lib().oracle_orbit_camera(target3, radius, yaw, pitch, fov_y, cam_ref)
+
+    @staticmethod
+    def mat3_from_euler(x, y, z, out9):
+        lib().oracle_mat3_from_euler(x, y, z, out9)
+
+    @staticmethod
+    def quat_to_mat3(q4, out9):
+        lib().oracle_quat_to_mat3(q4, out9)

@@ -72,6 +72,63 @@ def test_euler_rotation_matches_oracle_bitwise():
         assert np.array_equal(np.array(a, np.float32), np.array(list(out), np.float32))
 
 
+def test_quat_rotation_matches_oracle_bitwise():
+    """Quat::to_mat3 (vec.rs:318-326, after Quat::normalize at :276-283), which places the seeded
+    procedural scenes' objects: the library's helper against the oracle's restatement, bit for
+    bit, on random quaternions and on zero, tiny and unnormalised ones."""
+    rng = np.random.default_rng(5)
+    qs = [q for q in rng.normal(size=(300, 4)).astype(np.float32)]
+    qs += [np.array(v, np.float32) for v in ((0, 0, 0, 0), (1e-13, 0, 0, 0), (0, 0, 0, -2), (3e-7, 1e-7, 2e-7, 4e-7),
+                                              (1e20, -3e19, 2e19, 5e19), (0.5, 0.5, 0.5, 0.5))]
+    for q in qs:
+        a = np.array(mm3e_cuda.quat_to_mat3(tuple(float(v) for v in q)), np.float32)
+        out = (C.c_float * 9)()
+        oracle_py.lib().oracle_quat_to_mat3((C.c_float * 4)(*q), out)
+        b = np.array(list(out), np.float32)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (q, a, b)
+
+
+def _scene_bits(scene, cam):
+    rows = [bytes(cam)]
+    for o in scene.objects:
+        rows.append(np.array(o.xform.rot + o.xform.pos + (o.xform.scale,), np.float32).tobytes())
+    return rows
+
+
+def test_oracle_host_math_builds_identical_scenes():
+    """Scenes and cameras built through the oracle's helpers (the CPU reference arm's route, which
+    must not load the CUDA library) hold the same binary32 values as those built through the
+    library's helpers."""
+    from mm3e_cuda.scene import use_host_math
+
+    builders = [lambda: scenes.gallery_scene(64, 36), lambda: scenes.spheres_scene(64, 36),
+                lambda: scenes.cornell_scene(64, 36), lambda: scenes.procedural_scene(3, 64, 36),
+                lambda: scenes.procedural_scene(17, 64, 36)]
+    for build in builders:
+        a = _scene_bits(*build())
+        prev = use_host_math(oracle_py.HostMath())
+        try:
+            b = _scene_bits(*build())
+        finally:
+            use_host_math(prev)
+        assert a == b
+
+
+def test_reference_arm_loads_no_cuda_library():
+    """bench.py --impl reference builds its scene and camera and times the oracle without mapping
+    libmm3e_cuda.so into the process (checked in a child process's memory map)."""
+    code = ("import sys, os; sys.path.insert(0, os.path.join(%r, 'atom-3d-engine_gb300')); "
+            "sys.path.insert(0, os.path.join(%r, 'oracle')); import oracle_py; "
+            "from mm3e_cuda.scene import use_host_math; use_host_math(oracle_py.HostMath()); "
+            "from mm3e_cuda import scenes; s, c = scenes.gallery_scene(32, 18); scenes.procedural_scene(4, 32, 18); "
+            "oracle_py.render(s.desc(), c, threads=2); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('cuda' if 'libmm3e_cuda' in maps else 'clean', 'oracle' if 'liboracle_mm3e' in maps else '')"
+            ) % (ROOT, ROOT)
+    out = subprocess.check_output([os.sys.executable, "-c", code]).decode().split()
+    assert out == ["clean", "oracle"], out
+
+
 def test_row_bands_follow_reference_split():
     from mm3e_cuda.replicas import bands
     assert bands(4, 10) == [(0, 3), (3, 6), (6, 8), (8, 10)]
