@@ -144,6 +144,8 @@ PassPlan plain_plan(const mm3e_scene* s, const mm3e_camera& cam, uint32_t w, uin
     p.ao = (hd->flags & SF_AO) && hd->ao_samples > 0;
     p.shadows = (hd->flags & SF_SHADOWS) && hd->shadow_steps > 0 && hd->n_lights > 0;
     p.bloom = (p.job0.flags & JF_BLOOM) != 0;
+    p.wait_limit = s->ctx->wait_limit;
+    p.wait_probe = s->ctx->wait_probe;
     return p;
 }
 
@@ -322,6 +324,8 @@ int march_centers(mm3e_scene* s, const mm3e_camera* cam, const unsigned char* ta
     a.src = SRC_CENTER;
     a.n_items = n;
     a.counter = s->buf.counters;
+    a.wait_limit = c->wait_limit;
+    a.wait_probe = c->wait_probe;
     const SpecKernels* sp = tape == s->d_tape ? s->spec_kernels() : nullptr;
     CK(launch_march(a, s->tuning(), c->stream, c->sm_count, log, sp));
     if (want_ao) CK(launch_ao(a, c->stream, log, sp));
@@ -557,6 +561,13 @@ int mm3e_ctx_set_host_writes(mm3e_ctx* ctx, int enable, int* active) {
     if (!ctx) return MM3E_ERR_INVALID;
     ctx->host_writes = enable != 0;
     if (active) *active = ctx->host_access && ctx->host_writes ? 1 : 0;
+    return MM3E_OK;
+}
+
+int mm3e_ctx_set_tape_wait(mm3e_ctx* ctx, uint32_t limit, int probe) {
+    if (!ctx) return MM3E_ERR_INVALID;
+    ctx->wait_limit = limit;
+    ctx->wait_probe = probe ? 1u : 0u;
     return MM3E_OK;
 }
 

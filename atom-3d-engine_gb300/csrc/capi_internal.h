@@ -27,6 +27,8 @@ struct mm3e_ctx {
     // NVLink-C2C host such as Grace): kernels then write host framebuffers directly.
     bool host_access = false;
     bool host_writes = true;  // use that for host outputs (mm3e_ctx_set_host_writes)
+    uint32_t wait_limit = 0;  // tape-staging wait limit of the plain calls (mm3e_ctx_set_tape_wait)
+    uint32_t wait_probe = 0;
     std::string err;
     std::set<mm3e_scene*> scenes;       // live scenes; destroyed with the context
     mm3e::TuneParams tune;              // launch shape of the march / shadow passes

@@ -670,8 +670,9 @@ MD D dd_box(D x, D y, D z, V half) {
     D in = dmin(dmax(qx, dmax(qy, qz)), dc(0.0f));
     return dadd(out, in);
 }
-// Prim::distance_dual (lib.rs:244-261; dual.rs:129-232)
-static __device__ __noinline__ D prim_dual(uint32_t kind, const float* q, D x, D y, D z) {
+// Prim::distance_dual (lib.rs:244-261; dual.rs:129-232). Inlined where the primitive is a
+// compile-time constant (a scene-specialised program); called through prim_dual elsewhere.
+MD D prim_dual_inl(uint32_t kind, const float* q, D x, D y, D z) {
     switch (kind) {
         case 0: return dadds(dsqrt(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z))), -q[0]);
         case 1: return dd_box(x, y, z, V{q[0], q[1], q[2]});
@@ -740,7 +741,11 @@ static __device__ __noinline__ D prim_dual(uint32_t kind, const float* q, D x, D
         default: return dc(__int_as_float(0x7f800000));
     }
 }
-// Object::field_dual (lib.rs:435-463)
+static __device__ __noinline__ D prim_dual(uint32_t kind, const float* q, D x, D y, D z) {
+    return prim_dual_inl(kind, q, x, y, z);
+}
+// Object::field_dual (lib.rs:435-463); INL inlines the primitive (a constant object record).
+template <bool INL = false>
 MD D object_dual(const DevObject& o, V p) {
     D wx{p.x, V{1.f, 0.f, 0.f}}, wy{p.y, V{0.f, 1.f, 0.f}}, wz{p.z, V{0.f, 0.f, 1.f}};
     D tx = dadds(wx, -o.pos[0]), ty = dadds(wy, -o.pos[1]), tz = dadds(wz, -o.pos[2]);
@@ -765,32 +770,30 @@ MD D object_dual(const DevObject& o, V p) {
         if (o.repeat[1] > 0.0f) ly = dadds(ly, -roundf(ly.v / o.repeat[1]) * o.repeat[1]);
         if (o.repeat[2] > 0.0f) lz = dadds(lz, -roundf(lz.v / o.repeat[2]) * o.repeat[2]);
     }
-    D d = dscale(prim_dual(o.prim, o.params, lx, ly, lz), o.scale);
+    D d = dscale(INL ? prim_dual_inl(o.prim, o.params, lx, ly, lz) : prim_dual(o.prim, o.params, lx, ly, lz), o.scale);
     if (f & OF_ROUND) d = dadds(d, -o.round);
     if (f & OF_ONION) d = dadds(dabs(d), -o.onion);
     return d;
 }
-// Scene::normal_dual (lib.rs:820-835): every object, no pruning; combine mode in flags bits 16-17.
+// One fold step of Scene::normal_dual (lib.rs:820-835): combine mode in flags bits 16-17.
+MD D dual_fold(D acc, D f, uint32_t flags, float k) {
+    uint32_t comb = (flags >> 16) & 3u;
+    if (comb == 0u) return dmin(acc, f);
+    if (comb == 1u) {
+        if (k <= 0.0f) return dmin(acc, f);
+        D h = dclamp(dadds(dscale(dsub(f, acc), 0.5f / k), 0.5f), 0.0f, 1.0f);
+        D omh = dsub(dc(1.0f), h);
+        return dsub(dadd(dmul(f, omh), dmul(acc, h)), dscale(dmul(h, omh), k));
+    }
+    return dmax(acc, dneg(f));
+}
+// Scene::normal_dual (lib.rs:820-835): every object, no pruning.
 static __device__ __noinline__ V normal_dual(const DevObject* objs, uint32_t n, V p) {
     if (n == 0) return V{0.f, 0.f, 0.f};
     D acc = object_dual(objs[0], p);
     for (uint32_t i = 1; i < n; ++i) {
         const DevObject& o = objs[i];
-        D f = object_dual(o, p);
-        uint32_t comb = (o.flags >> 16) & 3u;
-        if (comb == 0u) {
-            acc = dmin(acc, f);
-        } else if (comb == 1u) {
-            if (o.k <= 0.0f) {
-                acc = dmin(acc, f);
-            } else {
-                D h = dclamp(dadds(dscale(dsub(f, acc), 0.5f / o.k), 0.5f), 0.0f, 1.0f);
-                D omh = dsub(dc(1.0f), h);
-                acc = dsub(dadd(dmul(f, omh), dmul(acc, h)), dscale(dmul(h, omh), o.k));
-            }
-        } else {
-            acc = dmax(acc, dneg(f));
-        }
+        acc = dual_fold(acc, object_dual(o, p), o.flags, o.k);
     }
     return normalize(acc.g);
 }

@@ -224,6 +224,8 @@ WaveArgs wave_args(const PassPlan& plan, PassBuffers& buf, const TuneParams& tun
     a.b.hdr = buf.hdr;
     a.b.fg = buf.fg;
     a.film = plan.film ? 1u : 0u;
+    a.wait_limit = plan.wait_limit;
+    a.wait_probe = plan.wait_probe;
     return a;
 }
 }  // namespace

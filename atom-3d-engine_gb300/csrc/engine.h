@@ -128,6 +128,8 @@ struct PassPlan {
     // Primary rays from queue a (count in this device word, outside buf.counters) instead of
     // the jobs' camera samples; sample k of the queue is queue entry k. The caller resolves.
     const uint32_t* queue0 = nullptr;
+    uint32_t wait_limit = 0;        // tape-staging wait limit and probe mode (WaveArgs)
+    uint32_t wait_probe = 0;
 };
 
 // Enqueues the passes on `s`: counters cleared, march / AO / shadow / shade per level,

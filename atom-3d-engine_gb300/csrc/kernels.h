@@ -110,6 +110,8 @@ struct WaveArgs {
     uint32_t aov_mode;          // RenderMode for the AOV resolve
     uint32_t emit;              // shade appends reflection rays (else a reflect pass did)
     uint32_t film;              // resolve also writes coverage (hdr.w) and the foreground (b.fg)
+    uint32_t wait_limit;        // iterations of the tape-staging wait before it gives up (0: 2^22)
+    uint32_t wait_probe;        // 1: issue no tape copy, so the staging wait runs to its limit
 };
 
 // Status bits written by kernels.

@@ -16,9 +16,26 @@
 namespace mm3e {
 namespace wave {
 
-// The tape interpreter's world field (WorldPlan::eval, accel.rs:209-252).
+// The tape interpreter's world field (WorldPlan::eval, accel.rs:209-252), the marcher settings
+// read from the tape header, and the exact-gradient normal over the tape's objects. A
+// scene-specialised program supplies a class with the same members that returns its scene's
+// settings as constants, so the pass bodies fold their branches on them.
 struct InterpField {
     static __device__ __forceinline__ Field eval(const Tape& T, V p) { return world_eval(T, p); }
+    static __device__ __forceinline__ V normal_dual(const Tape& T, V p) {
+        return mm3e::normal_dual(T.obj, T.h->n_objects, p);
+    }
+    static __device__ __forceinline__ uint32_t flags(const TapeHeader& h) { return h.flags; }
+    static __device__ __forceinline__ uint32_t max_steps(const TapeHeader& h) { return h.max_steps; }
+    static __device__ __forceinline__ uint32_t shadow_steps(const TapeHeader& h) { return h.shadow_steps; }
+    static __device__ __forceinline__ uint32_t ao_samples(const TapeHeader& h) { return h.ao_samples; }
+    static __device__ __forceinline__ uint32_t n_lights(const TapeHeader& h) { return h.n_lights; }
+    static __device__ __forceinline__ float max_dist(const TapeHeader& h) { return h.max_dist; }
+    static __device__ __forceinline__ float eps(const TapeHeader& h) { return h.eps; }
+    static __device__ __forceinline__ float step_scale(const TapeHeader& h) { return h.step_scale; }
+    static __device__ __forceinline__ float lod_footprint(const TapeHeader& h) { return h.lod_footprint; }
+    static __device__ __forceinline__ float subitize(const TapeHeader& h) { return h.subitize; }
+    static __device__ __forceinline__ float normal_h(const TapeHeader& h) { return h.normal_h; }
 };
 
 
@@ -45,6 +62,14 @@ template <int FIELD> __device__ __forceinline__ uint32_t find_job(const FrameJob
     return lo;
 }
 
+// Whether an earlier pass of this call gave up (its tape staging timed out or found a corrupt
+// tape): the passes after it then do nothing, since the hit records they would read were never
+// written, and the call reports the error. The word is constant while a pass runs (only earlier
+// launches in stream order write it), so the early return is uniform.
+__device__ __forceinline__ bool pass_failed(const WaveArgs& a) {
+    return a.status && (*(volatile const uint32_t*)a.status & (ST_TAPE_TIMEOUT | ST_TAPE_CORRUPT)) != 0u;
+}
+
 // Job of a queue slot (its index is carried in the ray direction's w).
 __device__ __forceinline__ uint32_t slot_job(const WaveArgs& a, uint32_t slot) {
     return a.jobs ? __float_as_uint(a.b.q_d[slot].w) : 0u;
@@ -67,9 +92,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, uint32
 }
 
 // Stage the tape into shared memory: TMA bulk copies (<= 32 KB each) completing on one
-// mbarrier, waited on with an iteration limit. Returns false (status word set) on failure.
+// mbarrier, waited on with an iteration limit (`limit`, 0: 2^22). Returns false (status word
+// set) on failure. A wait that gives up while copies were issued waits again, with a longer
+// limit, for them to land, so the CTA does not return with a copy still writing its shared
+// memory. With `probe` nothing arrives on the barrier and no copy is issued: the wait runs to
+// its limit with nothing in flight (a test of the give-up path).
 __device__ __forceinline__ bool stage_tape(unsigned char* smem, const unsigned char* tape, uint32_t bytes,
-                                           uint32_t* status) {
+                                           uint32_t* status, uint32_t limit, bool probe) {
     __shared__ __align__(8) uint64_t mbar_storage;
     __shared__ uint32_t tape_ok;
     uint32_t mbar = (uint32_t)__cvta_generic_to_shared(&mbar_storage);
@@ -81,7 +110,7 @@ __device__ __forceinline__ bool stage_tape(unsigned char* smem, const unsigned c
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !probe) {
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
         for (uint32_t off = 0; off < bytes; off += 32768u) {
             uint32_t n = bytes - off < 32768u ? bytes - off : 32768u;
@@ -92,7 +121,10 @@ __device__ __forceinline__ bool stage_tape(unsigned char* smem, const unsigned c
                 : "memory");
         }
     }
-    if (!mbar_wait(mbar, 0u, 1u << 22)) tape_ok = 0u;
+    if (!mbar_wait(mbar, 0u, limit ? limit : (1u << 22))) {
+        tape_ok = 0u;
+        if (!probe) mbar_wait(mbar, 0u, 1u << 26);  // the issued copies land before the CTA leaves
+    }
     __syncthreads();
     bool ok = tape_ok && reinterpret_cast<const TapeHeader*>(smem)->magic == TAPE_MAGIC;
     if (!ok && threadIdx.x == 0) atomicOr(status, tape_ok ? ST_TAPE_CORRUPT : ST_TAPE_TIMEOUT);
@@ -231,7 +263,7 @@ __device__ __forceinline__ void m_write(MLane& L, const WaveArgs& a, bool hit, V
 }
 
 // Start the lane's ray for its fresh item; false when the item needs no march.
-template <int TM>
+template <int TM, class FP>
 __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveArgs& a) {
     uint32_t job = 0;
     if (a.src == SRC_SAMPLES) {
@@ -289,14 +321,14 @@ __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveAr
     L.step = 0.0f;
     L.t_prev = 0.0f;
     L.d_prev = __int_as_float(0x7f800000);
-    bool lip = h.step_scale >= 1.0f;
-    L.omega = lip ? 1.4f : h.step_scale;
-    L.subz = lip ? h.subitize : 0.0f;
-    L.secant_on = ((h.flags & SF_SECANT) && lip) ? 1u : 0u;
+    bool lip = FP::step_scale(h) >= 1.0f;
+    L.omega = lip ? 1.4f : FP::step_scale(h);
+    L.subz = lip ? FP::subitize(h) : 0.0f;
+    L.secant_on = ((FP::flags(h) & SF_SECANT) && lip) ? 1u : 0u;
     L.boost = BOOST_OMEGA;
     L.i = 0;
     L.phase = M_MARCH;
-    if (h.max_steps == 0) {
+    if (FP::max_steps(h) == 0) {
         m_write(L, a, false, V{0.f, 0.f, 0.f}, 0u);
         return false;
     }
@@ -308,11 +340,11 @@ template <int TM, class FP>
 __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const WaveArgs& a) {
     const Tape T = LT.get();
     const TapeHeader& h = *T.h;
-    const uint32_t max_steps = h.max_steps;
+    const uint32_t max_steps = FP::max_steps(h);
     V p;
     if (L.phase == M_MARCH) p = m_at(L, L.t);
     else if (L.phase == M_COVER) p = m_at(L, 0.5f * ((L.t_prev + L.prev_r) + (L.t - L.x1)));
-    else p = m_at(L, L.t) + scale(tetra_k(L.xu), h.normal_h);
+    else p = m_at(L, L.t) + scale(tetra_k(L.xu), FP::normal_h(h));
     Field f = FP::eval(T, p);
     if (L.phase == M_TETRA) {
         V kd = scale(tetra_k(L.xu), f.d);
@@ -331,7 +363,7 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         d = f.d;
         m = f.m;
         radius = fabsf(d);
-        e = h.eps * (1.0f + L.t * 0.5f) + h.lod_footprint * L.t;
+        e = FP::eps(h) * (1.0f + L.t * 0.5f) + FP::lod_footprint(h) * L.t;
         bool overlap_fail = (L.step > 0.0f && d < 0.0f) || L.step > radius + L.prev_r;
         if (overlap_fail && d > 0.0f) {  // check the gap midpoint first
             L.x0 = d;
@@ -355,8 +387,8 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
     // march.rs:173-206
     if (d < e) {
         L.hmat = m;
-        if (h.flags & SF_DUAL_SAFE) {
-            m_write(L, a, true, normal_dual(T.obj, h.n_objects, m_at(L, L.t)), L.i);
+        if (FP::flags(h) & SF_DUAL_SAFE) {
+            m_write(L, a, true, FP::normal_dual(T, m_at(L, L.t)), L.i);
         } else {
             L.phase = M_TETRA;
             L.xu = 0;
@@ -384,7 +416,7 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         L.d_prev = d;
         L.t_prev = L.t;
         L.t = L.t + step_len;
-        if (L.t > h.max_dist) {
+        if (L.t > FP::max_dist(h)) {
             m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
             return;
         }
@@ -410,7 +442,7 @@ __device__ __forceinline__ void march_body(const WaveArgs& a) {
     extern __shared__ __align__(128) unsigned char smem[];
     LaneTape<TM> LT;
     if constexpr (TM == TM_SMEM) {
-        if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status)) return;
+        if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status, a.wait_limit, a.wait_probe != 0u)) return;
         LT.T = tape_view(smem);
     } else {
         LT.p = a.job0.tape;
@@ -424,7 +456,7 @@ __device__ __forceinline__ void march_body(const WaveArgs& a) {
         bool fresh;
         refill(L.item, retired, n, a.counter, fresh);
         if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
-        if (fresh && !m_start(L, LT, a)) continue;
+        if (fresh && !m_start<TM, FP>(L, LT, a)) continue;
 #pragma unroll 1
         for (int u = 0; u < UNROLL; ++u) {
             if (L.phase == M_IDLE) break;
@@ -445,16 +477,16 @@ __device__ __forceinline__ void ao_slot(const WaveArgs& a, uint32_t slot) {
     }
     const Tape T = tape_view(job_ref(a, slot_job(a, slot)).tape);
     const TapeHeader& h = *T.h;
-    uint32_t ns = h.ao_samples;
+    uint32_t ns = FP::ao_samples(h);
     // A table of jobs runs AO for every job; the shading of a job without AO ignores it.
-    if (ns == 0 || (a.jobs && !(h.flags & SF_AO))) {
+    if (ns == 0 || (a.jobs && !(FP::flags(h) & SF_AO))) {
         a.b.occ[slot] = 1.0f;
         return;
     }
     float4 hn4 = a.b.h_n[slot], o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
     V hp = V{o4.x, o4.y, o4.z} + scale(V{d4.x, d4.y, d4.z}, hn4.w);
     V n{hn4.x, hn4.y, hn4.z};
-    float base = fmaxf(h.normal_h, 0.01f);
+    float base = fmaxf(FP::normal_h(h), 0.01f);
     float span = (float)((ns > 2u ? ns : 2u) - 1u);
     float occ = 0.0f, sca = 1.0f;
     for (uint32_t i = 0; i < ns; ++i) {
@@ -468,6 +500,7 @@ __device__ __forceinline__ void ao_slot(const WaveArgs& a, uint32_t slot) {
 
 template <class FP>
 __device__ __forceinline__ void ao_body(const WaveArgs& a) {
+    if (pass_failed(a)) return;
     const uint32_t n = item_count(a);
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < n; slot += gridDim.x * blockDim.x)
         ao_slot<FP>(a, slot);
@@ -482,7 +515,7 @@ struct SLane {
     float st, sres, sk, smax;
 };
 
-template <int TM>
+template <int TM, class FP>
 __device__ __forceinline__ bool s_start(SLane& S, LaneTape<TM>& LT, const WaveArgs& a, uint32_t n_slots) {
     // Work items run light-major (all hits' rays toward light 0, then light 1, ...), so a warp's
     // rays share a direction and pass the same objects; results keep the slot-major layout.
@@ -496,7 +529,7 @@ __device__ __forceinline__ bool s_start(SLane& S, LaneTape<TM>& LT, const WaveAr
         LT.set(job_ref(a, job).tape);
         const Tape T = LT.get();
         const TapeHeader& h = *T.h;
-        if (li < h.n_lights && (h.flags & SF_SHADOWS) && h.shadow_steps > 0) {
+        if (li < FP::n_lights(h) && (FP::flags(h) & SF_SHADOWS) && FP::shadow_steps(h) > 0) {
             V hp = V{o4.x, o4.y, o4.z} + scale(V{d4.x, d4.y, d4.z}, hn4.w);
             V hn{hn4.x, hn4.y, hn4.z};
             const DevLight& lt = T.light[li];
@@ -504,10 +537,10 @@ __device__ __forceinline__ bool s_start(SLane& S, LaneTape<TM>& LT, const WaveAr
             float ldist;
             light_toward(lt, hp, ldir, ldist);
             if (fmaxf(dot(hn, ldir), 0.0f) > 0.0f) {  // lib.rs:1315-1322
-                float lift = fmaxf(h.normal_h * 2.0f, 0.01f);
+                float lift = fmaxf(FP::normal_h(h) * 2.0f, 0.01f);
                 S.so = hp + scale(hn, lift);
                 S.sdir = ldir;
-                S.smax = fminf(ldist, h.max_dist);
+                S.smax = fminf(ldist, FP::max_dist(h));
                 S.sk = light_shadow_k(lt, ldist);
                 float hb = S.so.x * 127.1f + S.so.y * 311.7f + S.so.z * 74.7f;
                 float sv = sinf(hb) * 43758.547f;
@@ -539,7 +572,7 @@ __device__ __forceinline__ void s_step(SLane& S, const LaneTape<TM>& LT, const W
     if (!(kh > S.sres * S.st * 1.00000095f)) S.sres = fminf(S.sres, kh / S.st);
     S.st = S.st + clampf(hh, 0.06f, 0.5f + 0.7f * S.st);
     S.si += 1;
-    if (S.st > S.smax || S.si >= T.h->shadow_steps) {
+    if (S.st > S.smax || S.si >= FP::shadow_steps(*T.h)) {
         a.b.shadow[S.item] = clampf(S.sres, 0.0f, 1.0f);
         S.item = NIL;
     }
@@ -550,7 +583,7 @@ __device__ __forceinline__ void shadow_body(const WaveArgs& a) {
     extern __shared__ __align__(128) unsigned char smem[];
     LaneTape<TM> LT;
     if constexpr (TM == TM_SMEM) {
-        if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status)) return;
+        if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status, a.wait_limit, a.wait_probe != 0u)) return;
         LT.T = tape_view(smem);
     } else {
         LT.p = a.job0.tape;
@@ -564,7 +597,7 @@ __device__ __forceinline__ void shadow_body(const WaveArgs& a) {
         bool fresh;
         refill(S.item, retired, n, a.counter, fresh);
         if (__ballot_sync(0xFFFFFFFFu, !retired) == 0u) break;
-        if (fresh && !s_start(S, LT, a, n_slots)) continue;
+        if (fresh && !s_start<TM, FP>(S, LT, a, n_slots)) continue;
 #pragma unroll 1
         for (int u = 0; u < UNROLL; ++u) {
             if (S.item == NIL) break;

@@ -93,15 +93,89 @@ std::string farr(const float* f, int n) {
     return s + "}";
 }
 
+// The initializer of an object record, every float by its bits.
+std::string object_rec(const DevObject& o) {
+    std::ostringstream os;
+    os << "{" << farr(o.rot, 9) << ", " << farr(o.pos, 3) << ", " << fbits(o.inv) << ", " << fbits(o.scale) << ", "
+       << farr(o.params, 7) << ", " << o.prim << "u, " << o.mat << "u, " << o.flags << "u, " << o.aux << "u, "
+       << fbits(o.k) << ", " << farr(o.elongate, 3) << ", " << farr(o.repeat, 3) << ", " << fbits(o.twist) << ", "
+       << fbits(o.bend) << ", " << fbits(o.round) << ", " << fbits(o.onion) << ", " << farr(o.bc, 3) << ", "
+       << fbits(o.br) << "}";
+    return os.str();
+}
+
 std::string object_fn(uint32_t i, const DevObject& o) {
     std::ostringstream os;
     os << "__device__ __forceinline__ Field obj_" << i << "(const Tape& T, V p) {\n"
-       << "    const DevObject o = {" << farr(o.rot, 9) << ", " << farr(o.pos, 3) << ", " << fbits(o.inv) << ", "
-       << fbits(o.scale) << ", " << farr(o.params, 7) << ", " << o.prim << "u, " << o.mat << "u, " << o.flags << "u, "
-       << o.aux << "u, " << fbits(o.k) << ", " << farr(o.elongate, 3) << ", " << farr(o.repeat, 3) << ", "
-       << fbits(o.twist) << ", " << fbits(o.bend) << ", " << fbits(o.round) << ", " << fbits(o.onion) << ", "
-       << farr(o.bc, 3) << ", " << fbits(o.br) << "};\n"
+       << "    const DevObject o = " << object_rec(o) << ";\n"
        << "    return object_field(T, o, p);\n}\n";
+    return os.str();
+}
+
+// Leaves (object indices) of the BVH below node `root`.
+void bvh_leaves(const DevNode* node, uint32_t n_nodes, uint32_t root, std::vector<uint32_t>& out) {
+    if (root == NIL || root >= n_nodes) return;
+    std::vector<uint32_t> todo{root};
+    while (!todo.empty()) {
+        uint32_t k = todo.back();
+        todo.pop_back();
+        const DevNode& nd = node[k];
+        if (nd.leaf >= 0) {
+            out.push_back((uint32_t)nd.leaf);
+            continue;
+        }
+        if (nd.left >= 0 && (uint32_t)nd.left < n_nodes) todo.push_back((uint32_t)nd.left);
+        if (nd.right >= 0 && (uint32_t)nd.right < n_nodes) todo.push_back((uint32_t)nd.right);
+    }
+    std::sort(out.begin(), out.end());
+}
+
+// A plain-union run's Bvh::query (accel.rs:79-119) as generated code: bvh_segment's steps (its
+// unbounded members exactly in list order, then the sphere BVH near child first with the
+// `lower > best` prune and the `lower > slack` substitute, (distance, lowest index) fold), with
+// the run's objects dispatched to their inlined fields. Inlined at its call site, so the
+// specialised kernels make no function call (a call there costs a stack frame and spills).
+std::string walk_fn(uint32_t s, const DevSegment& sg, const DevNode* node, uint32_t n_nodes, const uint32_t* unb,
+                    float slack, bool seeded) {
+    std::ostringstream os;
+    os << "__device__ __forceinline__ Field walk_" << s << "(const Tape& T, V p, Field acc) {\n"
+       << "    const float INF = __int_as_float(0x7f800000);\n"
+       << "    float bd = " << (seeded ? "acc.d" : "INF") << ";\n    int32_t bi = " << (seeded ? "-1" : "0x7FFFFFFF")
+       << ";\n    uint32_t bm = " << (seeded ? "acc.m" : "0u") << ";\n";
+    for (uint32_t u = sg.ua; u < sg.ua + sg.ub; ++u)
+        os << "    {\n        Field f = obj_" << unb[u] << "(T, p);\n        if (f.d < bd || (f.d == bd && " << unb[u]
+           << " < bi)) {\n            bd = f.d;\n            bi = " << unb[u] << ";\n            bm = f.m;\n        }\n    }\n";
+    std::vector<uint32_t> leaves;
+    bvh_leaves(node, n_nodes, sg.c, leaves);
+    if (!leaves.empty()) {
+        os << "    NodeStack stk;\n    stk.clear();\n    stk.push(" << sg.c << "u);\n"
+           << "    while (stk.n > 0) {\n"
+           << "        const DevNode& nd = T.node[stk.pop()];\n"
+           << "        const float nd2 = length_sq(p - V{nd.cx, nd.cy, nd.cz});\n"
+           << "        if (far_beyond(nd2, bd, nd.r)) continue;\n"
+           << "        const float lower = sqrtf(nd2) - nd.r;\n"
+           << "        if (lower > bd) continue;\n"
+           << "        if (nd.leaf >= 0) {\n"
+           << "            const int32_t i = nd.leaf;\n"
+           << "            if (lower > " << fbits(slack) << ") {\n"
+           << "                if (lower < bd || (lower == bd && i < bi)) {\n"
+           << "                    bd = lower;\n                    bi = i;\n                    bm = T.obj[i].mat;\n"
+           << "                }\n                continue;\n            }\n"
+           << "            Field f;\n            switch (i) {\n";
+        for (uint32_t i : leaves) os << "                case " << i << ": f = obj_" << i << "(T, p); break;\n";
+        os << "                default: f = Field{INF, 0u}; break;\n            }\n"
+           << "            if (f.d < bd || (f.d == bd && i < bi)) {\n"
+           << "                bd = f.d;\n                bi = i;\n                bm = f.m;\n            }\n"
+           << "            continue;\n        }\n"
+           << "        const DevNode& L = T.node[nd.left];\n        const DevNode& R = T.node[nd.right];\n"
+           << "        const float ld = length_sq(p - V{L.cx, L.cy, L.cz});\n"
+           << "        const float rd = length_sq(p - V{R.cx, R.cy, R.cz});\n"
+           << "        const bool lnear = ld <= rd;\n"
+           << "        stk.push(lnear ? (uint32_t)nd.right : (uint32_t)nd.left);\n"
+           << "        stk.push(lnear ? (uint32_t)nd.left : (uint32_t)nd.right);\n"
+           << "    }\n";
+    }
+    os << "    return Field{bd, bm};\n}\n";
     return os.str();
 }
 
@@ -310,15 +384,37 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
           "typedef unsigned short uint16_t;\ntypedef unsigned char uint8_t;\ntypedef long long int64_t;\n"
           "#include \"march_kernels.cuh\"\n"
           "namespace mm3e {\nnamespace spec {\n";
+    const DevNode* node = reinterpret_cast<const DevNode*>(blob.data() + h->off_nodes);
+    // segments that need the BVH walk: big runs, and LINEAR runs with a non-conservative member
+    // (whose winner may undercut its sphere)
+    std::vector<bool> walk(h->n_segments, false);
+    for (uint32_t s = 0; s < h->n_segments; ++s) {
+        const DevSegment& sg = seg[s];
+        if (sg.kind == SEG_RUN) walk[s] = true;
+        if (sg.kind == SEG_LINEAR)
+            for (uint32_t k = 0; k < sg.b; ++k) {
+                const DevObject& o = obj[unb[sg.a + k]];
+                if ((o.flags & OF_NONCONS) && (o.flags & OF_BOUND)) walk[s] = true;
+            }
+    }
     std::vector<bool> used(h->n_objects, false);
     for (uint32_t s = 0; s < h->n_segments; ++s) {
         const DevSegment& sg = seg[s];
         if (sg.kind == SEG_ONE) used[sg.a] = true;
         if (sg.kind == SEG_LINEAR)
             for (uint32_t k = 0; k < sg.b; ++k) used[unb[sg.a + k]] = true;
+        if (walk[s]) {
+            for (uint32_t u = sg.ua; u < sg.ua + sg.ub; ++u) used[unb[u]] = true;
+            std::vector<uint32_t> leaves;
+            bvh_leaves(node, h->n_nodes, sg.c, leaves);
+            for (uint32_t i : leaves)
+                if (i < h->n_objects) used[i] = true;
+        }
     }
     for (uint32_t i = 0; i < h->n_objects; ++i)
         if (used[i]) os << object_fn(i, obj[i]);
+    for (uint32_t s = 0; s < h->n_segments; ++s)
+        if (walk[s]) os << walk_fn(s, seg[s], node, h->n_nodes, unb, h->slack, s > 0);
     const std::string slack = fbits(h->slack);
     os << "__device__ __forceinline__ Field eval(const Tape& T, V p) {\n"
           "    const float INF = __int_as_float(0x7f800000);\n"
@@ -449,18 +545,52 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             }
             for (uint32_t i : weak) member(i, false);
             if (any_noncons)
-                os << "        if (bnc) acc = bvh_segment(T, " << s << "u, p, " << (seeded ? "true" : "false")
-                   << ", acc);\n        else acc = Field{bd, bm};\n";
+                os << "        if (bnc) acc = walk_" << s << "(T, p, acc);\n        else acc = Field{bd, bm};\n";
             else
                 os << "        acc = Field{bd, bm};\n";
         } else {
-            os << "        acc = bvh_segment(T, " << s << "u, p, " << (seeded ? "true" : "false") << ", acc);\n";
+            os << "        acc = walk_" << s << "(T, p, acc);\n";
         }
         os << "    }\n";
     }
-    os << "    return acc;\n}\n"
-          "struct Field_ {\n    static __device__ __forceinline__ Field eval(const Tape& T, V p) { return spec::eval(T, p); }\n};\n"
-          "}  // namespace spec\n}  // namespace mm3e\n";
+    os << "    return acc;\n}\n";
+    // Scene::normal_dual (lib.rs:820-835) over the scene's objects with their records inlined
+    // (only reached when the scene is dual-safe)
+    os << "__device__ __forceinline__ V normal_dual(V p) {\n";
+    if ((h->flags & SF_DUAL_SAFE) && h->n_objects > 0) {
+        os << "    D acc;\n";
+        for (uint32_t i = 0; i < h->n_objects; ++i) {
+            os << "    {\n        const DevObject o = " << object_rec(obj[i]) << ";\n";
+            if (i == 0) os << "        acc = object_dual<true>(o, p);\n";
+            else os << "        acc = dual_fold(acc, object_dual<true>(o, p), o.flags, o.k);\n";
+            os << "    }\n";
+        }
+        os << "    return normalize(acc.g);\n}\n";
+    } else {
+        os << "    return V{0.f, 0.f, 0.f};\n}\n";
+    }
+    // the field class of the pass bodies: the field above, and the scene's marcher settings as
+    // constants (the tape header's values, which the scene's tape keeps while it is specialised)
+    auto u = [](uint32_t v) { return std::to_string(v) + "u"; };
+    os << "struct Field_ {\n"
+          "    static __device__ __forceinline__ Field eval(const Tape& T, V p) { return spec::eval(T, p); }\n"
+          "    static __device__ __forceinline__ V normal_dual(const Tape&, V p) { return spec::normal_dual(p); }\n"
+       << "    static __device__ __forceinline__ uint32_t flags(const TapeHeader&) { return " << u(h->flags) << "; }\n"
+       << "    static __device__ __forceinline__ uint32_t max_steps(const TapeHeader&) { return " << u(h->max_steps) << "; }\n"
+       << "    static __device__ __forceinline__ uint32_t shadow_steps(const TapeHeader&) { return " << u(h->shadow_steps)
+       << "; }\n"
+       << "    static __device__ __forceinline__ uint32_t ao_samples(const TapeHeader&) { return " << u(h->ao_samples)
+       << "; }\n"
+       << "    static __device__ __forceinline__ uint32_t n_lights(const TapeHeader&) { return " << u(h->n_lights) << "; }\n"
+       << "    static __device__ __forceinline__ float max_dist(const TapeHeader&) { return " << fbits(h->max_dist) << "; }\n"
+       << "    static __device__ __forceinline__ float eps(const TapeHeader&) { return " << fbits(h->eps) << "; }\n"
+       << "    static __device__ __forceinline__ float step_scale(const TapeHeader&) { return " << fbits(h->step_scale)
+       << "; }\n"
+       << "    static __device__ __forceinline__ float lod_footprint(const TapeHeader&) { return " << fbits(h->lod_footprint)
+       << "; }\n"
+       << "    static __device__ __forceinline__ float subitize(const TapeHeader&) { return " << fbits(h->subitize) << "; }\n"
+       << "    static __device__ __forceinline__ float normal_h(const TapeHeader&) { return " << fbits(h->normal_h) << "; }\n"
+       << "};\n}  // namespace spec\n}  // namespace mm3e\n";
     const int tm = smem_tape ? 0 : 1;
     const std::string bounds = min_blocks ? std::to_string(block) + ", " + std::to_string(min_blocks) : std::to_string(block);
     // With no explicit register budget the march kernel still asks for 7 CTAs of 128 (3 of 256)

@@ -107,6 +107,7 @@ __device__ __forceinline__ void shade_slots(const WaveArgs& a, uint32_t slot, bo
 }
 
 __global__ void __launch_bounds__(SHADE_THREADS) k_shade(const __grid_constant__ WaveArgs a) {
+    if (pass_failed(a)) return;
     const uint32_t n = item_count(a);
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
         shade_slots(a, base + threadIdx.x, base + threadIdx.x < n);  // block-uniform trip count
@@ -154,6 +155,7 @@ __device__ __forceinline__ void reflect_slots(const WaveArgs& a, uint32_t slot, 
 }
 
 __global__ void __launch_bounds__(SHADE_THREADS) k_reflect(const __grid_constant__ WaveArgs a) {
+    if (pass_failed(a)) return;
     const uint32_t n = item_count(a);
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x)
         reflect_slots(a, base + threadIdx.x, base + threadIdx.x < n);
@@ -205,6 +207,7 @@ __device__ __forceinline__ void resolve_slot(const WaveArgs& a, uint32_t slot, u
 }
 
 __global__ void __launch_bounds__(SHADE_THREADS) k_resolve(const __grid_constant__ WaveArgs a, uint32_t n_slots) {
+    if (pass_failed(a)) return;
     uint32_t nj = 1;
     if (a.jobs) {
         n_slots = a.totals->n_slots;
@@ -216,6 +219,7 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_resolve(const __grid_constant
 
 // AOV display values (lib.rs:1185-1217) for pixel-centre hits of job 0 (row-major slots).
 __global__ void __launch_bounds__(SHADE_THREADS) k_aov(const __grid_constant__ WaveArgs a, float4* out) {
+    if (pass_failed(a)) return;
     const Tape T = tape_view(a.job0.tape);
     const TapeHeader& h = *T.h;
     uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
@@ -250,6 +254,7 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_aov(const __grid_constant__ W
 
 // Scene::gather (lib.rs:686-711): emissive + unshadowed direct light, or the diffuse sky.
 __global__ void __launch_bounds__(SHADE_THREADS) k_gather_shade(const __grid_constant__ WaveArgs a, float4* radiance) {
+    if (pass_failed(a)) return;
     const Tape T = tape_view(a.job0.tape);
     const TapeHeader& h = *T.h;
     uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;

@@ -85,6 +85,11 @@ class Context:
         self.check(lib().mm3e_ctx_set_host_writes(self._ptr, 1 if on else 0, C.byref(active)))
         return bool(active.value)
 
+    def set_tape_wait(self, limit=0, probe=False):
+        """Iteration limit of the kernels' tape-staging wait (0: the default); probe=True issues no
+        tape copy so that the wait runs out (renders then fail with ERR_TIMEOUT)."""
+        self.check(lib().mm3e_ctx_set_tape_wait(self._ptr, int(limit), 1 if probe else 0))
+
     def kernel_times(self):
         """{kind: (launches, ms)} of the passes run since the last call (profiling on)."""
         arr = (abi.KernelTime * 16)()

@@ -67,6 +67,7 @@ def _declare_extra(lib):
         "mm3e_ctx_get_tuning": (C.c_int, [C.c_void_p, P(abi.Tuning)]),
         "mm3e_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
         "mm3e_ctx_set_host_writes": (C.c_int, [C.c_void_p, C.c_int, P(C.c_int)]),
+        "mm3e_ctx_set_tape_wait": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int]),
         "mm3e_ctx_kernel_times": (C.c_int, [C.c_void_p, P(abi.KernelTime), C.c_uint32, P(C.c_uint32)]),
         "mm3e_scene_device_bytes": (C.c_int, [C.c_void_p, P(C.c_size_t)]),
         "mm3e_batch_configure": (C.c_int, [C.c_void_p, P(abi.BatchConfig)]),

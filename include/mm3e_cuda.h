@@ -357,6 +357,14 @@ int mm3e_ctx_set_profiling(mm3e_ctx* ctx, int enable);
  * staged through pinned memory. Frames are identical either way. *active (may be NULL) receives
  * 1 when direct writes are in use. */
 int mm3e_ctx_set_host_writes(mm3e_ctx* ctx, int enable, int* active);
+/* The march and shadow kernels stage the scene tape into shared memory and wait for it on an
+ * mbarrier with an iteration limit (the reference bounds every loop, march.rs:142,248; a device
+ * wait here is bounded the same way): when the limit runs out the kernel records
+ * MM3E_ERR_TIMEOUT for the call and returns, and the context stays usable. `limit` sets the
+ * iterations of that wait for this context's plain calls (0: the default, 2^22). With probe = 1
+ * the kernels issue no tape copy, so the wait runs to its limit with nothing in flight: a test of
+ * the give-up path (every render then fails with MM3E_ERR_TIMEOUT until probe is set back to 0). */
+int mm3e_ctx_set_tape_wait(mm3e_ctx* ctx, uint32_t limit, int probe);
 int mm3e_ctx_kernel_times(mm3e_ctx* ctx, mm3e_kernel_time* out, uint32_t cap, uint32_t* n_out);
 
 /* ---- scenes ------------------------------------------------------------------------------- */
