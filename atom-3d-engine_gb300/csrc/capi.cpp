@@ -1261,10 +1261,12 @@ int mm3e_march_rays_noalloc(mm3e_scene* s, const float* d_rays6, size_t n, float
                             uint32_t* d_steps) {
     if (!s || (n && (!d_rays6 || !d_t || !d_mat))) return MM3E_ERR_INVALID;
     mm3e_ctx* c = s->ctx;
-    cudaSetDevice(c->device);
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mm3e_march_rays_noalloc: selecting the context's device");
     const char* what = "";
-    int rc = noalloc_march_rays(s->d_tape, (uint32_t)s->low.blob.size(), c->device, c->sm_count, c->stream, d_rays6, n,
-                                d_t, d_mat, d_steps, &what);
+    // the launch shape of mm3e_march_rays (the context's), so both calls march identically
+    int rc = noalloc_march_rays(s->d_tape, (uint32_t)s->low.blob.size(), c->device, c->sm_count, c->stream, c->tune,
+                                d_rays6, n, d_t, d_mat, d_steps, &what);
     if (rc == 1) return fail(c, MM3E_ERR_INVALID, what);
     if (rc == 2) return fail(c, MM3E_ERR_CUDA, what);
     if (rc == 3) return fail(c, MM3E_ERR_TIMEOUT, what);

@@ -56,9 +56,15 @@ __global__ void k_split_hits(const float4* __restrict__ hn, const uint2* __restr
     if (steps) steps[i] = m.y;
 }
 
-// Set-up, once per device, with that device current: resolve the array's device address.
+// Set-up, once per device, with that device current: resolve the array's device address. The
+// address is cached for the life of the process's context on that device; cudaDeviceReset
+// ends that context (and every scene and stream of this library on it) and invalidates it.
 cudaError_t scratch_for(int device, NoAllocScratch** out) {
     if (device < 0 || device >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    int current = -1;
+    cudaError_t ce = cudaGetDevice(&current);
+    if (ce != cudaSuccess) return ce;
+    if (current != device) return cudaErrorInvalidDevice;  // the address is per device
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_addr[device]) {
         void* p = nullptr;
@@ -73,8 +79,8 @@ cudaError_t scratch_for(int device, NoAllocScratch** out) {
 }  // namespace
 
 int noalloc_march_rays(const unsigned char* tape, uint32_t tape_bytes, int device, int sm_count, cudaStream_t stream,
-                       const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat, uint32_t* d_steps,
-                       const char** what) {
+                       const TuneParams& tune, const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat,
+                       uint32_t* d_steps, const char** what) {
     *what = "";
     if (n == 0) return 0;
     if (n > NOALLOC_MAX_RAYS) {
@@ -107,7 +113,7 @@ int noalloc_march_rays(const unsigned char* tape, uint32_t tape_bytes, int devic
         a.b.q_d = s->q_d;
         a.b.h_n = s->h_n;
         a.b.h_m = s->h_m;
-        e = launch_march(a, TuneParams{}, stream, sm_count, nullptr);
+        e = launch_march(a, tune, stream, sm_count, nullptr);
     }
     if (e == cudaSuccess) {
         k_split_hits<<<blocks, 128, 0, stream>>>(s->h_n, s->h_m, nn, d_t, d_mat, d_steps);

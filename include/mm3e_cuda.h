@@ -609,6 +609,10 @@ void mm3e_server_destroy(mm3e_server* srv);
  * MM3E_ERR_INVALID). The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture. Every call shares the
  * array and overwrites it; calls that overlap on the GPU race on it, so serialise them.
+ * The call runs on the context's stream (the caller's own stream after mm3e_ctx_set_stream):
+ * d_rays6 must be complete before it runs, so either synchronise the work that writes it first
+ * or write it on the stream given to mm3e_ctx_set_stream. cudaDeviceReset invalidates the cached
+ * array address along with every context and scene of this library on that device.
  * Blocking: returns after the results are written. */
 int mm3e_march_rays_noalloc(mm3e_scene* scene, const float* d_rays6, size_t n, float* d_t, uint32_t* d_mat,
                             uint32_t* d_steps);
