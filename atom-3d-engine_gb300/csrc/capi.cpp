@@ -1005,7 +1005,7 @@ int mm3e_scene_autotune(mm3e_scene* s, const mm3e_camera* camera, int spec_mode,
     mm3e_ctx* c = s->ctx;
     if (spec_mode < 0 || spec_mode > 2) return fail(c, MM3E_ERR_INVALID, "spec_mode must be 0, 1 or 2");
     static const mm3e_tuning builtin[] = {{128, 3, 64, 0}, {128, 2, 64, 0}, {128, 4, 64, 0}, {256, 4, 64, 0},
-                                          {256, 3, 64, 0}, {128, 5, 64, 0}, {128, 3, 32, 0}, {128, 4, 32, 0}};
+                                          {256, 3, 64, 0}, {256, 3, 64, 3}, {128, 3, 64, 7}, {128, 3, 32, 0}};
     if (!n_candidates) {
         candidates = builtin;
         n_candidates = (uint32_t)(sizeof(builtin) / sizeof(builtin[0]));

@@ -21,6 +21,7 @@ namespace wave {
 // scene-specialised program supplies a class with the same members that returns its scene's
 // settings as constants, so the pass bodies fold their branches on them.
 struct InterpField {
+    static constexpr bool kConstSettings = false;  // the settings below are read at run time
     static __device__ __forceinline__ Field eval(const Tape& T, V p) { return world_eval(T, p); }
     static __device__ __forceinline__ V normal_dual(const Tape& T, V p) {
         return mm3e::normal_dual(T.obj, T.h->n_objects, p);
@@ -214,6 +215,21 @@ __device__ __forceinline__ void lens_ray(const FrameJob& J, uint32_t x, uint32_t
     rd = normalize(focus - origin);
 }
 
+// Which boosts of Marcher::march_with a scene's settings allow (march.rs:132-141): over-
+// relaxation (omega 1.4, relaxed to 1 after a rollback) only with step_scale >= 1, the leap only
+// with a positive subitize as well, the secant step only with the secant flag as well. A field
+// class with constant settings (a scene-specialised program) turns a boost that cannot occur
+// into a compile-time false, and its lane state is never read or kept; the interpreter keeps all.
+template <class FP> struct MarchBoosts {
+    bool relax, leap, secant;
+    __device__ __forceinline__ explicit MarchBoosts(const TapeHeader& h) {
+        const bool lip = FP::step_scale(h) >= 1.0f;
+        relax = !FP::kConstSettings || lip;
+        leap = !FP::kConstSettings || (lip && FP::subitize(h) > 0.0f);
+        secant = !FP::kConstSettings || (lip && (FP::flags(h) & SF_SECANT) != 0u);
+    }
+};
+
 __device__ __forceinline__ V tetra_k(uint32_t t) {
     // k0 = (1,-1,-1), k1 = (-1,-1,1), k2 = (-1,1,-1), k3 = (1,1,1) (march.rs:212-223)
     return V{(t == 0u || t == 3u) ? 1.0f : -1.0f, (t >= 2u) ? 1.0f : -1.0f, (t == 1u || t == 3u) ? 1.0f : -1.0f};
@@ -320,12 +336,13 @@ __device__ __forceinline__ bool m_start(MLane& L, LaneTape<TM>& LT, const WaveAr
     L.prev_r = 0.0f;
     L.step = 0.0f;
     L.t_prev = 0.0f;
-    L.d_prev = __int_as_float(0x7f800000);
+    const MarchBoosts<FP> can(h);
     bool lip = FP::step_scale(h) >= 1.0f;
-    L.omega = lip ? 1.4f : FP::step_scale(h);
-    L.subz = lip ? FP::subitize(h) : 0.0f;
-    L.secant_on = ((FP::flags(h) & SF_SECANT) && lip) ? 1u : 0u;
-    L.boost = BOOST_OMEGA;
+    if (can.secant) L.d_prev = __int_as_float(0x7f800000);
+    if (can.relax) L.omega = lip ? 1.4f : FP::step_scale(h);
+    if (can.leap) L.subz = lip ? FP::subitize(h) : 0.0f;
+    if (can.secant) L.secant_on = ((FP::flags(h) & SF_SECANT) && lip) ? 1u : 0u;
+    if (can.leap || can.secant) L.boost = BOOST_OMEGA;
     L.i = 0;
     L.phase = M_MARCH;
     if (FP::max_steps(h) == 0) {
@@ -396,13 +413,14 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         return;
     }
     {
-        float step_len = d * L.omega;
+        const MarchBoosts<FP> can(h);
+        float step_len = d * (can.relax ? L.omega : FP::step_scale(h));
         uint32_t boost = BOOST_OMEGA;
-        if (L.subz > 0.0f && d > e * 6.0f) {
+        if (can.leap && L.subz > 0.0f && d > e * 6.0f) {
             step_len = step_len * (1.0f + L.subz);
             boost = BOOST_LEAP;
         }
-        if (L.secant_on && d < 0.08f && isfinite(L.d_prev)) {
+        if (can.secant && L.secant_on && d < 0.08f && isfinite(L.d_prev)) {
             float dt = L.t - L.t_prev;
             float dd = d - L.d_prev;
             if (dt > 1e-6f && dd < -1e-6f) {
@@ -411,9 +429,9 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
             }
         }
         L.step = step_len;
-        L.boost = boost;
+        if (can.leap || can.secant) L.boost = boost;
         L.prev_r = radius;
-        L.d_prev = d;
+        if (can.secant) L.d_prev = d;
         L.t_prev = L.t;
         L.t = L.t + step_len;
         if (L.t > FP::max_dist(h)) {
@@ -426,13 +444,21 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
     }
 rollback:  // retreat to the last safe frontier (march.rs:155-170)
     L.t = L.t_prev + L.prev_r;
-    if (L.boost == BOOST_OMEGA) L.omega = fminf(L.omega, 1.0f);
-    else if (L.boost == BOOST_LEAP) L.subz = 0.0f;
-    else L.secant_on = 0;
-    L.boost = BOOST_OMEGA;
+    {
+        const MarchBoosts<FP> can(h);
+        const uint32_t boost = (can.leap || can.secant) ? L.boost : (uint32_t)BOOST_OMEGA;
+        if (boost == BOOST_OMEGA) {
+            if (can.relax) L.omega = fminf(L.omega, 1.0f);  // (step_scale < 1 stays as it is)
+        } else if (boost == BOOST_LEAP) {
+            L.subz = 0.0f;
+        } else {
+            L.secant_on = 0;
+        }
+        if (can.leap || can.secant) L.boost = BOOST_OMEGA;
+        if (can.secant) L.d_prev = __int_as_float(0x7f800000);
+    }
     L.prev_r = 0.0f;
     L.step = 0.0f;
-    L.d_prev = __int_as_float(0x7f800000);
     L.i += 1;
     if (L.i >= max_steps) m_write(L, a, false, V{0.f, 0.f, 0.f}, max_steps);
 }

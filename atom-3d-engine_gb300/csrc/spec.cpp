@@ -573,6 +573,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
     // constants (the tape header's values, which the scene's tape keeps while it is specialised)
     auto u = [](uint32_t v) { return std::to_string(v) + "u"; };
     os << "struct Field_ {\n"
+          "    static constexpr bool kConstSettings = true;\n"
           "    static __device__ __forceinline__ Field eval(const Tape& T, V p) { return spec::eval(T, p); }\n"
           "    static __device__ __forceinline__ V normal_dual(const Tape&, V p) { return spec::normal_dual(p); }\n"
        << "    static __device__ __forceinline__ uint32_t flags(const TapeHeader&) { return " << u(h->flags) << "; }\n"
@@ -592,13 +593,14 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
        << "    static __device__ __forceinline__ float normal_h(const TapeHeader&) { return " << fbits(h->normal_h) << "; }\n"
        << "};\n}  // namespace spec\n}  // namespace mm3e\n";
     const int tm = smem_tape ? 0 : 1;
-    const std::string bounds = min_blocks ? std::to_string(block) + ", " + std::to_string(min_blocks) : std::to_string(block);
-    // With no explicit register budget the march kernel still asks for 7 CTAs of 128 (3 of 256)
-    // per SM, at most 72 / 85 registers: one eval call site keeps it free of spills, and the extra
-    // resident warps hide its branch and instruction-fetch latency (measured 5-6% faster on the
-    // gallery and hero scenes, neutral on the Cornell room). The shadow kernel loses at that budget.
-    const uint32_t march_mb = min_blocks ? min_blocks : (block <= 128 ? 7u : 3u);
-    const std::string march_bounds = std::to_string(block) + ", " + std::to_string(march_mb);
+    // With no explicit register budget both persistent kernels ask for 8 CTAs of 128 (4 of 256)
+    // per SM, at most 64 registers: with no function call left in the generated field (the BVH
+    // walks are inlined), the gallery's march and shadow fit that without spills (62 / 59), and the
+    // extra resident warps hide branch and instruction-fetch latency. (Left to itself, ptxas gave
+    // the shadow kernel 64 registers with spills.)
+    const uint32_t mb = min_blocks ? min_blocks : (block <= 128 ? 8u : 4u);
+    const std::string march_bounds = std::to_string(block) + ", " + std::to_string(mb);
+    const std::string bounds = march_bounds;
     os << "extern \"C\" __global__ void __launch_bounds__(" << march_bounds
        << ") mm3e_spec_march(const __grid_constant__ mm3e::WaveArgs a) {\n    mm3e::wave::march_body<" << tm << ", "
        << unroll << ", mm3e::spec::Field_>(a);\n}\n"

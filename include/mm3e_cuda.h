@@ -330,9 +330,9 @@ int mm3e_ctx_device_info(mm3e_ctx* ctx, int* sm_count, int* clock_khz);
  * work refills (unroll 1..64, default 64; the tape interpreter's kernels round it down to 1, 16
  * or 64);
  * min_blocks (0..16) asks the compiler of scene-specialised
- * kernels to fit that many CTAs per SM in the register file (0: the compiler's choice for the
- * shadow / AO kernels and 7 CTAs of 128 or 3 of 256 for the march kernel). Results do not depend
- * on it. mm3e_autotune picks block / tile / unroll. */
+ * kernels to fit that many CTAs per SM in the register file (0: 8 CTAs of 128 or 4 of 256 for the
+ * march and shadow kernels, the compiler's choice for the AO kernel). Results do not depend on it.
+ * mm3e_autotune picks block / tile / unroll. */
 typedef struct mm3e_tuning {
     uint32_t block, tile_wlog, unroll, min_blocks;
 } mm3e_tuning;
