@@ -11,7 +11,8 @@
                         suite checks the oracle still reproduces them bit-exactly and the GPU
                         suite compares the CUDA path against them.
 * reference_images.json agreement of the oracle with the images the reference repository
-                        ships (its own renders of its example scenes), when those are present.
+                        ships (its own renders of its example scenes), when its checkout is
+                        given in the environment variable MM3E_REFERENCE_DIR.
 """
 import hashlib
 import json
@@ -30,7 +31,8 @@ import oracle_py  # noqa: E402
 from mm3e_cuda import scenes  # noqa: E402
 from mm3e_cuda.scene import GiVolume  # noqa: E402
 
-REFERENCE = "/root/reference"
+# A checkout of the reference repository (its shipped PNG renders), if any.
+REFERENCE = os.environ.get("MM3E_REFERENCE_DIR", "")
 
 
 def desc_digest(scene):
@@ -79,7 +81,7 @@ def frames():
 
 def reference_images():
     res = {}
-    if not os.path.isdir(REFERENCE):
+    if not REFERENCE or not os.path.isdir(REFERENCE):
         return res
     from tests_png import read_png
     for fname, fn, bake in (("spheres.png", lambda: scenes.hero_scene(960, 540, 2, 2), None),

@@ -265,13 +265,17 @@ def test_oracle_reproduces_committed_frames():
         assert np.array_equal(got, frames[name]), name
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/gallery.png"), reason="reference images not present")
+REFERENCE_DIR = os.environ.get("MM3E_REFERENCE_DIR", "")
+
+
+@pytest.mark.skipif(not (REFERENCE_DIR and os.path.exists(os.path.join(REFERENCE_DIR, "gallery.png"))),
+                    reason="MM3E_REFERENCE_DIR (a checkout of the reference with its shipped renders) is not set")
 def test_oracle_matches_reference_gallery_render():
     """The reference ships gallery.png, its own render of examples/gallery.rs."""
     from golden.tests_png import read_png
     s, cam = scenes.reference_gallery_scene()
     ours = mm3e_cuda.to_rgba8(oracle_py.render(s.desc(), cam))[..., :3].astype(np.int32)
-    ref = read_png("/root/reference/gallery.png")[..., :3].astype(np.int32)
+    ref = read_png(os.path.join(REFERENCE_DIR, "gallery.png"))[..., :3].astype(np.int32)
     d = np.abs(ours - ref).max(-1)
     assert (d == 0).mean() >= 0.985
     assert (d <= 1).mean() >= 0.999
