@@ -7,6 +7,7 @@
 #include <cstring>
 
 #include "mesh.h"
+#include "spec.h"
 
 namespace mm3e {
 
@@ -74,6 +75,28 @@ struct ServerScene {
     size_t bytes = 0;
     uint64_t last_use = 0;
     uint32_t pending = 0;       // admitted requests that render it
+    bool resident = false;      // added with mm3e_server_add_scene (kept for camera updates)
+    // its specialised kernels: requested from the compile workers, and the cubin once built
+    // (kept on the host, so a scene dropped from the device and compiled again reloads it)
+    bool spec_requested = false;
+    std::shared_ptr<std::vector<char>> spec_cubin;
+    uint32_t spec_block = 0;
+    bool spec_smem = false;
+};
+
+// A resident scene's specialised program for the compile workers, and what they return.
+struct SpecJob {
+    uint32_t scene_id = 0;
+    std::string source;
+    uint32_t block = 0;
+    bool smem = false;
+};
+struct SpecDone {
+    uint32_t scene_id = 0;
+    std::shared_ptr<std::vector<char>> cubin;
+    std::string err;
+    uint32_t block = 0;
+    bool smem = false;
 };
 
 struct ServerRequest {
@@ -107,8 +130,8 @@ class Server {
     struct Slot {
         cudaStream_t stream = nullptr;
         std::unique_ptr<BatchEngine> engine;
-        PassBuffers plain_buf;           // plain mode: the per-frame launch's buffers
-        uint32_t* h_status = nullptr;    // pinned copy of the pass sequence's status word
+        PassBuffers plain_buf;           // per-frame launches: plain mode, and specialised frames
+        uint32_t* h_status = nullptr;    // pinned copies of the status words (pass sequence, per-frame)
         cudaEvent_t done = nullptr;
         std::vector<ServerRequest*> reqs;
         bool busy = false;
@@ -122,6 +145,10 @@ class Server {
     bool make_room(size_t bytes);
     void finish(ServerRequest* q, int status);
     size_t slot_bytes() const;
+    void request_spec(ServerScene& sc);
+    void load_spec(ServerScene& sc);
+    bool poll_spec();
+    void spec_worker();
 
     mm3e_ctx* ctx_;
     mm3e_server_config cfg_;
@@ -154,6 +181,13 @@ class Server {
     mm3e_server_stats st_{};    // guarded by mu_
     int init_rc_ = MM3E_OK;
     bool ready_ = false;
+    // background specialisation: jobs for the compile workers and their results
+    std::vector<std::thread> spec_threads_;
+    std::mutex smu_;
+    std::condition_variable scv_;
+    std::deque<SpecJob> spec_jobs_;   // guarded by smu_
+    std::deque<SpecDone> spec_done_;  // guarded by smu_
+    bool spec_stop_ = false;          // guarded by smu_
 };
 
 Server::Server(mm3e_ctx* ctx, const mm3e_server_config& cfg) : ctx_(ctx), cfg_(cfg), t0_(Clock::now()) {
@@ -162,10 +196,13 @@ Server::Server(mm3e_ctx* ctx, const mm3e_server_config& cfg) : ctx_(ctx), cfg_(c
     if (!cfg_.max_inflight) cfg_.max_inflight = 2;
     cfg_.max_inflight = std::min<uint32_t>(std::max<uint32_t>(cfg_.max_inflight, 1u), 4u);
     if (cfg_.plain) cfg_.max_inflight = 1;
+    if (cfg_.plain) cfg_.spec_workers = 0;
+    cfg_.spec_workers = std::min<uint32_t>(cfg_.spec_workers, 64u);
     st_.budget_bytes = cfg_.hbm_budget_bytes;
 }
 
 int Server::init() {
+    for (uint32_t i = 0; i < cfg_.spec_workers; ++i) spec_threads_.emplace_back([this] { spec_worker(); });
     worker_ = std::thread([this] { run(); });
     std::unique_lock<std::mutex> lk(mu_);
     cv_done_.wait(lk, [this] { return ready_; });
@@ -180,6 +217,99 @@ Server::~Server() {
     }
     cv_in_.notify_all();
     if (worker_.joinable()) worker_.join();
+    {
+        std::lock_guard<std::mutex> lk(smu_);
+        spec_stop_ = true;
+        spec_jobs_.clear();
+    }
+    scv_.notify_all();
+    for (std::thread& t : spec_threads_) t.join();
+}
+
+// ------------------------------------------------------------------------------------------
+// background specialisation of resident scenes
+// ------------------------------------------------------------------------------------------
+// A compile worker: NVRTC-compiles queued programs (host only; no device work) until stopped.
+void Server::spec_worker() {
+    for (;;) {
+        SpecJob job;
+        {
+            std::unique_lock<std::mutex> lk(smu_);
+            scv_.wait(lk, [this] { return spec_stop_ || !spec_jobs_.empty(); });
+            if (spec_stop_) return;
+            job = std::move(spec_jobs_.front());
+            spec_jobs_.pop_front();
+        }
+        SpecDone d;
+        d.scene_id = job.scene_id;
+        d.block = job.block;
+        d.smem = job.smem;
+        d.cubin = std::make_shared<std::vector<char>>();
+        std::string err = spec_compile(job.source, *d.cubin);
+        if (!err.empty() && err.compare(0, 4, "LOG:") != 0) d.err = err;
+        std::lock_guard<std::mutex> lk(smu_);
+        if (!spec_stop_) spec_done_.push_back(std::move(d));
+    }
+}
+
+// Queue a resident scene's specialised program (worker thread; the scene is on the device).
+void Server::request_spec(ServerScene& sc) {
+    if (!cfg_.spec_workers || !sc.resident || sc.spec_requested || !sc.dev) return;
+    sc.spec_requested = true;
+    if (spec_size(sc.dev->low.blob).objects > SPEC_AUTO_MAX_OBJECTS) return;  // the interpreter is faster
+    SpecJob job;
+    job.scene_id = sc.id;
+    const TuneParams& t = ctx_->tune;
+    job.block = t.block;
+    job.smem = sc.dev->low.blob.size() <= 96 * 1024;
+    job.source = spec_source(sc.dev->low.blob, t.block, t.unroll, job.smem, t.min_blocks);
+    {
+        std::lock_guard<std::mutex> lk(smu_);
+        spec_jobs_.push_back(std::move(job));
+    }
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        st_.spec_pending += 1;
+    }
+    scv_.notify_one();
+}
+
+// Attach a scene's built kernels to its device copy (worker thread, between launches: frames
+// already queued keep the kernels they were launched with).
+void Server::load_spec(ServerScene& sc) {
+    if (!sc.dev || sc.dev->spec || !sc.spec_cubin) return;
+    std::unique_ptr<SpecModule> m(new SpecModule());
+    m->kernels.block = sc.spec_block;
+    m->kernels.smem_tape = sc.spec_smem;
+    if (!m->load(*sc.spec_cubin, ctx_->device).empty()) return;  // keep rendering with the interpreter
+    sc.dev->spec = std::move(m);
+}
+
+// Take finished compiles and load them; true if any finished.
+bool Server::poll_spec() {
+    std::deque<SpecDone> done;
+    {
+        std::lock_guard<std::mutex> lk(smu_);
+        done.swap(spec_done_);
+    }
+    for (SpecDone& d : done) {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            if (st_.spec_pending) st_.spec_pending -= 1;
+        }
+        auto it = scenes_.find(d.scene_id);
+        if (it == scenes_.end() || !d.err.empty() || d.cubin->empty()) continue;
+        ServerScene& sc = *it->second;
+        sc.spec_cubin = d.cubin;
+        sc.spec_block = d.block;
+        sc.spec_smem = d.smem;
+        load_spec(sc);
+        if (sc.dev && sc.dev->spec) {
+            std::lock_guard<std::mutex> lk(mu_);
+            st_.scenes_specialized += 1;
+        }
+    }
+    return !done.empty();
 }
 
 size_t Server::slot_bytes() const {
@@ -313,6 +443,7 @@ int Server::ensure_resident(ServerScene& sc, bool& wait_for_memory) {
     }
     int rc = mm3e_scene_compile(ctx_, &sc.src.d, &sc.dev);
     if (rc) return rc;
+    load_spec(sc);  // a resident scene compiled again after it was dropped keeps its kernels
     sc.bytes = sc.dev->device_bytes();
     sc.last_use = ++use_clock_;
     std::lock_guard<std::mutex> lk(mu_);
@@ -420,7 +551,8 @@ bool Server::poll_slots() {
         cudaError_t e = cudaEventQuery(s.done);
         if (e == cudaErrorNotReady) continue;
         any = true;
-        int status = e == cudaSuccess ? status_error(ctx_, *s.h_status) : cuda_fail(ctx_, e, "served pass sequence");
+        int status = e == cudaSuccess ? status_error(ctx_, s.h_status[0] | s.h_status[1])
+                                      : cuda_fail(ctx_, e, "served pass sequence");
         for (ServerRequest* q : s.reqs) {
             if (status == MM3E_OK) std::memcpy(q->r.host_out, q->h_pin, q->frame_bytes);
             finish(q, status);
@@ -500,9 +632,42 @@ bool Server::launch_free_slots() {
             st_.sequences += 1;
             st_.frames_in_sequences += 1;
         } else {
-            std::vector<mm3e_job> jobs(batch.size());
-            for (size_t i = 0; i < batch.size(); ++i) {
-                ServerRequest* q = batch[i];
+            // Requests whose scene has its specialised kernels loaded render first, each through
+            // the per-frame launch sequence with those kernels (on the slot's stream and per-frame
+            // buffers, sized once for the largest); the rest share one coalesced pass sequence.
+            std::vector<ServerRequest*> spec_reqs, table_reqs;
+            for (ServerRequest* q : batch) (scenes_[q->scene_id]->dev->spec ? spec_reqs : table_reqs).push_back(q);
+            s.h_status[0] = 0;
+            s.h_status[1] = 0;
+            if (!spec_reqs.empty()) {
+                std::vector<PassPlan> plans;
+                uint64_t ns = 0, np = 0;
+                uint32_t lights = 0, levels = 1;
+                for (ServerRequest* q : spec_reqs) {
+                    mm3e_scene* sc = scenes_[q->scene_id]->dev;
+                    PassPlan p = plain_plan(sc, q->r.camera, q->w, q->h, q->r.format, q->d_out, ctx_->tune.tile_wlog);
+                    p.spec = sc->spec_kernels();
+                    p.clear_status = plans.empty();  // one status word for the slot's specialised frames
+                    ns = std::max<uint64_t>(ns, p.n_samples);
+                    np = std::max<uint64_t>(np, p.n_pixels);
+                    lights = std::max(lights, p.lights_max);
+                    levels = std::max(levels, p.levels);
+                    plans.push_back(p);
+                }
+                cudaError_t e = s.plain_buf.ensure(ns, lights, levels, np);
+                for (size_t i = 0; e == cudaSuccess && i < plans.size(); ++i)
+                    e = run_beauty(plans[i], s.plain_buf, ctx_->tune, s.stream, ctx_->sm_count, nullptr);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(s.h_status + 1, s.plain_buf.counters + (N_COUNTERS - 1), sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost, s.stream);
+                if (e != cudaSuccess) rc = cuda_fail(ctx_, e, "specialised frames");
+                std::lock_guard<std::mutex> lk(mu_);
+                st_.sequences += spec_reqs.size();
+                st_.spec_frames += spec_reqs.size();
+            }
+            std::vector<mm3e_job> jobs(table_reqs.size());
+            for (size_t i = 0; i < table_reqs.size(); ++i) {
+                ServerRequest* q = table_reqs[i];
                 mm3e_job& j = jobs[i];
                 j = mm3e_job{};
                 j.scene = scenes_[q->scene_id]->dev;
@@ -514,8 +679,8 @@ bool Server::launch_free_slots() {
                 j.out_bytes = q->frame_bytes;
             }
             mm3e_batch_stats bst{};
-            rc = s.engine->enqueue(jobs.data(), jobs.size(), &bst);
-            if (rc == MM3E_OK) {
+            if (rc == MM3E_OK && !jobs.empty()) rc = s.engine->enqueue(jobs.data(), jobs.size(), &bst);
+            if (rc == MM3E_OK && !jobs.empty()) {
                 cudaError_t e = cudaMemcpyAsync(s.h_status, s.engine->status_word(), sizeof(uint32_t),
                                                 cudaMemcpyDeviceToHost, s.stream);
                 if (e != cudaSuccess) rc = cuda_fail(ctx_, e, "served status");
@@ -554,12 +719,13 @@ void Server::run() {
     for (Slot& s : slots_) {
         cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&s.h_status), sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&s.h_status), 2 * sizeof(uint32_t));
         if (e != cudaSuccess) {
             rc = cuda_fail(ctx_, e, "server slot");
             break;
         }
-        *s.h_status = 0;
+        s.h_status[0] = 0;
+        s.h_status[1] = 0;
         s.engine.reset(new BatchEngine(ctx_, s.stream));
         mm3e_batch_config bc{cfg_.max_samples, cfg_.use_graphs};
         s.engine->configure(bc);
@@ -605,9 +771,11 @@ void Server::run() {
                 std::unique_ptr<ServerScene> sc(new ServerScene());
                 sc->id = next_scene_++;
                 sc->src.assign(*a->d);
+                sc->resident = true;
                 bool wait_mem = false;
                 arc = ensure_resident(*sc, wait_mem);
                 if (!arc) {
+                    request_spec(*sc);
                     id = sc->id;
                     scenes_[sc->id] = std::move(sc);
                 }
@@ -618,7 +786,8 @@ void Server::run() {
             a->done = true;
             cv_done_.notify_all();
         }
-        bool progressed = poll_slots();
+        bool progressed = poll_spec();
+        progressed = poll_slots() || progressed;
         progressed = launch_free_slots() || progressed;
         if (!progressed) {
             bool busy = false;

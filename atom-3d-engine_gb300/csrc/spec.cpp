@@ -10,7 +10,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <sstream>
 
@@ -351,6 +353,8 @@ void cluster_members(const DevObject* obj, std::vector<uint32_t> m, std::vector<
 
 std::string nvrtc_status() { return nvrtc().status; }
 
+std::string spec_compile_uncached(const std::string& source, std::vector<char>& cubin);
+
 SpecSize spec_size(const std::vector<unsigned char>& blob) {
     const TapeHeader* h = reinterpret_cast<const TapeHeader*>(blob.data());
     const DevObject* obj = reinterpret_cast<const DevObject*>(blob.data() + h->off_objects);
@@ -616,7 +620,49 @@ SpecModule::~SpecModule() {
     if (lib_) cudaLibraryUnload(lib_);
 }
 
+// Cubins of programs compiled in this process, by their source text: the same program always
+// gives the same cubin, so a scene specialised again (another context or server, a re-lowered
+// copy, an autotune candidate seen before) skips NVRTC. Bounded to the most recent 256.
+struct CubinCache {
+    std::mutex mu;
+    std::map<std::string, std::vector<char>> by_source;
+    std::deque<std::string> order;
+};
+CubinCache& cubin_cache() {
+    static CubinCache c;
+    return c;
+}
+
 std::string spec_compile(const std::string& source, std::vector<char>& cubin) {
+    Nvrtc& n = nvrtc();
+    if (!n.status.empty()) return n.status;
+    const char* verbose0 = std::getenv("MM3E_SPEC_VERBOSE");
+    const bool cacheable = !(verbose0 && verbose0[0] == '1');
+    if (cacheable) {
+        CubinCache& cc = cubin_cache();
+        std::lock_guard<std::mutex> lk(cc.mu);
+        auto it = cc.by_source.find(source);
+        if (it != cc.by_source.end()) {
+            cubin = it->second;
+            return "";
+        }
+    }
+    std::string err = spec_compile_uncached(source, cubin);
+    if (cacheable && err.empty() && !cubin.empty()) {
+        CubinCache& cc = cubin_cache();
+        std::lock_guard<std::mutex> lk(cc.mu);
+        if (cc.by_source.emplace(source, cubin).second) {
+            cc.order.push_back(source);
+            if (cc.order.size() > 256) {
+                cc.by_source.erase(cc.order.front());
+                cc.order.pop_front();
+            }
+        }
+    }
+    return err;
+}
+
+std::string spec_compile_uncached(const std::string& source, std::vector<char>& cubin) {
     Nvrtc& n = nvrtc();
     if (!n.status.empty()) return n.status;
     const char* names[] = {"tape.h", "device_math.cuh", "kernels.h", "march_kernels.cuh"};
@@ -667,6 +713,14 @@ std::string SpecModule::build(const std::string& source, int device, double* com
     std::vector<char> cubin;
     std::string err = spec_compile(source, cubin);
     if (!err.empty() && err.compare(0, 4, "LOG:") != 0) return err;
+    err = load(cubin, device);
+    if (!err.empty()) return err;
+    if (compile_ms) *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return "";
+}
+
+std::string SpecModule::load(const std::vector<char>& cubin, int device) {
+    if (lib_) return "specialised kernels already loaded";
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaLibraryLoadData(&lib_, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
     cudaKernel_t km = nullptr, ks = nullptr, ka = nullptr;
@@ -677,7 +731,6 @@ std::string SpecModule::build(const std::string& source, int device, double* com
     kernels.march = reinterpret_cast<const void*>(km);
     kernels.shadow = reinterpret_cast<const void*>(ks);
     kernels.ao = reinterpret_cast<const void*>(ka);
-    if (compile_ms) *compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return "";
 }
 

@@ -45,6 +45,8 @@ class SpecModule {
     ~SpecModule();
     // Compiles `source` (NVRTC, sm_103a cubin) and loads its kernels. Returns "" or an error.
     std::string build(const std::string& source, int device, double* compile_ms);
+    // Loads the kernels of a cubin spec_compile made (e.g. on another host thread).
+    std::string load(const std::vector<char>& cubin, int device);
     SpecKernels kernels;
 
   private:

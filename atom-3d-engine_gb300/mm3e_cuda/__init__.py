@@ -451,11 +451,13 @@ class Server:
 
     While a server runs on a Context, use the context only through the server."""
 
-    def __init__(self, ctx, hbm_budget_bytes=0, max_samples=0, max_inflight=0, use_graphs=True, plain=False):
+    def __init__(self, ctx, hbm_budget_bytes=0, max_samples=0, max_inflight=0, use_graphs=True, plain=False,
+                 spec_workers=0):
         self.ctx = ctx
         self._ptr = C.c_void_p()
         self._keep = {}  # request inputs that must outlive submission (ticket -> objects)
-        cfg = abi.ServerConfig(hbm_budget_bytes, max_samples, max_inflight, 1 if use_graphs else 0, 1 if plain else 0)
+        cfg = abi.ServerConfig(hbm_budget_bytes, max_samples, max_inflight, 1 if use_graphs else 0, 1 if plain else 0,
+                               int(spec_workers))
         ctx.check(lib().mm3e_server_create(ctx.handle, C.byref(cfg), C.byref(self._ptr)))
 
     def add_scene(self, scene):

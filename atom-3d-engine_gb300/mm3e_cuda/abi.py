@@ -127,7 +127,7 @@ class Mesh(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_samples", C.c_uint64), ("max_inflight", C.c_uint32),
-                ("use_graphs", C.c_uint32), ("plain", C.c_uint32)]
+                ("use_graphs", C.c_uint32), ("plain", C.c_uint32), ("spec_workers", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -146,7 +146,7 @@ class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "sequences", "frames_in_sequences",
                                           "scenes_compiled", "scenes_evicted", "mesh_bakes", "mesh_bake_hits",
                                           "admitted_bytes", "peak_admitted_bytes", "budget_bytes",
-                                          "reserved_bytes")]
+                                          "reserved_bytes", "scenes_specialized", "spec_pending", "spec_frames")]
 
 
 class TuneEntry(C.Structure):

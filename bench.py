@@ -287,9 +287,28 @@ def bench_batched(ctx, stream, torch, n_scenes):
             plain_ms.append(ev[0].elapsed_time(ev[1]))
     b = statistics.median(batch_ms)
     p = statistics.median(plain_ms)
+    # per resolution class: that class's frames as one batch against the plain call of each
+    by_res = {}
+    for res in sorted({(s.width, s.height) for s, _ in items}, key=lambda r: r[0] * r[1]):
+        idx = [i for i, (s, _) in enumerate(items) if (s.width, s.height) == res]
+        cjobs = ctx.make_jobs([(compiled[i], items[i][1], 0, 0, abi.FB_RGBA8, outs[i].data_ptr(), None) for i in idx])
+        ctx.render_batch(cjobs)
+        cb = statistics.median(ctx.render_batch(cjobs)["device_ms"] for _ in range(2))
+        cp = []
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                ev[0].record(stream)
+                for i in idx:
+                    compiled[i].render_device(items[i][1], abi.FB_RGBA8, outs[i].data_ptr(), outs[i].numel())
+                ev[1].record(stream)
+                stream.synchronize()
+                cp.append(ev[0].elapsed_time(ev[1]))
+        cpm = statistics.median(cp)
+        by_res[f"{res[0]}x{res[1]}"] = {"frames": len(idx), "batch_ms": cb, "plain_ms": cpm,
+                                        "batched_over_plain": cpm / cb}
     for c in compiled:
         c.close()
-    return {"workload": f"procedural_batch_{n_scenes}", "frames": n_scenes, "pixels": pixels,
+    return {"workload": f"procedural_batch_{n_scenes}", "frames": n_scenes, "pixels": pixels, "by_resolution": by_res,
             "batched_frames_per_s": n_scenes * 1000.0 / b, "batched_mrays_per_s_primary": pixels / b / 1e3,
             "plain_frames_per_s": n_scenes * 1000.0 / p, "batched_over_plain": p / b,
             "batch_ms": b, "plain_ms": p, "sequences": stats["sequences"],
@@ -297,11 +316,13 @@ def bench_batched(ctx, stream, torch, n_scenes):
             "tuning": best, "autotune_s": tune_s, "autotune_table": table}
 
 
-def bench_served(ctx_factory, seconds, max_requests, rates=(200, 1000, 5000), seed=7):
+def bench_served(ctx_factory, seconds, max_requests, rates=(200, 1000, 5000), seed=7, spec_workers=12):
     """Served form: Poisson arrivals at each rate; 70% camera updates of resident procedural
     scenes, 20% new procedural scenes, 10% scenes around a 128^3 grid baked on the GPU from a
     seeded displaced icosphere (subdivision 5); HBM budget 40 GB. The same trace replayed through
-    the continuous-batching server and through the plain per-request launch (one at a time)."""
+    the served form (continuous batching; the resident scenes' specialised kernels compiled on
+    `spec_workers` host threads before the stream starts) and through the plain per-request
+    launch (one at a time, the tape interpreter)."""
     import numpy as np
 
     import mm3e_cuda
@@ -346,9 +367,18 @@ def bench_served(ctx_factory, seconds, max_requests, rates=(200, 1000, 5000), se
         row = {"requests": n, "arrival_window_s": float(arrivals[-1]) if n else 0.0}
         for mode in ("batched", "plain"):
             ctx = ctx_factory()
-            srv = mm3e_cuda.Server(ctx, hbm_budget_bytes=40 << 30, plain=(mode == "plain"))
+            workers = 0 if mode == "plain" else spec_workers
+            srv = mm3e_cuda.Server(ctx, hbm_budget_bytes=40 << 30, plain=(mode == "plain"), spec_workers=workers)
+            spec_warmup_s = None
             try:
                 ids = [srv.add_scene(s) for s, _ in resident]
+                if workers:
+                    # the resident scenes' kernels compile on host threads while the server starts:
+                    # the stream begins once they are loaded (a warm server)
+                    t0 = time.perf_counter()
+                    while srv.stats()["spec_pending"] > 0 and time.perf_counter() - t0 < 600:
+                        time.sleep(0.05)
+                    spec_warmup_s = time.perf_counter() - t0
                 reqs, keep = [], []
                 for kind, j, cam, w, h in plan:
                     out = out_for(w, h)
@@ -376,7 +406,9 @@ def bench_served(ctx_factory, seconds, max_requests, rates=(200, 1000, 5000), se
                          "sequences": st["sequences"], "frames_per_sequence":
                              st["frames_in_sequences"] / max(1, st["sequences"]),
                          "mesh_bakes": st["mesh_bakes"], "scenes_compiled": st["scenes_compiled"],
-                         "peak_admitted_bytes": st["peak_admitted_bytes"], "reserved_bytes": st["reserved_bytes"]}
+                         "peak_admitted_bytes": st["peak_admitted_bytes"], "reserved_bytes": st["reserved_bytes"],
+                         "spec_workers": workers, "scenes_specialized": st["scenes_specialized"],
+                         "spec_frames": st["spec_frames"], "spec_warmup_s": spec_warmup_s}
         if row["batched"]["frames_per_s"] and row["plain"]["frames_per_s"]:
             row["batched_over_plain_frames_per_s"] = row["batched"]["frames_per_s"] / row["plain"]["frames_per_s"]
         results[str(rate)] = row

@@ -549,6 +549,11 @@ typedef struct mm3e_server_config {
     uint32_t use_graphs;       /* replay pass sequences from captured CUDA graphs */
     uint32_t plain;            /* 1: no coalescing; one request at a time through the per-frame
                                   launch sequence (the plain baseline) */
+    uint32_t spec_workers;     /* host threads that compile scene-specialised kernels (NVRTC) for
+                                  the resident scenes (mm3e_server_add_scene) in the background,
+                                  at most 64 objects each; a scene's frames render with them once
+                                  they are loaded, with the tape interpreter before (the same
+                                  frames either way). 0: none. Not in plain mode. */
 } mm3e_server_config;
 
 typedef struct mm3e_request {
@@ -580,6 +585,9 @@ typedef struct mm3e_server_stats {
     uint64_t scenes_compiled, scenes_evicted, mesh_bakes, mesh_bake_hits;
     uint64_t admitted_bytes, peak_admitted_bytes, budget_bytes;
     uint64_t reserved_bytes; /* pass-sequence slot buffers, allocated when the server starts */
+    uint64_t scenes_specialized; /* resident scenes whose specialised kernels are loaded */
+    uint64_t spec_pending;       /* resident scenes whose specialised kernels are still compiling */
+    uint64_t spec_frames;        /* frames rendered with specialised kernels */
 } mm3e_server_stats;
 
 int mm3e_server_create(mm3e_ctx* ctx, const mm3e_server_config* cfg, mm3e_server** out);

@@ -64,13 +64,30 @@ def _requests(srv, resident_ids, resident, items):
     return reqs, keeps, outs
 
 
-@pytest.mark.parametrize("plain", [False, True])
-def test_alone_equals_in_mix(plain):
+def _wait_specialized(srv, n, timeout_s=300.0):
+    """Poll the server until its background compiles are done; returns its stats."""
+    import time
+    t0 = time.time()
+    while True:
+        st = srv.stats()
+        if st["spec_pending"] == 0 and st["scenes_specialized"] >= n:
+            return st
+        assert time.time() - t0 < timeout_s, st
+        time.sleep(0.05)
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain", "specialized"])
+def test_alone_equals_in_mix(mode):
+    """In the "specialized" mode the resident scenes' kernels are compiled in the background
+    (spec_workers) and their requests render with them beside the coalesced pass sequences."""
+    plain = mode == "plain"
     ctx = mm3e_cuda.Context(0)
-    srv = mm3e_cuda.Server(ctx, max_inflight=2, plain=plain)
+    srv = mm3e_cuda.Server(ctx, max_inflight=2, plain=plain, spec_workers=4 if mode == "specialized" else 0)
     try:
         resident, items = _stream(7, 24)
         ids = [srv.add_scene(s) for s, _ in resident]
+        if mode == "specialized":
+            _wait_specialized(srv, len(resident))
         # alone: one request at a time
         reqs, keeps, alone = _requests(srv, ids, resident, items)
         for r in reqs:
@@ -86,8 +103,13 @@ def test_alone_equals_in_mix(plain):
             assert np.array_equal(a, b), f"request {i} ({items[i][0]}) differs alone vs in the mix"
         st = srv.stats()
         assert st["completed"] == 2 * len(items) and st["failed"] == 0
-        if not plain:
+        if mode == "batched":
             assert st["frames_in_sequences"] > st["sequences"], st  # requests were coalesced
+        if mode == "specialized":
+            n_resident = sum(1 for it in items if it[0] == "resident")
+            assert st["scenes_specialized"] == len(resident) and st["spec_frames"] == 2 * n_resident, st
+        else:
+            assert st["spec_frames"] == 0, st
         assert st["mesh_bakes"] >= 1 and st["mesh_bake_hits"] >= 1
     finally:
         srv.close()
