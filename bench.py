@@ -80,6 +80,10 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=256, help="scenes of the batched-form measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0,
                     help="arrival window per rate of the served-form measurement (the full spec is 60)")
+    ap.add_argument("--served-rates", default="200,1000,5000",
+                    help="Poisson arrival rates (requests/s) of the served-form measurement")
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the served-form measurement and print it as its own JSON line")
     ap.add_argument("--served-max-requests", type=int, default=2000,
                     help="cap on requests per rate (the arrival window shrinks to fit)")
     ap.add_argument("--no-forms", action="store_true", help="skip the Cornell / batched / served measurements")
@@ -796,14 +800,26 @@ def run_ours(args):
         line["preview"] = bench_preview(ctx, torch, not args.no_cpu)
         line["published_scene"] = bench_published(ctx, stream, torch)
         ctx.set_stream(None)
-        line["served"] = bench_served(lambda: mm3e_cuda.Context(local), args.served_seconds, args.served_max_requests)
+        line["served"] = bench_served(lambda: mm3e_cuda.Context(local), args.served_seconds, args.served_max_requests,
+                                      rates=tuple(int(r) for r in args.served_rates.split(",")))
     print(json.dumps(line))
     ctx.close()
 
 
+def run_served_only(args):
+    """Only the served-form measurement (e.g. the full 60 s windows), printed as its own line."""
+    import mm3e_cuda
+
+    out = bench_served(lambda: mm3e_cuda.Context(0), args.served_seconds, args.served_max_requests,
+                       rates=tuple(int(r) for r in args.served_rates.split(",")))
+    print(json.dumps({"served": out}))
+
+
 def main():
     args = parse()
-    if args.profile_frames:
+    if args.served_only:
+        run_served_only(args)
+    elif args.profile_frames:
         run_profile_frames(args)
     elif args.impl == "reference":
         run_reference(args)
