@@ -42,9 +42,9 @@ COUNTS_FIXTURE = os.path.join(ROOT, "tests", "golden", "workload_counts.json")
 
 # DRAM bytes (read + write) of one primary-level march launch (the scene-specialised kernel in the
 # timed launch shape), from an ncu capture of the same kernel on the workload at 960x540
-# (635,904 + 2,197,248 bytes), scaled by the pixel ratio to the bench resolution: the tape lives
-# in shared memory and the queues in L2, so DRAM traffic is small.
-MARCH_DRAM_BYTES_960x540 = {"gallery_1080p": 2833152}
+# (71,168 + 0 bytes), scaled by the pixel ratio to the bench resolution: the tape lives in shared
+# memory and the queues in L2, so DRAM traffic is small.
+MARCH_DRAM_BYTES_960x540 = {"gallery_1080p": 71168}
 
 
 def workloads(size=None):
