@@ -329,6 +329,15 @@ MD V local_point(const DevObject& o, V p) {
     return l;
 }
 
+// The tail of Object::field (lib.rs:380-397): the shape's distance d at the local point, scaled,
+// rounded and onioned.
+MD Field object_finish(const DevObject& o, float d) {
+    d = d * o.scale;
+    if (o.flags & OF_ROUND) d = d - o.round;
+    if (o.flags & OF_ONION) d = fabsf(d) - o.onion;
+    return Field{d, o.mat};
+}
+
 // Object::field (lib.rs:380-397)
 MD Field object_field(const Tape& T, const DevObject& o, V p) {
     V l = local_point(o, p);
@@ -337,10 +346,7 @@ MD Field object_field(const Tape& T, const DevObject& o, V p) {
     else if (o.prim == 11u) d = csg_eval(T.csg + o.aux, l);
     else if (o.prim == 12u) d = volume_sample(T.vol[o.aux], l);
     else d = __int_as_float(0x7f800000);
-    d = d * o.scale;
-    if (o.flags & OF_ROUND) d = d - o.round;
-    if (o.flags & OF_ONION) d = fabsf(d) - o.onion;
-    return Field{d, o.mat};
+    return object_finish(o, d);
 }
 
 // Register-resident traversal stack: twelve 16-bit node indices in three 64-bit words.

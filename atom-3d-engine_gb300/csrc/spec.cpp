@@ -106,11 +106,75 @@ std::string object_rec(const DevObject& o) {
     return os.str();
 }
 
-std::string object_fn(uint32_t i, const DevObject& o) {
+// A CSG program (csg.rs:95-118, the post-order stack program csg_eval runs over `op`, at most
+// `n` ops) as straight-line code over the local point `l`: the stack depths after every op are
+// known when the program is generated, so each stack slot becomes a named local and each
+// primitive and transform gets its constants inline. Every arithmetic step is the interpreter's,
+// in its order. Empty when the program is not one the interpreter runs to a well-defined end
+// (a stack underflow or overflow); the object then keeps the interpreter.
+std::string csg_body(const DevCsgOp* op, size_t n) {
     std::ostringstream os;
+    std::vector<std::string> vals, pts;
+    std::string cur = "l";
+    int nv = 0, np = 0;
+    for (size_t g = 0; g < 4096 && g < n; ++g, ++op) {
+        const uint32_t o = op->op;
+        if (o == CSG_OP_PRIM) {
+            if (vals.size() >= (size_t)MAX_CSG_STACK) return "";
+            const std::string q = "q" + std::to_string(nv), v = "v" + std::to_string(nv);
+            os << "    const float " << q << "[7] = " << farr(op->p, 7) << ";\n    float " << v
+               << " = prim_distance(" << op->kind << "u, " << q << ", " << cur << ");\n";
+            nv += 1;
+            vals.push_back(v);
+        } else if (o == CSG_OP_XFORM) {
+            if (pts.size() >= (size_t)MAX_CSG_STACK) return "";
+            const std::string r = "r" + std::to_string(np), x = "x" + std::to_string(np);
+            os << "    const float " << r << "[9] = " << farr(op->rot, 9) << ";\n    const V " << x << " = scale(rot_t("
+               << r << ", " << cur << " - V{" << fbits(op->pos[0]) << ", " << fbits(op->pos[1]) << ", "
+               << fbits(op->pos[2]) << "}), " << fbits(op->inv) << ");\n";
+            np += 1;
+            pts.push_back(cur);
+            cur = x;
+        } else if (o == CSG_OP_UNXFORM) {
+            if (pts.empty() || vals.empty()) return "";
+            cur = pts.back();
+            pts.pop_back();
+            os << "    " << vals.back() << " = " << vals.back() << " * " << fbits(op->scale) << ";\n";
+        } else if (o == CSG_OP_UNION || o == CSG_OP_INTERSECT || o == CSG_OP_SUBTRACT || o == CSG_OP_SMOOTH) {
+            if (vals.size() < 2) return "";
+            const std::string b = vals.back();
+            vals.pop_back();
+            const std::string a = vals.back();
+            if (o == CSG_OP_UNION) os << "    " << a << " = fminf(" << a << ", " << b << ");\n";
+            if (o == CSG_OP_INTERSECT) os << "    " << a << " = fmaxf(" << a << ", " << b << ");\n";
+            if (o == CSG_OP_SUBTRACT) os << "    " << a << " = fmaxf(" << a << ", -" << b << ");\n";
+            if (o == CSG_OP_SMOOTH)
+                os << "    " << a << " = f_smooth_union(Field{" << a << ", 0u}, Field{" << b << ", 0u}, "
+                   << fbits(op->p[0]) << ").d;\n";
+        } else if (o == CSG_OP_OFFSET || o == CSG_OP_SHELL) {
+            if (vals.empty()) return "";
+            const std::string a = vals.back();
+            if (o == CSG_OP_OFFSET) os << "    " << a << " = " << a << " - " << fbits(op->p[0]) << ";\n";
+            else os << "    " << a << " = fabsf(" << a << ") - " << fbits(op->p[0]) << ";\n";
+        } else {
+            break;
+        }
+    }
+    os << "    return " << (vals.empty() ? std::string("__int_as_float(0x7f800000)") : vals.front()) << ";\n";
+    return os.str();
+}
+
+// An object's field with its record inlined; a CSG object's program is generated code too
+// (csg_ops: the tape's CSG ops, n_csg of them).
+std::string object_fn(uint32_t i, const DevObject& o, const DevCsgOp* csg_ops, uint32_t n_csg) {
+    std::ostringstream os;
+    const std::string body = o.prim == 11u && o.aux < n_csg ? csg_body(csg_ops + o.aux, n_csg - o.aux) : "";
+    if (!body.empty())
+        os << "__device__ __forceinline__ float csg_" << i << "(V l) {\n" << body << "}\n";
     os << "__device__ __forceinline__ Field obj_" << i << "(const Tape& T, V p) {\n"
-       << "    const DevObject o = " << object_rec(o) << ";\n"
-       << "    return object_field(T, o, p);\n}\n";
+       << "    const DevObject o = " << object_rec(o) << ";\n";
+    if (!body.empty()) os << "    return object_finish(o, csg_" << i << "(local_point(o, p)));\n}\n";
+    else os << "    return object_field(T, o, p);\n}\n";
     return os.str();
 }
 
@@ -415,8 +479,9 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 if (i < h->n_objects) used[i] = true;
         }
     }
+    const DevCsgOp* csg = reinterpret_cast<const DevCsgOp*>(blob.data() + h->off_csg);
     for (uint32_t i = 0; i < h->n_objects; ++i)
-        if (used[i]) os << object_fn(i, obj[i]);
+        if (used[i]) os << object_fn(i, obj[i], csg, h->n_csg_ops);
     for (uint32_t s = 0; s < h->n_segments; ++s)
         if (walk[s]) os << walk_fn(s, seg[s], node, h->n_nodes, unb, h->slack, s > 0);
     const std::string slack = fbits(h->slack);

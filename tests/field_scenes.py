@@ -52,3 +52,62 @@ def smooth_chain_scene(seed, width=64, height=36):
         s.objects.append(o)
     cam = look_at((0.5, 3.0, -8.5), (0.0, 0.8, 0.0), (0.0, 1.0, 0.0), radians(55.0))
     return s, cam
+
+
+def csg_zoo_scene(seed, width=64, height=36):
+    """Objects whose shapes are CSG programs over every operation (union, intersection,
+    subtraction, smooth union, offset, shell, nested transforms with rotations and scales), some of
+    the objects also rounded, onioned, mirrored or smooth-unioned, on a plane; with a camera
+    looking at them."""
+    from mm3e_cuda import abi
+    from mm3e_cuda.scene import Expr
+    from mm3e_cuda.scenes import _random_prim
+
+    rng = np.random.default_rng(seed)
+    s = Scene(width, height)
+    s.materials = [Material((0.8, 0.8, 0.8)), Material((0.7, 0.25, 0.2)), Material((0.2, 0.5, 0.7))]
+    s.objects = [Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, 0)]
+
+    def leaf():
+        p = _random_prim(rng)
+        while p.kind == abi.PRIM_PLANE:
+            p = _random_prim(rng)
+        e = Expr(p.kind, tuple(float(v) * 0.6 for v in p.params[:7]) if p.kind != abi.PRIM_CAPSULE else p.params[:7])
+        return e
+
+    def tree(depth):
+        if depth == 0:
+            return leaf()
+        op = int(rng.integers(0, 7))
+        if op == 0:
+            return Expr.union(tree(depth - 1), tree(depth - 1))
+        if op == 1:
+            return Expr.intersect(tree(depth - 1), leaf())
+        if op == 2:
+            return Expr.subtract(tree(depth - 1), tree(depth - 1))
+        if op == 3:
+            return Expr.smooth_union(tree(depth - 1), tree(depth - 1), float(rng.uniform(0.05, 0.4)))
+        if op == 4:
+            return Expr.offset(tree(depth - 1), float(rng.uniform(-0.05, 0.1)))
+        if op == 5:
+            return Expr.shell(tree(depth - 1), float(rng.uniform(0.02, 0.08)))
+        rot = mat3_from_euler(*rng.uniform(-1.5, 1.5, 3))
+        return Expr.transform(tree(depth - 1), Transform(tuple(rng.uniform(-0.4, 0.4, 3)), rot,
+                                                         float(rng.uniform(0.6, 1.4))))
+
+    for k in range(10):
+        pos = tuple(float(v) for v in rng.uniform([-4, 0.6, -3], [4, 2.2, 3]))
+        rot = mat3_from_euler(*rng.uniform(-1.2, 1.2, 3))
+        o = Object(Prim.csg(s.csg(tree(int(rng.integers(1, 4))))), Transform(pos, rot, float(rng.uniform(0.7, 1.3))),
+                   1 + k % 2)
+        if k % 5 == 1:
+            o = o.round(0.05)
+        elif k % 5 == 2:
+            o = o.onion(0.04)
+        elif k % 5 == 3:
+            o = o.mirror(True, False, bool(k % 2))
+        if k == 4:
+            o = o.smooth(0.3)
+        s.objects.append(o)
+    cam = look_at((0.0, 3.2, -9.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), radians(50.0))
+    return s, cam

@@ -15,7 +15,7 @@ import mm3e_cuda
 import oracle_py
 from mm3e_cuda import abi, scenes
 from mm3e_cuda.scene import DynSphere, GiVolume
-from field_scenes import noncons_scene, smooth_chain_scene
+from field_scenes import csg_zoo_scene, noncons_scene, smooth_chain_scene
 from parity import hit_metrics, image_metrics
 
 pytestmark = pytest.mark.gpu
@@ -258,6 +258,19 @@ def test_smooth_chain_scene_parity(gpu_ctx):
     _check_hits("smooth_chain", compiled, scene, cam)
     compiled.specialize(compiled.SPEC_ALWAYS)
     _check_image("smooth_chain_spec", compiled.render(cam, fmt=abi.FB_RGBA8), ref)
+
+
+@pytest.mark.parametrize("seed", [1, 3])
+def test_csg_zoo_scene_parity(gpu_ctx, seed):
+    """CSG programs over every operation (csg.rs:95-118): the interpreter's stack program and the
+    specialised field's generated straight-line programs both against the oracle."""
+    scene, cam = csg_zoo_scene(seed, 160, 90)
+    compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image("csg_zoo", gpu, ref)
+    _check_hits("csg_zoo", compiled, scene, cam)
+    compiled.specialize(compiled.SPEC_ALWAYS)
+    _check_image("csg_zoo_spec", compiled.render(cam, fmt=abi.FB_RGBA8), ref)
+    _check_hits("csg_zoo_spec", compiled, scene, cam)
 
 
 def _mirror_scene(bounces, shadows=True):

@@ -9,7 +9,7 @@ import pytest
 
 import mm3e_cuda
 from mm3e_cuda import abi, scenes
-from field_scenes import noncons_scene, smooth_chain_scene
+from field_scenes import csg_zoo_scene, noncons_scene, smooth_chain_scene
 from mm3e_cuda.scene import DynSphere
 
 pytestmark = pytest.mark.gpu
@@ -24,6 +24,9 @@ SCENES = {
     "procedural4": lambda: scenes.procedural_scene(4, 96, 64),
     "noncons": lambda: noncons_scene(21, 160, 90),
     "smooth_chain": lambda: smooth_chain_scene(5, 160, 90),
+    "csg_zoo1": lambda: csg_zoo_scene(1, 160, 90),
+    "csg_zoo3": lambda: csg_zoo_scene(3, 160, 90),
+    "procedural9": lambda: scenes.procedural_scene(9, 128, 72),
 }
 
 

@@ -61,3 +61,22 @@ def test_plain_sphere_members_only_where_the_bound_is_the_field():
     assert count(Object(Prim.sphere(0.7), Transform((0.5, 1.0, -0.25), mat3_from_euler(0.1, 0.2, 0.3)), 0)) == 1
     assert count(plain.round(0.05)) == 1
     assert count(Object(Prim.box((0.5, 0.5, 0.5)), Transform((0.5, 1.0, -0.25)), 0)) == 1
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_csg_programs_are_generated_code(seed):
+    """Every CSG object's program (csg.rs:95-118) becomes straight-line code in the specialised
+    field: no call of the stack interpreter remains, each object gets its own program, and the
+    program compiles."""
+    from field_scenes import csg_zoo_scene
+
+    s, _ = csg_zoo_scene(seed, 32, 18)
+    src = mm3e_cuda.spec_source(s)
+    n_csg = sum(1 for o in s.objects if o.prim.kind == 11)
+    assert n_csg == 10
+    assert "csg_eval" not in src
+    assert src.count("__device__ __forceinline__ float csg_") == n_csg
+    ok, msg, ms = mm3e_cuda.spec_compile_check(s)
+    if not ok and "libnvrtc not found" in msg:
+        pytest.skip("NVRTC is not installed")
+    assert ok, msg
