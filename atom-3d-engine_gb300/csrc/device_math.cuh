@@ -162,12 +162,22 @@ MD Field f_smooth_union(Field a, Field b, float k) {  // sdf.rs:152-160
 }
 MD float rep_axis(float v, float period) { return period > 0.0f ? v - period * roundf(v / period) : v; }
 
+// Squared norms for the cull pre-tests below, with fused multiply-adds: within a few units of
+// roundoff of length_sq (both are within three of the exact square of the same binary32
+// vector), which the tests' margins absorb. Never a value that the field returns.
+MD float length_sq_fma(V a) { return __fmaf_rn(a.x, a.x, __fmaf_rn(a.y, a.y, a.z * a.z)); }
+MD V rot_t_fma(const float* r, V v) {
+    return V{__fmaf_rn(r[0], v.x, __fmaf_rn(r[1], v.y, r[2] * v.z)), __fmaf_rn(r[3], v.x, __fmaf_rn(r[4], v.y, r[5] * v.z)),
+             __fmaf_rn(r[6], v.x, __fmaf_rn(r[7], v.y, r[8] * v.z))};
+}
+
 // Cull pre-test of a bounded union member (accel.rs:98-100: a sphere whose lower bound exceeds the
-// best distance so far cannot win). With d2 = length_sq(p - c) computed exactly as length() does,
-// true only when fl(fl(sqrt(d2)) - r) > bd holds for certain: squared distances with a relative
-// margin of 2^-14, far wider than the few roundings on either side, and only for bd >= 0 (where
-// a margin proportional to bd + r also clears bd's own rounding step). Skips the square root of
-// members that the exact test would cull anyway; never culls one that it would keep.
+// best distance so far cannot win). With d2 the squared distance |p - c|^2 (length_sq, as length()
+// computes it, or length_sq_fma), true only when fl(fl(sqrt(length_sq(p - c))) - r) > bd holds
+// for certain: squared distances with a relative margin of 2^-14, far wider than the few
+// roundings on either side, and only for bd >= 0 (where a margin proportional to bd + r also
+// clears bd's own rounding step). Skips the square root of members that the exact test would
+// cull anyway; never culls one that it would keep.
 MD bool far_beyond(float d2, float bd, float r) {
     float q = bd + r;
     return bd >= 0.0f && d2 > q * q * 1.00006103515625f;
@@ -187,9 +197,12 @@ MD bool weak_beyond(V l, bool ax, bool ay, bool az, float R, float c, float scl,
 // weak_beyond without the square root. In exact arithmetic its test is n > (bd + A) / K with
 // K = scl (c - 2^-10) > 0 and A = post + R scl (c + 2^-10) > 0; the generator passes A rounded up
 // and B = (1 + 2^-17) / K rounded up, so t = (bd + A) B exceeds the exact threshold by more than
-// the few binary32 roundings of t * t and n2 can take back, and n2 > t * t implies it.
+// the few binary32 roundings of t * t, n2 and the local point (rotated with fused multiply-adds,
+// rot_t_fma) can take back, and n2 > t * t implies it.
 MD bool weak_beyond_sq(V l, bool ax, bool ay, bool az, float A, float B, float bd) {
-    float n2 = (ax ? l.x * l.x : 0.0f) + (ay ? l.y * l.y : 0.0f) + (az ? l.z * l.z : 0.0f);
+    float n2 = az ? l.z * l.z : 0.0f;
+    n2 = ay ? __fmaf_rn(l.y, l.y, n2) : n2;
+    n2 = ax ? __fmaf_rn(l.x, l.x, n2) : n2;
     float t = (bd + A) * B;
     return bd >= 0.0f && n2 > t * t;
 }

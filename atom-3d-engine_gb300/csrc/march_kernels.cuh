@@ -380,7 +380,12 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         d = f.d;
         m = f.m;
         radius = fabsf(d);
-        e = FP::eps(h) * (1.0f + L.t * 0.5f) + FP::lod_footprint(h) * L.t;
+        // With a zero footprint, lod * t is a zero for every finite t (t is finite here: it
+        // passed the max_dist test). Adding a zero leaves a nonzero sum as it is and can change
+        // only the sign of a zero one, and e enters nothing but comparisons, where that sign does
+        // not count; so a field class with constant settings leaves the term out.
+        if (FP::kConstSettings && FP::lod_footprint(h) == 0.0f) e = FP::eps(h) * (1.0f + L.t * 0.5f);
+        else e = FP::eps(h) * (1.0f + L.t * 0.5f) + FP::lod_footprint(h) * L.t;
         bool overlap_fail = (L.step > 0.0f && d < 0.0f) || L.step > radius + L.prev_r;
         if (overlap_fail && d > 0.0f) {  // check the gap midpoint first
             L.x0 = d;

@@ -164,8 +164,33 @@ std::string csg_body(const DevCsgOp* op, size_t n) {
     return os.str();
 }
 
+// A plane whose normal is an axis, (+-1 on axis k, +0 on the others), with the identity
+// rotation, no point operations and an offset other than -0. For a finite local point l its
+// field dot(l, n) + h = ((l.x n.x + l.y n.y) + l.z n.z) + h is fl(+-l_k + h) bit for bit: the
+// products by +0 are zeros, which leave a nonzero sum as it is; where +-l_k is itself zero the
+// sum is a zero, and adding h gives h (h != 0) or +0 (h = +0) whatever the zeros' signs. For the
+// same reason the sign fix-ups of the identity rotation cannot show, so l_k is (p_k - pos_k) inv.
+bool axis_plane(const DevObject& o, int& k, bool& neg) {
+    if (o.prim != 10u || !(o.flags & OF_ROT_IDENTITY) || (o.flags & OF_POINT_OPS)) return false;
+    if (!std::isfinite(o.inv) || o.inv == 0.0f) return false;
+    uint32_t bits[4];
+    std::memcpy(bits, o.params, sizeof bits);
+    if (bits[3] == 0x80000000u || !std::isfinite(o.params[3])) return false;
+    k = -1;
+    for (int a = 0; a < 3; ++a) {
+        if (bits[a] == 0x3f800000u || bits[a] == 0xbf800000u) {
+            if (k >= 0) return false;
+            k = a;
+            neg = bits[a] == 0xbf800000u;
+        } else if (bits[a] != 0u) {
+            return false;
+        }
+    }
+    return k >= 0;
+}
+
 // An object's field with its record inlined; a CSG object's program is generated code too
-// (csg_ops: the tape's CSG ops, n_csg of them).
+// (csg_ops: the tape's CSG ops, n_csg of them), and an axis-aligned plane is one addition.
 std::string object_fn(uint32_t i, const DevObject& o, const DevCsgOp* csg_ops, uint32_t n_csg) {
     std::ostringstream os;
     const std::string body = o.prim == 11u && o.aux < n_csg ? csg_body(csg_ops + o.aux, n_csg - o.aux) : "";
@@ -173,8 +198,17 @@ std::string object_fn(uint32_t i, const DevObject& o, const DevCsgOp* csg_ops, u
         os << "__device__ __forceinline__ float csg_" << i << "(V l) {\n" << body << "}\n";
     os << "__device__ __forceinline__ Field obj_" << i << "(const Tape& T, V p) {\n"
        << "    const DevObject o = " << object_rec(o) << ";\n";
-    if (!body.empty()) os << "    return object_finish(o, csg_" << i << "(local_point(o, p)));\n}\n";
-    else os << "    return object_field(T, o, p);\n}\n";
+    int k = -1;
+    bool neg = false;
+    if (!body.empty()) {
+        os << "    return object_finish(o, csg_" << i << "(local_point(o, p)));\n}\n";
+    } else if (axis_plane(o, k, neg)) {
+        const char* axis[3] = {"p.x", "p.y", "p.z"};
+        os << "    const float lk = (" << axis[k] << " - " << fbits(o.pos[k]) << ") * " << fbits(o.inv) << ";\n"
+           << "    return object_finish(o, " << (neg ? "-lk" : "lk") << " + " << fbits(o.params[3]) << ");  // axis plane\n}\n";
+    } else {
+        os << "    return object_field(T, o, p);\n}\n";
+    }
     return os.str();
 }
 
@@ -334,7 +368,7 @@ std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
     std::ostringstream os;
     const std::string d =
         "p - V{" + fbits(o.pos[0]) + ", " + fbits(o.pos[1]) + ", " + fbits(o.pos[2]) + "}";
-    const std::string local = "scale(" + ((o.flags & OF_ROT_IDENTITY) ? d : "rot_t(RO, " + d + ")") + ", " +
+    const std::string local = "scale(" + ((o.flags & OF_ROT_IDENTITY) ? d : "rot_t_fma(RO, " + d + ")") + ", " +
                               fbits(o.inv) + "), " + (w.axis[0] ? "true" : "false") + ", " +
                               (w.axis[1] ? "true" : "false") + ", " + (w.axis[2] ? "true" : "false");
     const double eps = 1.0 / 1024.0;
@@ -506,15 +540,15 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 const std::string thr = smooth      ? "__fadd_ru(acc.d, " + fbits(o.k) + ")"
                                         : sg.b == 2u ? std::string("-acc.d")
                                                      : std::string("acc.d");
-                os << "        const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
-                   << fbits(o.bc[2]) << "});\n        if (!(acc.d < INF && acc.d > -INF"
-                   << (smooth ? " && acc.d != 0.0f" : "") << " && far_beyond(d2, fmaxf(" << thr << ", " << slack
+                os << "        const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
+                   << fbits(o.bc[2]) << "};\n        if (!(acc.d < INF && acc.d > -INF"
+                   << (smooth ? " && acc.d != 0.0f" : "") << " && far_beyond(length_sq_fma(dc), fmaxf(" << thr << ", " << slack
                    << "), " << fbits(o.br) << "))) {\n";
             }
             os << "        Field f;\n        bool sub = false;\n";
             if (o.flags & OF_BOUND)
                 os << "        {\n            float lower = "
-                   << (skip ? "sqrtf(d2) - " + fbits(o.br) : lower_expr(o)) << ";\n"
+                   << (skip ? "sqrtf(length_sq(dc)) - " + fbits(o.br) : lower_expr(o)) << ";\n"
                    << "            if (lower > " << slack << ") {\n                f = Field{lower, " << o.mat
                    << "u};\n                sub = true;\n            }\n        }\n";
             os << "        if (!sub) f = obj_" << sg.a << "(T, p);\n";
@@ -544,9 +578,9 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 const DevObject& o = obj[i];
                 if (cull && plain_sphere(o)) {
                     os << "        {  // member " << i << " (its exact field is its bound distance)\n"
-                       << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
-                       << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, bd, " << fbits(o.br)
-                       << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n"
+                       << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
+                       << fbits(o.bc[2]) << "};\n            if (!far_beyond(length_sq_fma(dc), bd, " << fbits(o.br)
+                       << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n"
                        << "            if (lower < bd || (lower == bd && " << i << " < bi)) {\n                bd = lower;\n"
                        << "                bi = " << i << ";\n                bm = " << o.mat
                        << "u;\n                bnc = false;\n            }\n            }\n        }\n";
@@ -571,15 +605,15 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 }
                 if (o.flags & OF_BOUND) {
                     if (cull) {
-                        os << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
-                           << ", " << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, bd, " << fbits(o.br)
-                           << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n";
+                        os << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
+                           << ", " << fbits(o.bc[2]) << "};\n            if (!far_beyond(length_sq_fma(dc), bd, " << fbits(o.br)
+                           << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n";
                     } else {
                         // beyond both the slack and bd, the member's value is its sphere distance and
                         // it cannot win: the squared pre-test skips the square root there
-                        os << "            const float d2 = length_sq(p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
-                           << ", " << fbits(o.bc[2]) << "});\n            if (!far_beyond(d2, fmaxf(bd, " << slack << "), "
-                           << fbits(o.br) << ")) {\n            const float lower = sqrtf(d2) - " << fbits(o.br) << ";\n";
+                        os << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
+                           << ", " << fbits(o.bc[2]) << "};\n            if (!far_beyond(length_sq_fma(dc), fmaxf(bd, " << slack << "), "
+                           << fbits(o.br) << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n";
                     }
                     if (cull) os << "            if (!(lower > bd)) {\n";
                     os << "            if (lower > " << slack << ") {\n                if (lower < bd || (lower == bd && "
@@ -606,7 +640,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             cluster_members(obj, cullable, clusters);
             for (const MemberCluster& cl : clusters) {
                 if (cl.members.size() > 1)
-                    os << "        if (!far_beyond(length_sq(p - V{" << fbits(cl.c[0]) << ", " << fbits(cl.c[1]) << ", "
+                    os << "        if (!far_beyond(length_sq_fma(p - V{" << fbits(cl.c[0]) << ", " << fbits(cl.c[1]) << ", "
                        << fbits(cl.c[2]) << "}), bd, " << fbits(cl.r) << ")) {  // cluster of "
                        << cl.members.size() << "\n";
                 for (uint32_t i : cl.members) member(i, true);

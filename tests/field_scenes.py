@@ -111,3 +111,23 @@ def csg_zoo_scene(seed, width=64, height=36):
         s.objects.append(o)
     cam = look_at((0.0, 3.2, -9.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), radians(50.0))
     return s, cam
+
+
+def planes_scene(width=64, height=36):
+    """A room of axis-aligned planes (normals +-x, +-y, -z; offsets positive, negative, +0 and -0;
+    translated and scaled objects) with a tilted plane and spheres in it: the specialised field
+    evaluates axis planes as one addition, which must give the interpreter's bits everywhere."""
+    s = Scene(width, height)
+    s.materials = [Material((0.8, 0.8, 0.8)), Material((0.7, 0.3, 0.2)), Material((0.2, 0.5, 0.7))]
+    s.objects = [
+        Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, 0),
+        Object(Prim.plane((0.0, -1.0, 0.0), 4.0), Transform.IDENTITY, 1),
+        Object(Prim.plane((1.0, 0.0, 0.0), 5.0), Transform((0.25, 0.0, 0.0)), 2),
+        Object(Prim.plane((-1.0, 0.0, 0.0), -0.0), Transform((5.5, 0.0, 0.0)), 1),
+        Object(Prim.plane((0.0, 0.0, -1.0), 6.0), Transform((0.0, 0.0, 0.5), scale=2.0), 2),
+        Object(Prim.plane((0.0, 0.6, 0.8), 2.5), Transform.IDENTITY, 0),
+        Object(Prim.sphere(0.8), Transform((-1.0, 0.8, 0.0)), 1),
+        Object(Prim.sphere(0.6), Transform((1.2, 0.6, 1.0)), 2),
+    ]
+    cam = look_at((0.0, 2.0, -9.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), radians(60.0))
+    return s, cam

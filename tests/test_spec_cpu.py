@@ -36,7 +36,7 @@ def test_generated_program_compiles_with_every_cull(name):
     if name == "smooth_chain":
         assert "__fadd_ru(acc.d, " in src and "fmaxf(-acc.d, " in src
     if name == "noncons":
-        assert "far_beyond(d2, fmaxf(bd, " in src
+        assert "far_beyond(length_sq_fma(dc), fmaxf(bd, " in src
     ok, msg, ms = mm3e_cuda.spec_compile_check(s)
     if not ok and "libnvrtc not found" in msg:
         pytest.skip("NVRTC is not installed")
@@ -76,6 +76,22 @@ def test_csg_programs_are_generated_code(seed):
     assert n_csg == 10
     assert "csg_eval" not in src
     assert src.count("__device__ __forceinline__ float csg_") == n_csg
+    ok, msg, ms = mm3e_cuda.spec_compile_check(s)
+    if not ok and "libnvrtc not found" in msg:
+        pytest.skip("NVRTC is not installed")
+    assert ok, msg
+
+
+def test_axis_planes_are_one_addition():
+    """Planes whose normal is an axis (+0 elsewhere), with the identity rotation and an offset
+    other than -0, are generated as one addition; the tilted plane and the -0 offset keep the
+    general field. The bit-identity with the interpreter is checked on the GPU
+    (test_gpu_spec.py, planes)."""
+    from field_scenes import planes_scene
+
+    s, _ = planes_scene(32, 18)
+    src = mm3e_cuda.spec_source(s)
+    assert src.count("// axis plane") == 4
     ok, msg, ms = mm3e_cuda.spec_compile_check(s)
     if not ok and "libnvrtc not found" in msg:
         pytest.skip("NVRTC is not installed")

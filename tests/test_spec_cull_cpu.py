@@ -4,8 +4,9 @@ A LINEAR union member is skipped when its bound lower = |p - c| - r exceeds the 
 far (accel.rs:98-100). The generated code first tests squared distances with a relative margin
 (far_beyond in device_math.cuh) for single members and for spatial clusters of members, skipping
 the square root. These tests replay that arithmetic in IEEE binary32 (numpy float32: correctly
-rounded, no contraction, as the device code compiled with --fmad=false) on adversarial points
-just outside the cull boundary, and check the clusters' enclosing spheres in exact arithmetic.
+rounded, no contraction, as the device code compiled with --fmad=false; the generated pre-tests'
+squared norms with their explicit fused multiply-adds, length_sq_fma) on adversarial points just
+outside the cull boundary, and check the clusters' enclosing spheres in exact arithmetic.
 """
 import re
 from fractions import Fraction
@@ -28,6 +29,19 @@ def length_sq(e):
     return F(F(F(e[..., 0] * e[..., 0]) + F(e[..., 1] * e[..., 1])) + F(e[..., 2] * e[..., 2]))
 
 
+def fma32(a, b, c):
+    """fl(a b + c) for float32 operands: the product is exact in binary64, the sum rounds there
+    and then to binary32 (a double rounding that can differ from one fused rounding by one unit
+    in rare ties, far inside the margins tested here)."""
+    return F(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+def length_sq_fma(e):
+    """device_math.cuh length_sq_fma: the squared norm the generated cull pre-tests take."""
+    z2 = F(e[..., 2] * e[..., 2])
+    return fma32(e[..., 0], e[..., 0], fma32(e[..., 1], e[..., 1], z2))
+
+
 def exact_lower(p, c, r):
     e = (p - c).astype(F)
     return F(np.sqrt(length_sq(e)).astype(F) - r)
@@ -47,14 +61,15 @@ def test_member_pretest_implies_exact_cull():
         r = F(rng.choice([0.0, rng.uniform(1e-3, 8.0)]))
         bd = F(rng.choice([0.0, rng.uniform(1e-6, 1e-2), rng.uniform(0.01, 30.0)]))
         p = _points_near(rng, c, float(bd) + float(r), 20000)
-        d2 = length_sq((p - c).astype(F))
-        skip = far_beyond(d2, bd, r)
         lower = exact_lower(p, c, r)
-        assert (lower[skip] > bd).all()
-        # the margin is narrow: most points the exact test culls are culled by the pre-test too
         culled = lower > bd
-        if culled.sum() > 1000:
-            assert skip.sum() >= 0.5 * culled.sum()
+        for norm in (length_sq, length_sq_fma):  # the interpreter's pre-test and the generated one
+            d2 = norm((p - c).astype(F))
+            skip = far_beyond(d2, bd, r)
+            assert (lower[skip] > bd).all()
+            # the margin is narrow: most points the exact test culls are culled by the pre-test too
+            if culled.sum() > 1000:
+                assert skip.sum() >= 0.5 * culled.sum()
 
 
 def test_negative_best_is_never_pretested():
@@ -68,16 +83,16 @@ def _clusters(src):
     out, cur = [], None
     lines = src.splitlines()
     for k, line in enumerate(lines):
-        m = re.search(r"far_beyond\(length_sq\(p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
+        m = re.search(r"far_beyond\(length_sq_fma\(p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
                       r"__uint_as_float\(0x(\w+)u\)\}\), bd, __uint_as_float\(0x(\w+)u\)\)\) \{  // cluster", line)
         if m:
             cur = (np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(m.group(4)), [])
             out.append(cur)
             continue
-        m = re.search(r"const float d2 = length_sq\(p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
-                      r"__uint_as_float\(0x(\w+)u\)\}\);", line)
+        m = re.search(r"const V dc = p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
+                      r"__uint_as_float\(0x(\w+)u\)\};", line)
         if m and cur is not None:
-            r = re.search(r"far_beyond\(d2, bd, __uint_as_float\(0x(\w+)u\)\)", lines[k + 1])
+            r = re.search(r"far_beyond\(length_sq_fma\(dc\), bd, __uint_as_float\(0x(\w+)u\)\)", lines[k + 1])
             cur[2].append((np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(r.group(1))))
         if "// end of cluster" in line:
             cur = None
@@ -106,7 +121,7 @@ def test_cluster_spheres_enclose_members_and_cull_safely():
                 assert _exact_norm_le((C.astype(np.float64) - c.astype(np.float64)), Fraction(float(R)) - Fraction(float(r)))
             for bd in (F(0.0), F(1e-4), F(0.3), F(4.0)):
                 p = _points_near(rng, C, float(bd) + float(R), 20000)
-                skip = far_beyond(length_sq((p - C).astype(F)), bd, R)
+                skip = far_beyond(length_sq_fma((p - C).astype(F)), bd, R)
                 for c, r in members:
                     assert (exact_lower(p[skip], c, r) > bd).all()
     assert n_clusters >= 2
@@ -211,3 +226,30 @@ def test_smooth_skip_holds_for_large_accumulators_and_small_blends():
         dist, h = _smooth_union_d(acc, lower, k)
         assert (h[skip] == F(1)).all()
         assert np.array_equal(dist[skip].view(np.uint32), acc[skip].view(np.uint32))
+
+
+def test_axis_plane_is_the_plane_field_bit_for_bit():
+    """An axis-aligned plane (+-1 on one axis, +0 on the others, identity rotation, offset other
+    than -0) is generated as fl(+-l_k + h) with l_k = (p_k - pos_k) inv (spec.cpp axis_plane).
+    Checked bit for bit against the field the interpreter takes, dot(l, n) + h with l the
+    identity-rotated, scaled local point (vec.rs:24-26 order; rot_t_identity), on signed zeros,
+    subnormals and ordinary coordinates, for every axis, sign, offset and scale tested."""
+    special = np.array([0.0, -0.0, 1e-45, -1e-45, 1.5e-39, -2.5e-39, 1.0, -1.0, 3.25, -7.5e3, 0.5, -0.25], F)
+    g = np.stack(np.meshgrid(special, special, special, indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(3)
+    g = np.concatenate([g, rng.uniform(-20, 20, (4000, 3)).astype(F)])
+    for k in range(3):
+        for sign in (F(1.0), F(-1.0)):
+            for h in (F(0.0), F(4.0), F(-2.5), F(1e-30)):
+                for pos, inv in ((np.zeros(3, F), F(1.0)), (np.array([0.25, -1.5, 0.5], F), F(0.5))):
+                    n = np.zeros(3, F)
+                    n[k] = sign
+                    d = (g - pos).astype(F)
+                    r = np.stack([F(d[:, 0] + _zero_with_sign_and(d[:, 1], d[:, 2])),
+                                  F(d[:, 1] + _zero_with_sign_and(d[:, 0], d[:, 2])),
+                                  F(d[:, 2] + _zero_with_sign_and(d[:, 0], d[:, 1]))], -1)
+                    l = (r * inv).astype(F)
+                    ref = F(F(F(F(l[:, 0] * n[0]) + F(l[:, 1] * n[1])) + F(l[:, 2] * n[2])) + h)
+                    lk = F(F(g[:, k] - pos[k]) * inv)
+                    fast = F((lk if sign > 0 else -lk) + h)
+                    assert np.array_equal(ref.view(np.uint32), fast.view(np.uint32)), (k, sign, h)

@@ -64,9 +64,9 @@ def _weak_constants(src):
     m = re.search(r"const float RO\[9\] = \{([^}]*)\};", src)
     if m:
         rot = np.array([_f(h) for h in re.findall(r"0x([0-9a-f]+)u", m.group(1))], F)
-        local = r"rot_t\(RO, p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}\)"
+        local = r"rot_t_fma\(RO, p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}\)"
     else:  # an identity rotation is left out of the test
-        rot = np.eye(3, dtype=F).reshape(-1)
+        rot = None
         local = r"p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}"
     head = r"\(scale\(" + local + ", " + _HEX + r"\), (true|false), (true|false), (true|false), "
     sq = re.search(r"weak_beyond_sq" + head + _HEX + ", " + _HEX + r", bd\) /\* weak bound R c scale post: " +
@@ -87,11 +87,30 @@ def _weak_constants(src):
     return (rot, pos, inv, axes) + consts + (ab,)
 
 
-def _local_n2(pts, rot, pos, inv, axes):
+def _fma32(a, b, c):
+    """fl(a b + c): the product is exact in binary64; the sum rounds there and then to binary32
+    (a double rounding that can differ from one fused rounding by a unit in rare ties, far
+    inside the margins tested here)."""
+    return F(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+def _local_n2(pts, rot, pos, inv, axes, fused=False):
+    """The squared norm of the local point over the kept axes, as the generated test computes it:
+    the rotation with fused multiply-adds (rot_t_fma; none for the identity), then the sum of
+    squares in weak_beyond's order, or with fused multiply-adds for weak_beyond_sq (fused)."""
     d = (pts - pos).astype(F)
-    l = np.stack([F(F(F(rot[3 * k] * d[:, 0]) + F(rot[3 * k + 1] * d[:, 1])) + F(rot[3 * k + 2] * d[:, 2]))
-                  for k in range(3)], axis=1)
+    if rot is None:
+        l = d
+    else:
+        l = np.stack([_fma32(rot[3 * k], d[:, 0], _fma32(rot[3 * k + 1], d[:, 1], F(rot[3 * k + 2] * d[:, 2])))
+                      for k in range(3)], axis=1)
     l = (l * inv).astype(F)
+    if fused:
+        n2 = F(l[:, 2] * l[:, 2]) if axes[2] else np.zeros(len(pts), F)
+        for a in (1, 0):
+            if axes[a]:
+                n2 = _fma32(l[:, a], l[:, a], n2)
+        return n2
     n2 = np.zeros(len(pts), F)
     for a in range(3):
         n2 = F(n2 + (F(l[:, a] * l[:, a]) if axes[a] else F(0)))
@@ -141,7 +160,7 @@ def test_weak_bound_holds(prim, mod, rotated):
     K = float(scl) * (float(c) - 2.0 ** -10)
     assert K > 0 and A >= float(post) + float(R) * float(scl) * (float(c) + 2.0 ** -10)
     assert B >= (1.0 + 2.0 ** -17) / K
-    n2 = _local_n2(pts, rot, pos, inv, axes)
+    n2 = _local_n2(pts, rot, pos, inv, axes, fused=True)
     for scale_bd in (0.5, 0.9, 0.99, 0.999, 1.0, 1.001):
         bd = np.maximum(lb * F(scale_bd), F(0)).astype(F)
         t = F(F(bd + A) * B)
