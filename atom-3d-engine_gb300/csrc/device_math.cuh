@@ -182,6 +182,12 @@ MD bool far_beyond(float d2, float bd, float r) {
     float q = bd + r;
     return bd >= 0.0f && d2 > q * q * 1.00006103515625f;
 }
+// far_beyond for a threshold that cannot be negative (fmaxf(x, s) with a constant s > 0, which
+// is s for a NaN x).
+MD bool far_beyond_pos(float d2, float thr, float r) {
+    float q = thr + r;
+    return d2 > q * q * 1.00006103515625f;
+}
 
 // Weak-bound cull of a union member whose exact sphere test does not apply (an unbounded
 // object, or one whose field can undercut its sphere): with l its local point, the field is at

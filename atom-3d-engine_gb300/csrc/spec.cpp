@@ -519,6 +519,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
     for (uint32_t s = 0; s < h->n_segments; ++s)
         if (walk[s]) os << walk_fn(s, seg[s], node, h->n_nodes, unb, h->slack, s > 0);
     const std::string slack = fbits(h->slack);
+    // pre-tests against fmaxf(x, slack) need no sign test of the threshold when slack > 0
+    const std::string fb_pos = h->slack > 0.0f ? "far_beyond_pos" : "far_beyond";
     os << "__device__ __forceinline__ Field eval(const Tape& T, V p) {\n"
           "    const float INF = __int_as_float(0x7f800000);\n"
           "    Field acc{INF, 0u};\n";
@@ -541,8 +543,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                                         : sg.b == 2u ? std::string("-acc.d")
                                                      : std::string("acc.d");
                 os << "        const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
-                   << fbits(o.bc[2]) << "};\n        if (!(acc.d < INF && acc.d > -INF"
-                   << (smooth ? " && acc.d != 0.0f" : "") << " && far_beyond(length_sq_fma(dc), fmaxf(" << thr << ", " << slack
+                   << fbits(o.bc[2]) << "};\n        if (!(fabsf(acc.d) < INF"
+                   << (smooth ? " && acc.d != 0.0f" : "") << " && " << fb_pos << "(length_sq_fma(dc), fmaxf(" << thr << ", " << slack
                    << "), " << fbits(o.br) << "))) {\n";
             }
             os << "        Field f;\n        bool sub = false;\n";
@@ -612,7 +614,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                         // beyond both the slack and bd, the member's value is its sphere distance and
                         // it cannot win: the squared pre-test skips the square root there
                         os << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
-                           << ", " << fbits(o.bc[2]) << "};\n            if (!far_beyond(length_sq_fma(dc), fmaxf(bd, " << slack << "), "
+                           << ", " << fbits(o.bc[2]) << "};\n            if (!" << fb_pos << "(length_sq_fma(dc), fmaxf(bd, " << slack << "), "
                            << fbits(o.br) << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n";
                     }
                     if (cull) os << "            if (!(lower > bd)) {\n";
@@ -701,9 +703,15 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
     // walks are inlined), the gallery's march and shadow fit that without spills (62 / 59), and the
     // extra resident warps hide branch and instruction-fetch latency. (Left to itself, ptxas gave
     // the shadow kernel 64 registers with spills.)
+    // The shadow kernel of a small field (at most 16 objects, no CSG program) asks for 10 CTAs of
+    // 128 (5 of 256), 48 registers: the gallery's fits without spills and its shadow pass took
+    // 0.648 against 0.681 ms per 1080p frame. The fields of larger scenes (the C4 procedural
+    // scenes) mostly need fewer registers anyway, and some of them spill at 48.
+    const bool small_field = h->n_objects <= 16 && h->n_csg_ops == 0;
     const uint32_t mb = min_blocks ? min_blocks : (block <= 128 ? 8u : 4u);
+    const uint32_t mb_shadow = min_blocks ? min_blocks : small_field ? (block <= 128 ? 10u : 5u) : (block <= 128 ? 8u : 4u);
     const std::string march_bounds = std::to_string(block) + ", " + std::to_string(mb);
-    const std::string bounds = march_bounds;
+    const std::string bounds = std::to_string(block) + ", " + std::to_string(mb_shadow);
     os << "extern \"C\" __global__ void __launch_bounds__(" << march_bounds
        << ") mm3e_spec_march(const __grid_constant__ mm3e::WaveArgs a) {\n    mm3e::wave::march_body<" << tm << ", "
        << unroll << ", mm3e::spec::Field_>(a);\n}\n"
