@@ -612,6 +612,7 @@ __device__ __forceinline__ void s_step(SLane& S, const LaneTape<TM>& LT, const W
 template <int TM, int UNROLL, class FP>
 __device__ __forceinline__ void shadow_body(const WaveArgs& a) {
     extern __shared__ __align__(128) unsigned char smem[];
+    if (pass_failed(a)) return;
     LaneTape<TM> LT;
     if constexpr (TM == TM_SMEM) {
         if (!stage_tape(smem, a.job0.tape, a.tape_bytes, a.status, a.wait_limit, a.wait_probe != 0u)) return;

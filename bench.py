@@ -736,7 +736,9 @@ def run_ours(args):
     prof_total = sum(ms for _, ms in kt.values())
     kernels = {k: {"launches_per_frame": n / args.steps, "ms_per_frame": ms / args.steps,
                    "share": ms / prof_total if prof_total else None} for k, (n, ms) in kt.items()}
-    dom = max(kt, key=lambda k: kt[k][1]) if kt else "march"
+    # the roofline kernel is the primary-level march (the reflection level's event time includes
+    # its overlap with the primary level's passes on the other streams)
+    dom = "march" if "march" in kt else (max(kt, key=lambda k: kt[k][1]) if kt else "march")
     dom_s = kt[dom][1] / args.steps / 1000.0 if kt else None
     roofline = {"bound": "fp32", "unit": "TFLOP/s", "peak": peak,
                 "peak_basis": f"{sm} SMs x 128 FP32 lanes x 2 (FMA) x {max_mhz:.0f} MHz max SM clock "
