@@ -182,6 +182,25 @@ MD bool far_beyond(float d2, float bd, float r) {
     float q = bd + r;
     return bd >= 0.0f && d2 > q * q * 1.00006103515625f;
 }
+// Linearised pre-tests. cull_base(p) = fl(|p|^2 mu), mu = 1 - 2^-19, once per field evaluation;
+// dist2_below(p, base, -2c, mu |c|^2 rounded down) = fl((base + c2) - 2 p.c) in fused
+// multiply-adds. Its roundings stay within 11 units of roundoff (2^-24 each) of |p|^2 + |c|^2,
+// less than the 2^-19 (|p|^2 + |c|^2) that mu takes off, so it never exceeds |p - c|^2.
+// far_beyond_lin(d2, bd, 2 M r, M r^2) with M = 1 + 2^-14 and both constants rounded up: d2 above
+// fl(M bd^2 + 2 M r bd + M r^2) puts |p - c|^2 above (bd + r)^2 (1 + 2^-15), and from there
+// fl(fl(sqrt(length_sq(p - c))) - r) > bd for bd >= 0 as in far_beyond. Three fused
+// multiply-adds and one addition for the distance, two for the threshold: fewer instructions than
+// the difference vector, its norm and the squared threshold.
+MD float cull_base(V p) { return length_sq_fma(p) * 0.99999809265136719f; }
+MD float dist2_below(V p, float base, float ax, float ay, float az, float c2) {
+    return __fmaf_rn(p.x, ax, __fmaf_rn(p.y, ay, __fmaf_rn(p.z, az, base + c2)));
+}
+MD bool far_beyond_lin(float d2, float bd, float m2r, float mr2) {
+    return bd >= 0.0f && d2 > __fmaf_rn(bd, __fmaf_rn(bd, 1.00006103515625f, m2r), mr2);
+}
+MD bool far_beyond_lin_pos(float d2, float thr, float m2r, float mr2) {
+    return d2 > __fmaf_rn(thr, __fmaf_rn(thr, 1.00006103515625f, m2r), mr2);
+}
 // far_beyond for a threshold that cannot be negative (fmaxf(x, s) with a constant s > 0, which
 // is s for a NaN x).
 MD bool far_beyond_pos(float d2, float thr, float r) {

@@ -352,6 +352,13 @@ WeakBound weak_bound(const DevObject& o) {
     return w;
 }
 
+// The nearest binary32 value at or below x.
+float float_at_or_below(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+
 // The nearest binary32 value at or above x.
 float float_at_or_above(double x) {
     float f = (float)x;
@@ -393,6 +400,24 @@ bool plain_sphere(const DevObject& o) {
     return o.prim == 0u && (o.flags & OF_BOUND) && (o.flags & OF_ROT_IDENTITY) &&
            !(o.flags & (OF_POINT_OPS | OF_ROUND | OF_ONION)) && o.scale == 1.0f && o.inv == 1.0f &&
            o.bc[0] == o.pos[0] && o.bc[1] == o.pos[1] && o.bc[2] == o.pos[2] && o.br == o.params[0];
+}
+
+// The linearised sphere pre-test (far_beyond_lin in device_math.cuh) of the sphere (c, r)
+// against `thr`, which `pos` marks as never negative; CB is the evaluation's cull_base(p). The
+// constants are -2c (exact), mu |c|^2 rounded down, 2 M r and M r^2 rounded up (mu = 1 - 2^-19,
+// M = 1 + 2^-14), each from binary64 arithmetic nudged by 2^-50 the safe way. Empty when the
+// sphere's radius is not a finite non-negative number.
+std::string lin_test(const float* c, float r, const std::string& thr, bool pos) {
+    if (!(r >= 0.0f) || !std::isfinite(r)) return "";
+    const double mu = 1.0 - std::ldexp(1.0, -19), M = 1.0 + std::ldexp(1.0, -14), nudge = std::ldexp(1.0, -50);
+    const double cc = (double)c[0] * c[0] + (double)c[1] * c[1] + (double)c[2] * c[2];
+    const float c2 = float_at_or_below(mu * cc * (1.0 - nudge));
+    const float m2r = float_at_or_above(2.0 * M * (double)r * (1.0 + nudge));
+    const float mr2 = float_at_or_above(M * (double)r * (double)r * (1.0 + nudge));
+    if (!std::isfinite(c2) || !std::isfinite(m2r) || !std::isfinite(mr2)) return "";
+    return std::string(pos ? "far_beyond_lin_pos" : "far_beyond_lin") + "(dist2_below(p, CB, " + fbits(-2.0f * c[0]) +
+           ", " + fbits(-2.0f * c[1]) + ", " + fbits(-2.0f * c[2]) + ", " + fbits(c2) + "), " + thr + ", " + fbits(m2r) +
+           ", " + fbits(mr2) + ")";
 }
 
 std::string lower_expr(const DevObject& o) {
@@ -520,9 +545,18 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
         if (walk[s]) os << walk_fn(s, seg[s], node, h->n_nodes, unb, h->slack, s > 0);
     const std::string slack = fbits(h->slack);
     // pre-tests against fmaxf(x, slack) need no sign test of the threshold when slack > 0
-    const std::string fb_pos = h->slack > 0.0f ? "far_beyond_pos" : "far_beyond";
+    const bool slack_pos = h->slack > 0.0f;
+    const std::string fb_pos = slack_pos ? "far_beyond_pos" : "far_beyond";
+    // a sphere pre-test: the linearised form, or the squared distance where that is not available
+    auto sphere_test = [&](const float* c, float r, const std::string& thr, bool pos) -> std::string {
+        const std::string lt = lin_test(c, r, thr, pos);
+        if (!lt.empty()) return lt;
+        return std::string(pos ? fb_pos : std::string("far_beyond")) + "(length_sq_fma(p - V{" + fbits(c[0]) + ", " +
+               fbits(c[1]) + ", " + fbits(c[2]) + "}), " + thr + ", " + fbits(r) + ")";
+    };
     os << "__device__ __forceinline__ Field eval(const Tape& T, V p) {\n"
           "    const float INF = __int_as_float(0x7f800000);\n"
+          "    const float CB = cull_base(p);\n"
           "    Field acc{INF, 0u};\n";
     for (uint32_t s = 0; s < h->n_segments; ++s) {
         const DevSegment& sg = seg[s];
@@ -542,15 +576,18 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 const std::string thr = smooth      ? "__fadd_ru(acc.d, " + fbits(o.k) + ")"
                                         : sg.b == 2u ? std::string("-acc.d")
                                                      : std::string("acc.d");
-                os << "        const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
-                   << fbits(o.bc[2]) << "};\n        if (!(fabsf(acc.d) < INF"
-                   << (smooth ? " && acc.d != 0.0f" : "") << " && " << fb_pos << "(length_sq_fma(dc), fmaxf(" << thr << ", " << slack
-                   << "), " << fbits(o.br) << "))) {\n";
+                const std::string keep = "fabsf(acc.d) < INF" + std::string(smooth ? " && acc.d != 0.0f" : "");
+                const std::string thr2 = "fmaxf(" + thr + ", " + slack + ")";
+                const std::string lt = lin_test(o.bc, o.br, thr2, slack_pos);
+                if (!lt.empty())
+                    os << "        if (!(" << keep << " && " << lt << ")) {\n";
+                else
+                    os << "        if (!(" << keep << " && " << fb_pos << "(length_sq_fma(p - V{" << fbits(o.bc[0]) << ", "
+                       << fbits(o.bc[1]) << ", " << fbits(o.bc[2]) << "}), " << thr2 << ", " << fbits(o.br) << "))) {\n";
             }
             os << "        Field f;\n        bool sub = false;\n";
             if (o.flags & OF_BOUND)
-                os << "        {\n            float lower = "
-                   << (skip ? "sqrtf(length_sq(dc)) - " + fbits(o.br) : lower_expr(o)) << ";\n"
+                os << "        {\n            float lower = " << lower_expr(o) << ";\n"
                    << "            if (lower > " << slack << ") {\n                f = Field{lower, " << o.mat
                    << "u};\n                sub = true;\n            }\n        }\n";
             os << "        if (!sub) f = obj_" << sg.a << "(T, p);\n";
@@ -580,9 +617,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 const DevObject& o = obj[i];
                 if (cull && plain_sphere(o)) {
                     os << "        {  // member " << i << " (its exact field is its bound distance)\n"
-                       << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1]) << ", "
-                       << fbits(o.bc[2]) << "};\n            if (!far_beyond(length_sq_fma(dc), bd, " << fbits(o.br)
-                       << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n"
+                       << "            if (!" << sphere_test(o.bc, o.br, "bd", false) << ") {\n"
+                       << "            const float lower = " << lower_expr(o) << ";\n"
                        << "            if (lower < bd || (lower == bd && " << i << " < bi)) {\n                bd = lower;\n"
                        << "                bi = " << i << ";\n                bm = " << o.mat
                        << "u;\n                bnc = false;\n            }\n            }\n        }\n";
@@ -607,15 +643,13 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 }
                 if (o.flags & OF_BOUND) {
                     if (cull) {
-                        os << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
-                           << ", " << fbits(o.bc[2]) << "};\n            if (!far_beyond(length_sq_fma(dc), bd, " << fbits(o.br)
-                           << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n";
+                        os << "            if (!" << sphere_test(o.bc, o.br, "bd", false) << ") {\n"
+                           << "            const float lower = " << lower_expr(o) << ";\n";
                     } else {
                         // beyond both the slack and bd, the member's value is its sphere distance and
                         // it cannot win: the squared pre-test skips the square root there
-                        os << "            const V dc = p - V{" << fbits(o.bc[0]) << ", " << fbits(o.bc[1])
-                           << ", " << fbits(o.bc[2]) << "};\n            if (!" << fb_pos << "(length_sq_fma(dc), fmaxf(bd, " << slack << "), "
-                           << fbits(o.br) << ")) {\n            const float lower = sqrtf(length_sq(dc)) - " << fbits(o.br) << ";\n";
+                        os << "            if (!" << sphere_test(o.bc, o.br, "fmaxf(bd, " + slack + ")", slack_pos) << ") {\n"
+                           << "            const float lower = " << lower_expr(o) << ";\n";
                     }
                     if (cull) os << "            if (!(lower > bd)) {\n";
                     os << "            if (lower > " << slack << ") {\n                if (lower < bd || (lower == bd && "
@@ -642,9 +676,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             cluster_members(obj, cullable, clusters);
             for (const MemberCluster& cl : clusters) {
                 if (cl.members.size() > 1)
-                    os << "        if (!far_beyond(length_sq_fma(p - V{" << fbits(cl.c[0]) << ", " << fbits(cl.c[1]) << ", "
-                       << fbits(cl.c[2]) << "}), bd, " << fbits(cl.r) << ")) {  // cluster of "
-                       << cl.members.size() << "\n";
+                    os << "        if (!" << sphere_test(cl.c, cl.r, "bd", false) << ") {  // cluster of " << cl.members.size()
+                       << ", radius " << fbits(cl.r) << "\n";
                 for (uint32_t i : cl.members) member(i, true);
                 if (cl.members.size() > 1) os << "        }  // end of cluster\n";
             }

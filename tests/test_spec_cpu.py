@@ -36,7 +36,7 @@ def test_generated_program_compiles_with_every_cull(name):
     if name == "smooth_chain":
         assert "__fadd_ru(acc.d, " in src and "fmaxf(-acc.d, " in src
     if name == "noncons":
-        assert "far_beyond_pos(length_sq_fma(dc), fmaxf(bd, " in src
+        assert "far_beyond_lin_pos(dist2_below(p, CB, " in src and "fmaxf(bd, " in src
     ok, msg, ms = mm3e_cuda.spec_compile_check(s)
     if not ok and "libnvrtc not found" in msg:
         pytest.skip("NVRTC is not installed")

@@ -42,6 +42,50 @@ def length_sq_fma(e):
     return fma32(e[..., 0], e[..., 0], fma32(e[..., 1], e[..., 1], z2))
 
 
+def _round32(x):
+    """The binary32 value nearest the rational x (ties to even)."""
+    f = np.float32(float(x))
+    best = f
+    for cand in (np.nextafter(f, F(-np.inf)), np.nextafter(f, F(np.inf))):
+        dc, db = abs(Fraction(float(cand)) - x), abs(Fraction(float(best)) - x)
+        if dc < db or (dc == db and (int(cand.view(np.uint32)) & 1) == 0):
+            best = cand
+    return best
+
+
+def _fma(a, b, c):
+    return _round32(Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c)))
+
+
+MU = F(1.0 - 2.0 ** -19)
+
+
+def _lin_constants(c, r):
+    """spec.cpp lin_test's constants: -2c, mu |c|^2 rounded down, 2 M r and M r^2 rounded up."""
+    M = Fraction(1) + Fraction(1, 2 ** 14)
+    cc = sum(Fraction(float(x)) ** 2 for x in c) * Fraction(float(MU))
+    c2 = np.float32(float(cc))
+    if Fraction(float(c2)) > cc:
+        c2 = np.nextafter(c2, F(-np.inf))
+    up = lambda x: (lambda f: f if Fraction(float(f)) >= x else np.nextafter(f, F(np.inf)))(np.float32(float(x)))
+    return (-2 * c).astype(F), c2, up(2 * M * Fraction(float(r))), up(M * Fraction(float(r)) ** 2)
+
+
+def dist2_below_exact(p, c, base=None):
+    """device_math.cuh dist2_below(p, cull_base(p), -2c, c2), every rounding exact."""
+    a, c2, _, _ = _lin_constants(c, F(0))
+    P2 = _fma(p[0], p[0], _fma(p[1], p[1], _round32(Fraction(float(p[2])) ** 2)))
+    base = _round32(Fraction(float(P2)) * Fraction(float(MU)))
+    s = _round32(Fraction(float(base)) + Fraction(float(c2)))
+    return _fma(p[0], a[0], _fma(p[1], a[1], _fma(p[2], a[2], s)))
+
+
+def far_beyond_lin_exact(p, c, r, bd):
+    _, _, m2r, mr2 = _lin_constants(c, r)
+    q = _fma(bd, _fma(bd, F(1.00006103515625), m2r), mr2)
+    return bool(bd >= 0) and dist2_below_exact(p, c) > q
+
+
 def exact_lower(p, c, r):
     e = (p - c).astype(F)
     return F(np.sqrt(length_sq(e)).astype(F) - r)
@@ -78,22 +122,23 @@ def test_negative_best_is_never_pretested():
 
 
 def _clusters(src):
-    """(centre, radius, [(member centre, member radius)]) of every cluster in generated source."""
+    """(centre, radius, [(member centre, member radius)]) of every cluster in generated source: a
+    cluster's centre is -1/2 of its linearised test's -2c constants, its radius is in the line's
+    comment; a member's centre and radius are in its bound distance line (length(p - c) - r)."""
     hexf = lambda h: np.array([int(h, 16)], np.uint32).view(F)[0]
+    H = r"__uint_as_float\(0x(\w+)u\)"
     out, cur = [], None
-    lines = src.splitlines()
-    for k, line in enumerate(lines):
-        m = re.search(r"far_beyond\(length_sq_fma\(p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
-                      r"__uint_as_float\(0x(\w+)u\)\}\), bd, __uint_as_float\(0x(\w+)u\)\)\) \{  // cluster", line)
+    for line in src.splitlines():
+        m = re.search(r"far_beyond_lin\(dist2_below\(p, CB, " + H + ", " + H + ", " + H + ", " + H +
+                      r"\), bd, " + H + ", " + H + r"\)\) \{  // cluster of \d+, radius " + H, line)
         if m:
-            cur = (np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(m.group(4)), [])
+            c = np.array([hexf(m.group(i)) for i in (1, 2, 3)], F) * F(-0.5)
+            cur = (c.astype(F), hexf(m.group(7)), [])
             out.append(cur)
             continue
-        m = re.search(r"const V dc = p - V\{__uint_as_float\(0x(\w+)u\), __uint_as_float\(0x(\w+)u\), "
-                      r"__uint_as_float\(0x(\w+)u\)\};", line)
+        m = re.search(r"const float lower = length\(p - V\{" + H + ", " + H + ", " + H + r"\}\) - " + H + ";", line)
         if m and cur is not None:
-            r = re.search(r"far_beyond\(length_sq_fma\(dc\), bd, __uint_as_float\(0x(\w+)u\)\)", lines[k + 1])
-            cur[2].append((np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(r.group(1))))
+            cur[2].append((np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(m.group(4))))
         if "// end of cluster" in line:
             cur = None
     return out
@@ -124,6 +169,11 @@ def test_cluster_spheres_enclose_members_and_cull_safely():
                 skip = far_beyond(length_sq_fma((p - C).astype(F)), bd, R)
                 for c, r in members:
                     assert (exact_lower(p[skip], c, r) > bd).all()
+                # the linearised test the generated code takes
+                pts = p[rng.choice(len(p), 150, replace=False)]
+                skip = np.array([far_beyond_lin_exact(q, C, R, bd) for q in pts])
+                for c, r in members:
+                    assert (exact_lower(pts[skip], c, r) > bd).all()
     assert n_clusters >= 2
 
 
@@ -253,3 +303,36 @@ def test_axis_plane_is_the_plane_field_bit_for_bit():
                     lk = F(F(g[:, k] - pos[k]) * inv)
                     fast = F((lk if sign > 0 else -lk) + h)
                     assert np.array_equal(ref.view(np.uint32), fast.view(np.uint32)), (k, sign, h)
+
+
+def test_linearised_distance_never_exceeds_the_squared_distance():
+    """dist2_below (|p|^2 mu + mu |c|^2 - 2 p.c in fused multiply-adds) is a lower bound of
+    |p - c|^2 in exact arithmetic: on points all over, near c (where the difference cancels) and
+    far away, with every binary32 rounding done exactly."""
+    rng = np.random.default_rng(2)
+    for it in range(3000):
+        c = (rng.standard_normal(3) * rng.uniform(0, 30)).astype(F)
+        if it % 3 == 0:
+            p = (c + rng.standard_normal(3) * 10.0 ** rng.uniform(-6, 0)).astype(F)
+        else:
+            p = (rng.standard_normal(3) * 10.0 ** rng.uniform(-2, 2.5)).astype(F)
+        exact = sum((Fraction(float(p[i])) - Fraction(float(c[i]))) ** 2 for i in range(3))
+        assert Fraction(float(dist2_below_exact(p, c))) <= exact, (p, c)
+
+
+def test_linearised_pretest_implies_exact_cull():
+    """far_beyond_lin never culls a member that the exact bound test keeps, on points just outside
+    the cull boundary; 2% beyond it, it culls them all."""
+    rng = np.random.default_rng(13)
+    for _ in range(30):
+        c = rng.uniform(-50, 50, 3).astype(F)
+        r = F(rng.choice([0.0, rng.uniform(1e-3, 8.0)]))
+        bd = F(rng.choice([0.0, rng.uniform(1e-6, 1e-2), rng.uniform(0.01, 30.0)]))
+        p = _points_near(rng, c, float(bd) + float(r), 200)
+        lower = exact_lower(p, c, r)
+        skip = np.array([far_beyond_lin_exact(q, c, r, bd) for q in p])
+        assert (lower[skip] > bd).all()
+        if float(bd) + float(r) > 0.5:
+            far = _points_near(rng, c, (float(bd) + float(r)) * 1.02, 50)
+            assert all(far_beyond_lin_exact(q, c, r, bd) for q in far)
+    assert not far_beyond_lin_exact(np.array([1e3, 0, 0], F), np.zeros(3, F), F(1.0), F(-0.5))
