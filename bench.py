@@ -266,7 +266,7 @@ def bench_batched(ctx, stream, torch, n_scenes):
     pixels = sum(s.width * s.height for s, _ in items)
     jobs = ctx.make_jobs([(c, cam, 0, 0, abi.FB_RGBA8, o.data_ptr(), None)
                           for c, (s, cam), o in zip(compiled, items, outs)])
-    ctx.configure_batch(max_samples=1 << 24, use_graphs=True)
+    ctx.configure_batch(max_samples=1 << 28, use_graphs=True)  # all 256 scenes in one pass sequence
     t0 = time.perf_counter()
     best, table = ctx.autotune(ctx.make_jobs([(c, cam, 0, 0, abi.FB_RGBA8, o.data_ptr(), None)
                                               for c, (s, cam), o in list(zip(compiled, items, outs))[:32]]))
