@@ -386,7 +386,11 @@ __device__ __forceinline__ void m_step(MLane& L, const LaneTape<TM>& LT, const W
         // not count; so a field class with constant settings leaves the term out.
         if (FP::kConstSettings && FP::lod_footprint(h) == 0.0f) e = FP::eps(h) * (1.0f + L.t * 0.5f);
         else e = FP::eps(h) * (1.0f + L.t * 0.5f) + FP::lod_footprint(h) * L.t;
-        bool overlap_fail = (L.step > 0.0f && d < 0.0f) || L.step > radius + L.prev_r;
+        // With a step scale in [0, 1) there is no boost, so a step is fl(d_prev * scale), at most
+        // |d_prev| = prev_r (and 0 after a rollback): it never exceeds radius + prev_r, and with
+        // constant settings that test and the COVER phase it leads to are compiled out.
+        const bool can_overshoot = !FP::kConstSettings || !(FP::step_scale(h) >= 0.0f && FP::step_scale(h) < 1.0f);
+        bool overlap_fail = (L.step > 0.0f && d < 0.0f) || (can_overshoot && L.step > radius + L.prev_r);
         if (overlap_fail && d > 0.0f) {  // check the gap midpoint first
             L.x0 = d;
             L.xu = m;
