@@ -106,6 +106,11 @@ std::string object_rec(const DevObject& o) {
     return os.str();
 }
 
+// Fields of more objects than this take no weak bound for CSG objects and no weak skip of
+// unbounded one-object segments: their tests run at every sample, and in a field that large the
+// code they add costs more in instruction fetch than the exact evaluations they save.
+constexpr uint32_t kWeakExtraObjects = 32;
+
 // A CSG program (csg.rs:95-118, the post-order stack program csg_eval runs over `op`, at most
 // `n` ops) as straight-line code over the local point `l`: the stack depths after every op are
 // known when the program is generated, so each stack slot becomes a named local and each
@@ -294,11 +299,11 @@ struct WeakBound {
     bool axis[3] = {true, true, true};
 };
 
-WeakBound weak_bound(const DevObject& o) {
-    WeakBound w;
-    const float* q = o.params;
-    double R = 0.0, c = 0.999;
-    switch (o.prim) {
+// A primitive's weak constants: its field is at least c * (|q| - R) outside the ball of radius R
+// about its local origin (see WeakBound). False for a plane (unbounded) and unknown kinds.
+bool prim_weak(uint32_t kind, const float* q, double& R, double& c) {
+    c = 0.999;
+    switch (kind) {
         case 0: R = q[0]; break;
         case 1:
         case 2: R = std::sqrt((double)q[0] * q[0] + (double)q[1] * q[1] + (double)q[2] * q[2]); break;
@@ -313,7 +318,7 @@ WeakBound weak_bound(const DevObject& o) {
         case 6: R = std::max((double)q[0], (double)q[2] + q[1]); break;
         case 7: {
             double rmax = std::max(std::max(q[0], q[1]), q[2]), rmin = std::min(std::min(q[0], q[1]), q[2]);
-            if (!(rmin > 0.0)) return w;
+            if (!(rmin > 0.0)) return false;
             R = rmax;
             c = 0.999 * rmin / rmax;
             break;
@@ -324,7 +329,82 @@ WeakBound weak_bound(const DevObject& o) {
             R = std::sqrt(circ * circ + (double)q[1] * q[1]);
             break;
         }
-        default: return w;  // plane, CSG, volume
+        default: return false;  // plane, CSG, volume
+    }
+    return R >= 0.0 && std::isfinite(R);
+}
+
+// A CSG program's weak constants (csg.rs:95-118; the post-order program csg_eval runs), from the
+// bounds of its parts: with each part's field at least c_i (|q| - R_i) - post_i outside its ball,
+//   union, smooth union:  min over the parts, so c = min c_i, R = max R_i, post = max post_i
+//                         (+ k/4 for the smooth one, whose blend is at least the minimum - k/4);
+//   intersection:         at least either part (the one with the smaller ball is kept);
+//   subtraction:          at least its first part;
+//   offset o, shell t:    post + o, post + t (|d| - t >= d - t);
+//   transform (pos, s):   the part at the local point R^T (q - pos) / s, times s: c kept, R =
+//                         |pos| + s R_part, post = s post_part (the rotation keeps norms, checked).
+// False when a part has no bound (a plane) or the program is not one the interpreter runs to a
+// defined end.
+bool csg_weak(const DevCsgOp* op, size_t n, double& R, double& c, double& post) {
+    struct Part {
+        double R, c, post;
+    };
+    std::vector<Part> vals;
+    std::vector<double> pos_norm;
+    for (size_t g = 0; g < 4096 && g < n; ++g, ++op) {
+        const uint32_t k = op->op;
+        if (k == CSG_OP_PRIM) {
+            Part pt{0.0, 0.0, 0.0};
+            if (!prim_weak(op->kind, op->p, pt.R, pt.c)) return false;
+            vals.push_back(pt);
+        } else if (k == CSG_OP_XFORM) {
+            const float* r = op->rot;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    double d = (double)r[a * 3] * r[b * 3] + (double)r[a * 3 + 1] * r[b * 3 + 1] +
+                               (double)r[a * 3 + 2] * r[b * 3 + 2];
+                    if (std::fabs(d - (a == b ? 1.0 : 0.0)) > 1e-5) return false;
+                }
+            pos_norm.push_back(std::sqrt((double)op->pos[0] * op->pos[0] + (double)op->pos[1] * op->pos[1] +
+                                         (double)op->pos[2] * op->pos[2]));
+        } else if (k == CSG_OP_UNXFORM) {
+            if (vals.empty() || pos_norm.empty() || !(op->scale > 0.0f)) return false;
+            Part& t = vals.back();
+            t.R = pos_norm.back() + (double)op->scale * t.R;
+            t.post = (double)op->scale * t.post;
+            pos_norm.pop_back();
+        } else if (k == CSG_OP_UNION || k == CSG_OP_SMOOTH || k == CSG_OP_INTERSECT || k == CSG_OP_SUBTRACT) {
+            if (vals.size() < 2) return false;
+            const Part b = vals.back();
+            vals.pop_back();
+            Part& a = vals.back();
+            if (k == CSG_OP_UNION || k == CSG_OP_SMOOTH) {
+                a = Part{std::max(a.R, b.R), std::min(a.c, b.c), std::max(a.post, b.post)};
+                if (k == CSG_OP_SMOOTH && op->p[0] > 0.0f) a.post += 0.25 * (double)op->p[0];
+            } else if (k == CSG_OP_INTERSECT && b.R < a.R) {
+                a = b;
+            }
+        } else if (k == CSG_OP_OFFSET || k == CSG_OP_SHELL) {
+            if (vals.empty()) return false;
+            vals.back().post += (double)op->p[0];
+        } else {
+            break;
+        }
+    }
+    if (vals.size() != 1 || !pos_norm.empty()) return false;
+    R = vals[0].R;
+    c = vals[0].c;
+    post = vals[0].post;
+    return R >= 0.0 && std::isfinite(R) && std::isfinite(post) && c > 0.0;
+}
+
+WeakBound weak_bound(const DevObject& o, const DevCsgOp* csg, uint32_t n_csg) {
+    WeakBound w;
+    double R = 0.0, c = 0.999, shape_post = 0.0;
+    if (o.prim == 11u) {
+        if (!csg || o.aux >= n_csg || !csg_weak(csg + o.aux, n_csg - o.aux, R, c, shape_post)) return w;
+    } else if (!prim_weak(o.prim, o.params, R, c)) {
+        return w;
     }
     if (!(R >= 0.0) || !std::isfinite(R)) return w;
     if (o.flags & OF_ELONGATE)
@@ -338,7 +418,7 @@ WeakBound weak_bound(const DevObject& o) {
                 kept -= 1;
             }
     if (kept == 0) return w;
-    double post = 0.0;
+    double post = shape_post * (double)o.scale;
     if (o.flags & OF_ROUND) post += o.round;
     if (o.flags & OF_ONION) {
         if (!(o.onion >= 0.0f)) return w;
@@ -371,7 +451,7 @@ float float_at_or_above(double x) {
 // skipped products could only change the signs of zero coordinates). With positive constants the
 // test compares squared norms (weak_beyond_sq); a trailing comment keeps the bound's R, c, scale
 // and post for the soundness tests.
-std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
+std::string weak_cull_expr(const DevObject& o, const WeakBound& w, const std::string& thr = "bd") {
     std::ostringstream os;
     const std::string d =
         "p - V{" + fbits(o.pos[0]) + ", " + fbits(o.pos[1]) + ", " + fbits(o.pos[2]) + "}";
@@ -383,11 +463,11 @@ std::string weak_cull_expr(const DevObject& o, const WeakBound& w) {
     const double A = (double)w.post + (double)w.R * (double)o.scale * ((double)w.c + eps);
     const float Af = float_at_or_above(A), Bf = float_at_or_above((1.0 + 1.0 / 131072.0) / K);
     if (K > 0.0 && A > 0.0 && std::isfinite(Af) && std::isfinite(Bf)) {
-        os << "weak_beyond_sq(" << local << ", " << fbits(Af) << ", " << fbits(Bf) << ", bd) /* weak bound R c scale post: "
+        os << "weak_beyond_sq(" << local << ", " << fbits(Af) << ", " << fbits(Bf) << ", " << thr << ") /* weak bound R c scale post: "
            << fbits(w.R) << " " << fbits(w.c) << " " << fbits(o.scale) << " " << fbits(w.post) << " */";
     } else {
         os << "weak_beyond(" << local << ", " << fbits(w.R) << ", " << fbits(w.c) << ", " << fbits(o.scale) << ", "
-           << fbits(w.post) << ", bd)";
+           << fbits(w.post) << ", " << thr << ")";
     }
     return os.str();
 }
@@ -544,6 +624,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
     for (uint32_t s = 0; s < h->n_segments; ++s)
         if (walk[s]) os << walk_fn(s, seg[s], node, h->n_nodes, unb, h->slack, s > 0);
     const std::string slack = fbits(h->slack);
+    const bool weak_extra = h->n_objects <= kWeakExtraObjects;
+    const DevCsgOp* weak_csg = weak_extra ? csg : nullptr;  // CSG objects get weak bounds only then
     // pre-tests against fmaxf(x, slack) need no sign test of the threshold when slack > 0
     const bool slack_pos = h->slack > 0.0f;
     const std::string fb_pos = slack_pos ? "far_beyond_pos" : "far_beyond";
@@ -585,6 +667,19 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                     os << "        if (!(" << keep << " && " << fb_pos << "(length_sq_fma(p - V{" << fbits(o.bc[0]) << ", "
                        << fbits(o.bc[1]) << ", " << fbits(o.bc[2]) << "}), " << thr2 << ", " << fbits(o.br) << "))) {\n";
             }
+            // An unbounded object with a weak bound (bend, repeat; CSG programs) skips the same way
+            // where that bound clears the threshold: no bound substitute stands in for its field,
+            // so the threshold is the accumulator's alone.
+            const bool weak_skip = weak_extra && seeded && !(o.flags & OF_BOUND) && sg.b <= 2u;
+            const WeakBound owb = weak_skip ? weak_bound(o, weak_csg, h->n_csg_ops) : WeakBound{};
+            if (owb.ok) {
+                const std::string thr = smooth      ? "__fadd_ru(acc.d, " + fbits(o.k) + ")"
+                                        : sg.b == 2u ? std::string("-acc.d")
+                                                     : std::string("acc.d");
+                if (!(o.flags & OF_ROT_IDENTITY)) os << "        const float RO[9] = " << farr(o.rot, 9) << ";\n";
+                os << "        if (!(fabsf(acc.d) < INF" << (smooth ? " && acc.d != 0.0f" : "") << " && "
+                   << weak_cull_expr(o, owb, thr) << ")) {  // weak skip\n";
+            }
             os << "        Field f;\n        bool sub = false;\n";
             if (o.flags & OF_BOUND)
                 os << "        {\n            float lower = " << lower_expr(o) << ";\n"
@@ -602,7 +697,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             };
             if (comb_exact == sg.b) os << "        " << fold(sg.b) << "\n";
             else os << "        if (sub) { " << fold(sg.b) << " } else { " << fold(comb_exact) << " }\n";
-            if (skip) os << "        }\n";
+            if (skip || owb.ok) os << "        }\n";
         } else if (sg.kind == SEG_LINEAR) {
             // The fold is an argmin with lowest-index ties (the seed, index -1, wins its ties), and
             // a culled member cannot reach the minimum, so any member order gives the same
@@ -636,7 +731,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 os << "        {  // member " << i << "\n";
                 // members the exact sphere test never culls (the reference's unbounded members, and
                 // the non-conservative ones) skip their exact field where their weak bound clears bd
-                const WeakBound wb = cull ? WeakBound{} : weak_bound(o);
+                const WeakBound wb = cull ? WeakBound{} : weak_bound(o, weak_csg, h->n_csg_ops);
                 if (wb.ok) {
                     if (!(o.flags & OF_ROT_IDENTITY)) os << "            const float RO[9] = " << farr(o.rot, 9) << ";\n";
                     exact = "if (!" + weak_cull_expr(o, wb) + ") {\n            " + exact + "            }\n";
@@ -669,7 +764,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 uint32_t i = unb[sg.a + k];
                 bool cull = (obj[i].flags & OF_BOUND) && !(obj[i].flags & OF_NONCONS);
                 if (cull) cullable.push_back(i);
-                else if (weak_bound(obj[i]).ok) weak.push_back(i);
+                else if (weak_bound(obj[i], weak_csg, h->n_csg_ops).ok) weak.push_back(i);
                 else member(i, false);
             }
             std::vector<MemberCluster> clusters;

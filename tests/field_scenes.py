@@ -131,3 +131,36 @@ def planes_scene(width=64, height=36):
     ]
     cam = look_at((0.0, 2.0, -9.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), radians(60.0))
     return s, cam
+
+
+def unbounded_mix_scene(seed, width=64, height=36):
+    """Objects the reference leaves unbounded (bend, repeat) as smooth-union and subtracted
+    segments and as union members, CSG objects among them, after bounded ones on a plane: the
+    specialised field skips their exact fields where their weak bounds clear the threshold."""
+    from mm3e_cuda.scene import Expr
+
+    rng = np.random.default_rng(seed)
+    s = Scene(width, height)
+    s.materials = [Material((0.8, 0.8, 0.8)), Material((0.7, 0.3, 0.2)), Material((0.2, 0.5, 0.7))]
+    s.objects = [Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, 0)]
+    for k in range(14):
+        pos = tuple(float(v) for v in rng.uniform([-4, 0.5, -3], [4, 2.0, 3]))
+        rot = mat3_from_euler(*rng.uniform(-1.2, 1.2, 3))
+        if k % 3 == 0:
+            e = Expr.union(Expr.sphere(float(rng.uniform(0.2, 0.5))),
+                           Expr.transform(Expr.box(tuple(float(v) for v in rng.uniform(0.15, 0.4, 3))),
+                                          Transform(tuple(float(v) for v in rng.uniform(-0.3, 0.3, 3)), rot, 0.9)))
+            prim = Prim.csg(s.csg(e))
+        elif k % 3 == 1:
+            prim = Prim.cone(float(rng.uniform(0.3, 0.6)), float(rng.uniform(0.05, 0.2)), float(rng.uniform(0.6, 1.2)))
+        else:
+            prim = Prim.box(tuple(float(v) for v in rng.uniform(0.2, 0.5, 3)))
+        o = Object(prim, Transform(pos, rot, float(rng.uniform(0.8, 1.2))), 1 + k % 2)
+        o = o.bend(float(rng.uniform(-0.4, 0.4))) if k % 2 == 0 else o.repeat((float(rng.uniform(3.0, 5.0)), 0.0, 0.0))
+        if k % 4 == 1:
+            o = o.smooth(float(rng.uniform(0.1, 0.4)))
+        elif k % 4 == 3:
+            o = o.subtract()
+        s.objects.append(o)
+    cam = look_at((0.0, 3.0, -9.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0), radians(55.0))
+    return s, cam

@@ -15,7 +15,7 @@ import mm3e_cuda
 import oracle_py
 from mm3e_cuda import abi, scenes
 from mm3e_cuda.scene import DynSphere, GiVolume
-from field_scenes import csg_zoo_scene, noncons_scene, smooth_chain_scene
+from field_scenes import csg_zoo_scene, noncons_scene, smooth_chain_scene, unbounded_mix_scene
 from parity import hit_metrics, image_metrics
 
 pytestmark = pytest.mark.gpu
@@ -271,6 +271,19 @@ def test_csg_zoo_scene_parity(gpu_ctx, seed):
     compiled.specialize(compiled.SPEC_ALWAYS)
     _check_image("csg_zoo_spec", compiled.render(cam, fmt=abi.FB_RGBA8), ref)
     _check_hits("csg_zoo_spec", compiled, scene, cam)
+
+
+def test_unbounded_mix_scene_parity(gpu_ctx):
+    """Bent and repeated objects (unbounded in the reference) as smooth-union, subtracted and union
+    members, CSG objects among them: the interpreter and the specialised field, whose weak bounds
+    skip their exact fields, both against the oracle."""
+    scene, cam = unbounded_mix_scene(4, 160, 90)
+    compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image("unbounded_mix", gpu, ref)
+    _check_hits("unbounded_mix", compiled, scene, cam)
+    compiled.specialize(compiled.SPEC_ALWAYS)
+    _check_image("unbounded_mix_spec", compiled.render(cam, fmt=abi.FB_RGBA8), ref)
+    _check_hits("unbounded_mix_spec", compiled, scene, cam)
 
 
 def _mirror_scene(bounces, shadows=True):

@@ -9,7 +9,7 @@ import pytest
 
 import mm3e_cuda
 from mm3e_cuda import abi, scenes
-from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene
+from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene, unbounded_mix_scene
 from mm3e_cuda.scene import DynSphere
 
 pytestmark = pytest.mark.gpu
@@ -28,6 +28,7 @@ SCENES = {
     "csg_zoo3": lambda: csg_zoo_scene(3, 160, 90),
     "procedural9": lambda: scenes.procedural_scene(9, 128, 72),
     "planes": lambda: planes_scene(160, 90),
+    "unbounded_mix": lambda: unbounded_mix_scene(4, 160, 90),
 }
 
 

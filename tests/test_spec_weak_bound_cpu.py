@@ -17,7 +17,7 @@ import pytest
 
 import mm3e_cuda
 import oracle_py
-from mm3e_cuda.scene import IDENTITY_ROT, Material, Object, Prim, Scene, Transform, mat3_from_euler
+from mm3e_cuda.scene import IDENTITY_ROT, Expr, Material, Object, Prim, Scene, Transform, mat3_from_euler
 
 F = np.float32
 
@@ -43,6 +43,8 @@ MODS = {
 }
 
 _HEX = r"__uint_as_float\(0x([0-9a-f]+)u\)"
+# the threshold of a weak test: bd in a union run; the accumulator's in a skippable one-object segment
+_THR = r"(?:bd|-acc\.d|acc\.d|__fadd_ru\(acc\.d, __uint_as_float\(0x[0-9a-f]+u\)\))"
 
 
 def _f(h):
@@ -69,14 +71,14 @@ def _weak_constants(src):
         rot = None
         local = r"p - V\{" + _HEX + ", " + _HEX + ", " + _HEX + r"\}"
     head = r"\(scale\(" + local + ", " + _HEX + r"\), (true|false), (true|false), (true|false), "
-    sq = re.search(r"weak_beyond_sq" + head + _HEX + ", " + _HEX + r", bd\) /\* weak bound R c scale post: " +
+    sq = re.search(r"weak_beyond_sq" + head + _HEX + ", " + _HEX + ", " + _THR + r"\) /\* weak bound R c scale post: " +
                    " ".join([_HEX] * 4), src)
     if sq:
         g = sq.groups()
         consts = (_f(g[9]), _f(g[10]), _f(g[11]), _f(g[12]))
         ab = (_f(g[7]), _f(g[8]))
     else:
-        call = re.search(r"weak_beyond" + head + ", ".join([_HEX] * 4) + r", bd\)", src)
+        call = re.search(r"weak_beyond" + head + ", ".join([_HEX] * 4) + ", " + _THR + r"\)", src)
         assert call, "no weak-bound cull emitted"
         g = call.groups()
         consts = tuple(_f(x) for x in g[7:11])
@@ -140,12 +142,19 @@ def test_weak_bound_holds(prim, mod, rotated):
         assert not weak  # the exact sphere test covers it
         return
     assert weak
+    _check_bound(src, lambda: _scene(obj, False), rng)
+
+
+def _check_bound(src, field_scene, rng, centre=(0.4, 1.2, -0.6)):
+    """The weak test's constants in `src` against the oracle's field of `field_scene()` (the object
+    alone) on points all around `centre`: the bound never exceeds the field, it is not vacuous,
+    and the square-root-free form culls only where the plain bound clears the threshold."""
     *consts, ab = _weak_constants(src)
     d = rng.standard_normal((40000, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     r = rng.uniform(0.0, 6.0, 40000) ** 1.5
-    pts = (np.array([0.4, 1.2, -0.6]) + d * r[:, None]).astype(F)
-    field, _ = oracle_py.field(_scene(obj, False).desc(), pts)
+    pts = (np.array(centre) + d * r[:, None]).astype(F)
+    field, _ = oracle_py.field(field_scene().desc(), pts)
     lb = _bound(pts, *consts)
     live = lb >= 0
     assert live.mean() > 0.2  # the bound is not vacuous
@@ -169,3 +178,69 @@ def test_weak_bound_holds(prim, mod, rotated):
         assert not (sq & ~(field > bd)).any()
     bd = (lb * F(0.98)).astype(F)
     assert (n2 > F(F(F(bd + A) * B) ** 2))[lb > 0.1].mean() > 0.5  # and it still culls
+
+
+CSG_EXPRS = {
+    "union_transform": lambda: Expr.union(Expr.sphere(0.5), Expr.transform(
+        Expr.box((0.3, 0.6, 0.2)), Transform((0.4, 0.1, 0.0), mat3_from_euler(0.3, 0.2, 0.1), 0.8))),
+    "smooth_shell": lambda: Expr.shell(Expr.smooth_union(Expr.torus(0.5, 0.15),
+                                                         Expr.capsule((0, -0.4, 0), (0, 0.4, 0), 0.2), 0.3), 0.05),
+    "intersect_offset": lambda: Expr.offset(Expr.intersect(Expr.box((0.6, 0.6, 0.6)), Expr.sphere(0.75)), 0.05),
+    "subtract_scaled": lambda: Expr.subtract(Expr.transform(Expr.cylinder(0.5, 0.4), Transform((0.0, 0.0, 0.2),
+                                                                                             IDENTITY_ROT, 1.3)),
+                                             Expr.sphere(0.3)),
+    "ellipsoid_octahedron": lambda: Expr.union(Expr.ellipsoid((0.5, 0.3, 0.4)), Expr.octahedron(0.5)),
+    "negative_offset_cone": lambda: Expr.offset(Expr.cone(0.6, 0.2, 1.2), -0.1),
+}
+
+
+def _csg_scene(expr, mod, lead=None, combine=None):
+    s = Scene(32, 32)
+    s.materials = [Material((0.8, 0.8, 0.8))]
+    obj = MODS[mod](Object(Prim.csg(s.csg(expr)), Transform((0.4, 1.2, -0.6), mat3_from_euler(0.2, -0.5, 0.9), 1.1), 0))
+    if combine == "smooth":
+        obj = obj.smooth(0.3)
+    elif combine == "subtract":
+        obj = obj.subtract()
+    s.objects = ([lead] if lead is not None else []) + [obj]
+    return s
+
+
+@pytest.mark.parametrize("mod", ["bend", "repeat_x", "onion_bend"])
+@pytest.mark.parametrize("expr", list(CSG_EXPRS))
+def test_csg_weak_bound_holds(expr, mod):
+    """A CSG object that the reference leaves unbounded (bend, repeat) gets a weak bound from its
+    program's parts (csg_weak in spec.cpp); the bound holds against the oracle's field."""
+    rng = np.random.default_rng(abs(hash((expr, mod))) % (1 << 32))
+    anchor = Object(Prim.sphere(0.1), Transform((40.0, 40.0, 40.0)), 0)
+    s = _csg_scene(CSG_EXPRS[expr](), mod)
+    s.objects.append(anchor)
+    src = mm3e_cuda.spec_source(s)
+    assert "weak_beyond" in src
+    _check_bound(src, lambda: _csg_scene(CSG_EXPRS[expr](), mod), rng)
+
+
+@pytest.mark.parametrize("combine", ["smooth", "subtract"])
+@pytest.mark.parametrize("shape", ["bent_cone", "csg"])
+def test_unbounded_one_object_segment_weak_skip(shape, combine):
+    """An unbounded smooth-union or subtracted object (its own segment, after the accumulator of
+    the objects before it) skips its exact field where its weak bound clears the accumulator's
+    threshold; the bound holds against the oracle's field."""
+    rng = np.random.default_rng(7 if shape == "csg" else 8)
+    lead = Object(Prim.sphere(0.5), Transform((6.0, 0.5, 0.0)), 0)
+    if shape == "csg":
+        make = lambda with_lead: _csg_scene(CSG_EXPRS["union_transform"](), "bend", lead if with_lead else None,
+                                            combine if with_lead else None)
+    else:
+        def make(with_lead):
+            s = Scene(32, 32)
+            s.materials = [Material((0.8, 0.8, 0.8))]
+            o = Object(Prim.cone(0.6, 0.2, 1.2), Transform((0.4, 1.2, -0.6), mat3_from_euler(0.2, -0.5, 0.9), 1.1),
+                       0).bend(-0.36)
+            if with_lead:
+                o = o.smooth(0.3) if combine == "smooth" else o.subtract()
+            s.objects = ([lead] if with_lead else []) + [o]
+            return s
+    src = mm3e_cuda.spec_source(make(True))
+    assert "// weak skip" in src
+    _check_bound(src, lambda: make(False), rng)
