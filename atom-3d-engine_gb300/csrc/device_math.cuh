@@ -332,6 +332,28 @@ static __device__ __noinline__ float csg_eval(const DevCsgOp* op, V p) {
     return vs > 0 ? vals[0] : __int_as_float(0x7f800000);
 }
 
+// sin and cos of a twist or bend angle. A scene-specialised program of a large field defines
+// MM3E_SHARED_SINCOS: its objects then share one out-of-line copy of sincosf (a leaf call with
+// no stack use) instead of one inlined copy per twisted or bent object, which keeps the field's
+// code within the instruction cache. The values are sincosf's either way.
+#if defined(MM3E_SHARED_SINCOS)
+struct SinCos {
+    float s, c;
+};
+static __device__ __noinline__ SinCos sincos_shared(float a) {
+    SinCos r;
+    sincosf(a, &r.s, &r.c);
+    return r;
+}
+MD void angle_sincos(float a, float& s, float& c) {
+    const SinCos r = sincos_shared(a);
+    s = r.s;
+    c = r.c;
+}
+#else
+MD void angle_sincos(float a, float& s, float& c) { sincosf(a, &s, &c); }
+#endif
+
 // Object::local_point (lib.rs:400-419)
 MD V local_point(const DevObject& o, V p) {
     const V d = p - ld3(o.pos);
@@ -354,13 +376,13 @@ MD V local_point(const DevObject& o, V p) {
         if (f & OF_TWIST) {
             float a = o.twist * l.y;
             float s, c;
-            sincosf(a, &s, &c);
+            angle_sincos(a, s, c);
             l = V{c * l.x - s * l.z, l.y, s * l.x + c * l.z};
         }
         if (f & OF_BEND) {
             float a = o.bend * l.x;
             float s, c;
-            sincosf(a, &s, &c);
+            angle_sincos(a, s, c);
             l = V{c * l.x - s * l.y, s * l.x + c * l.y, l.z};
         }
     }

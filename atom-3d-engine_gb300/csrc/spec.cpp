@@ -106,6 +106,12 @@ std::string object_rec(const DevObject& o) {
     return os.str();
 }
 
+// Fields of more objects than this, or with CSG programs, share one out-of-line sincosf for
+// their twists and bends (MM3E_SHARED_SINCOS in device_math.cuh). Measured: the 16 seeded C4
+// scenes' specialised frames 3.23x faster than the interpreter (time-weighted) with it, 2.84x
+// without; the gallery (15 objects, whose march is not fetch-bound) 3.6% slower with it.
+constexpr uint32_t kSharedSincosObjects = 16;
+
 // Fields of more objects than this take no weak bound for CSG objects and no weak skip of
 // unbounded one-object segments: their tests run at every sample, and in a field that large the
 // code they add costs more in instruction fetch than the exact evaluations they save.
@@ -589,7 +595,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
     os << "// scene-specialised world field (generated)\n"
           "typedef unsigned int uint32_t;\ntypedef int int32_t;\ntypedef unsigned long long uint64_t;\n"
           "typedef unsigned short uint16_t;\ntypedef unsigned char uint8_t;\ntypedef long long int64_t;\n"
-          "#include \"march_kernels.cuh\"\n"
+       << (h->n_objects > kSharedSincosObjects || h->n_csg_ops > 0 ? "#define MM3E_SHARED_SINCOS 1\n" : "")
+       << "#include \"march_kernels.cuh\"\n"
           "namespace mm3e {\nnamespace spec {\n";
     const DevNode* node = reinterpret_cast<const DevNode*>(blob.data() + h->off_nodes);
     // segments that need the BVH walk: big runs, and LINEAR runs with a non-conservative member
