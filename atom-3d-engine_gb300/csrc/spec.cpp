@@ -107,9 +107,10 @@ std::string object_rec(const DevObject& o) {
 }
 
 // Fields of more objects than this, or with CSG programs, share one out-of-line sincosf for
-// their twists and bends (MM3E_SHARED_SINCOS in device_math.cuh). Measured: the 16 seeded C4
-// scenes' specialised frames 3.23x faster than the interpreter (time-weighted) with it, 2.84x
-// without; the gallery (15 objects, whose march is not fetch-bound) 3.6% slower with it.
+// their twists and bends (MM3E_SHARED_SINCOS in device_math.cuh). Measured: the specialised
+// frames of 16 seeded procedural scenes (8-64 primitives, CSG trees, domain ops; 256^2 to 1080p)
+// 3.23x faster than the interpreter's (time-weighted) with it, 2.84x without; the feature gallery
+// (15 objects, whose march is not fetch-bound) 3.6% slower with it.
 constexpr uint32_t kSharedSincosObjects = 16;
 
 // Fields of more objects than this take no weak bound for CSG objects and no weak skip of
@@ -840,8 +841,8 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
     // the shadow kernel 64 registers with spills.)
     // The shadow kernel of a small field (at most 16 objects, no CSG program) asks for 10 CTAs of
     // 128 (5 of 256), 48 registers: the gallery's fits without spills and its shadow pass took
-    // 0.648 against 0.681 ms per 1080p frame. The fields of larger scenes (the C4 procedural
-    // scenes) mostly need fewer registers anyway, and some of them spill at 48.
+    // 0.648 against 0.681 ms per 1080p frame. The fields of larger scenes (the seeded procedural
+    // scenes of 8-64 primitives) mostly need fewer registers anyway, and some of them spill at 48.
     const bool small_field = h->n_objects <= 16 && h->n_csg_ops == 0;
     const uint32_t mb = min_blocks ? min_blocks : (block <= 128 ? 8u : 4u);
     const uint32_t mb_shadow = min_blocks ? min_blocks : small_field ? (block <= 128 ? 10u : 5u) : (block <= 128 ? 8u : 4u);

@@ -1,7 +1,7 @@
 """The CPU oracle against the reference's own known answers and shipped renders.
 
 Each test restates a check from the reference's test suite (file:line in the MM3E repository)
-against the oracle, so the oracle is pinned before it judges the CUDA path.
+against the oracle, so the oracle is pinned before it checks the CUDA path.
 """
 import math
 import os
