@@ -559,6 +559,26 @@ void cluster_members(const DevObject* obj, std::vector<uint32_t> m, std::vector<
     cluster_members(obj, std::vector<uint32_t>(m.begin() + half, m.end()), out);
 }
 
+// A sphere enclosing the given spheres: |c - c_i| + r_i <= r for each of them in exact
+// arithmetic with a relative margin of 2^-20 (the same rule as the clusters' spheres).
+bool enclosing_sphere(const std::vector<std::pair<const float*, float>>& spheres, float* c, float& r) {
+    double mean[3] = {0.0, 0.0, 0.0};
+    for (const auto& sp : spheres)
+        for (int a = 0; a < 3; ++a) mean[a] += sp.first[a];
+    for (int a = 0; a < 3; ++a) c[a] = (float)(mean[a] / (double)spheres.size());
+    double rr = 0.0;
+    for (const auto& sp : spheres) {
+        if (!(sp.second >= 0.0f) || !std::isfinite(sp.second)) return false;
+        double dx = (double)sp.first[0] - c[0], dy = (double)sp.first[1] - c[1], dz = (double)sp.first[2] - c[2];
+        rr = std::max(rr, std::sqrt(dx * dx + dy * dy + dz * dz) + (double)sp.second);
+    }
+    rr = rr * (1.0 + 1.0 / 1048576.0) + 1e-30;
+    float rf = (float)rr;
+    if ((double)rf < rr) rf = std::nextafter(rf, INFINITY);
+    r = rf;
+    return std::isfinite(r) && std::isfinite(c[0]) && std::isfinite(c[1]) && std::isfinite(c[2]);
+}
+
 }  // namespace
 
 std::string nvrtc_status() { return nvrtc().status; }
@@ -777,6 +797,23 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             }
             std::vector<MemberCluster> clusters;
             cluster_members(obj, cullable, clusters);
+            // The clusters and the bounded weak members (whose sphere tests take fmaxf(bd, slack))
+            // under one enclosing sphere when there are three or more: where a sample is beyond
+            // it, every test inside would cull. Its threshold is fmaxf(bd, slack) when a bounded
+            // weak member is inside (no smaller than bd, so it covers the clusters too).
+            std::vector<uint32_t> weak_bounded, weak_free;
+            for (uint32_t i : weak) ((obj[i].flags & OF_BOUND) ? weak_bounded : weak_free).push_back(i);
+            std::vector<std::pair<const float*, float>> spheres;
+            for (const MemberCluster& cl : clusters) spheres.push_back({cl.c, cl.r});
+            for (uint32_t i : weak_bounded) spheres.push_back({obj[i].bc, obj[i].br});
+            float sc[3];
+            float sr = 0.0f;
+            const bool super = spheres.size() >= 3 && enclosing_sphere(spheres, sc, sr);
+            if (super) {
+                const std::string thr = weak_bounded.empty() ? std::string("bd") : "fmaxf(bd, " + slack + ")";
+                os << "        if (!" << sphere_test(sc, sr, thr, !weak_bounded.empty() && slack_pos)
+                   << ") {  // enclosing sphere of " << spheres.size() << " tests, radius " << fbits(sr) << "\n";
+            }
             for (const MemberCluster& cl : clusters) {
                 if (cl.members.size() > 1)
                     os << "        if (!" << sphere_test(cl.c, cl.r, "bd", false) << ") {  // cluster of " << cl.members.size()
@@ -784,7 +821,9 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
                 for (uint32_t i : cl.members) member(i, true);
                 if (cl.members.size() > 1) os << "        }  // end of cluster\n";
             }
-            for (uint32_t i : weak) member(i, false);
+            for (uint32_t i : weak_bounded) member(i, false);
+            if (super) os << "        }  // end of enclosing sphere\n";
+            for (uint32_t i : weak_free) member(i, false);
             if (any_noncons)
                 os << "        if (bnc) acc = walk_" << s << "(T, p, acc);\n        else acc = Field{bd, bm};\n";
             else

@@ -336,3 +336,35 @@ def test_linearised_pretest_implies_exact_cull():
             far = _points_near(rng, c, (float(bd) + float(r)) * 1.02, 50)
             assert all(far_beyond_lin_exact(q, c, r, bd) for q in far)
     assert not far_beyond_lin_exact(np.array([1e3, 0, 0], F), np.zeros(3, F), F(1.0), F(-0.5))
+
+
+def test_enclosing_sphere_covers_every_test_inside():
+    """The enclosing sphere over a union run's sphere tests (spec.cpp enclosing_sphere) contains
+    every cluster sphere and every member bound sphere inside its block, in exact arithmetic, so
+    a sample beyond it would be culled by each of them."""
+    hexf = lambda h: np.array([int(h, 16)], np.uint32).view(F)[0]
+    H = r"__uint_as_float\(0x(\w+)u\)"
+    n_super = 0
+    for src in (mm3e_cuda.spec_source(scenes.gallery_scene(64, 36)[0]),):
+        inside = None
+        for line in src.splitlines():
+            m = re.search(r"dist2_below\(p, CB, " + H + ", " + H + ", " + H + r".*// enclosing sphere of \d+ tests, radius " + H, line)
+            if m:
+                inside = (np.array([hexf(m.group(i)) for i in (1, 2, 3)], F) * F(-0.5), hexf(m.group(4)), [])
+                n_super += 1
+                continue
+            if inside is None:
+                continue
+            m = re.search(r"dist2_below\(p, CB, " + H + ", " + H + ", " + H + r".*// cluster of \d+, radius " + H, line)
+            if m:
+                inside[2].append((np.array([hexf(m.group(i)) for i in (1, 2, 3)], F) * F(-0.5), hexf(m.group(4))))
+            m = re.search(r"length\(p - V\{" + H + ", " + H + ", " + H + r"\}\) - " + H, line)
+            if m:
+                inside[2].append((np.array([hexf(m.group(i)) for i in (1, 2, 3)], F), hexf(m.group(4))))
+            if "// end of enclosing sphere" in line:
+                C, R, parts = inside
+                assert len(parts) >= 3
+                for c, r in parts:
+                    assert _exact_norm_le(C.astype(np.float64) - c.astype(np.float64), Fraction(float(R)) - Fraction(float(r)))
+                inside = None
+    assert n_super >= 1
