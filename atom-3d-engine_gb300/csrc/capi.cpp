@@ -518,6 +518,17 @@ int mm3e_scene_tape_bytes(const mm3e_scene_desc* desc, size_t* out_bytes) {
     return MM3E_OK;
 }
 
+int mm3e_scene_tape(const mm3e_scene_desc* desc, void* out, size_t cap, size_t* len) {
+    if (!desc) return MM3E_ERR_INVALID;
+    std::string msg;
+    LoweredScene low;
+    int rc = lower_scene(*desc, nullptr, 0, low, msg);
+    if (rc) return rc;
+    if (len) *len = low.blob.size();
+    if (out && cap) std::memcpy(out, low.blob.data(), low.blob.size() < cap ? low.blob.size() : cap);
+    return MM3E_OK;
+}
+
 int mm3e_ctx_create(int device, mm3e_ctx** out) {
     if (!out) return MM3E_ERR_INVALID;
     *out = nullptr;

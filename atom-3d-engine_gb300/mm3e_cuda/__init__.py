@@ -400,6 +400,20 @@ def spec_source(scene):
     return buf.value.decode()
 
 
+def scene_tape(scene):
+    """The lowered scene tape (host only): the bytes the device holds for the scene."""
+    h = scene.desc()
+    n = C.c_size_t()
+    rc = lib().mm3e_scene_tape(h.ptr, None, 0, C.byref(n))
+    if rc != abi.OK:
+        raise RenderError(rc, "scene tape")
+    buf = C.create_string_buffer(n.value)
+    rc = lib().mm3e_scene_tape(h.ptr, buf, n.value, C.byref(n))
+    if rc != abi.OK:
+        raise RenderError(rc, "scene tape")
+    return buf.raw[:n.value]
+
+
 def spec_compile_check(scene):
     """NVRTC compile of the scene's specialised program (host only): (ok, message, ms)."""
     h = scene.desc()

@@ -165,7 +165,7 @@ EXPORTED_SYMBOLS = [
     "mm3e_scene_device_bytes", "mm3e_batch_configure", "mm3e_render_batch", "mm3e_autotune",
     "mm3e_scene_parse_mm3e", "mm3e_parsed_scene_desc", "mm3e_parsed_scene_camera", "mm3e_parsed_scene_free",
     "mm3e_scene_write_mm3e", "mm3e_ctx_set_host_writes", "mm3e_ctx_set_tape_wait", "mm3e_scene_autotune", "mm3e_volume_parse_sdfv", "mm3e_volume_write_sdfv",
-    "mm3e_bake_mesh_sdf", "mm3e_render_film", "mm3e_render_gbuffer", "mm3e_reproject", "mm3e_scene_specialize", "mm3e_scene_is_specialized", "mm3e_scene_spec_source", "mm3e_spec_compile_check",
+    "mm3e_bake_mesh_sdf", "mm3e_render_film", "mm3e_render_gbuffer", "mm3e_reproject", "mm3e_scene_specialize", "mm3e_scene_is_specialized", "mm3e_scene_spec_source", "mm3e_spec_compile_check", "mm3e_scene_tape",
     "mm3e_server_create", "mm3e_server_add_scene", "mm3e_server_submit", "mm3e_server_wait", "mm3e_server_get_stats",
     "mm3e_server_replay", "mm3e_server_destroy",
 ]

@@ -85,6 +85,7 @@ def _declare_extra(lib):
         "mm3e_scene_specialize": (C.c_int, [C.c_void_p, C.c_int, P(C.c_double)]),
         "mm3e_scene_is_specialized": (C.c_int, [C.c_void_p]),
         "mm3e_scene_spec_source": (C.c_int, [P(abi.SceneDesc), C.c_char_p, C.c_size_t, P(C.c_size_t)]),
+        "mm3e_scene_tape": (C.c_int, [P(abi.SceneDesc), C.c_void_p, C.c_size_t, P(C.c_size_t)]),
         "mm3e_spec_compile_check": (C.c_int, [P(abi.SceneDesc), C.c_char_p, C.c_size_t, P(C.c_double)]),
         "mm3e_render_film": (C.c_int, [C.c_void_p, P(abi.Camera), C.c_float, C.c_float, P(C.c_float), P(C.c_float),
                                        P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_uint32)]),

@@ -284,6 +284,10 @@ void mm3e_light_directional(const float toward[3], const float color[3], mm3e_li
 int mm3e_scene_validate(const mm3e_scene_desc* desc, char* err, size_t err_len);
 /* Size in bytes of the lowered scene tape (host-side lowering, no device). */
 int mm3e_scene_tape_bytes(const mm3e_scene_desc* desc, size_t* out_bytes);
+/* The lowered scene tape itself (the bytes the device holds; host-side, no device): `len`
+ * receives its size; up to `cap` bytes are copied to `out` (which may be NULL). For tools and
+ * tests that evaluate the field on the host. */
+int mm3e_scene_tape(const mm3e_scene_desc* desc, void* out, size_t cap, size_t* len);
 
 /* ---- `.mm3e` text scenes (mm3e-orchestrator/src/scene_io.rs) -------------------------------- */
 /* Parses a `.mm3e` document (scene_io::parse, scene_io.rs:196-281) into an owned scene

@@ -1,0 +1,105 @@
+"""Scene-specialised fields against the tape interpreter, on the host.
+
+The specialised program (spec.cpp's generated field: inlined objects, generated CSG programs,
+axis planes, linearised and enclosing-sphere pre-tests, weak bounds and skips) and the
+interpreter's world_eval (WorldPlan::eval, accel.rs:209-252) compile as plain C++ with the host
+definitions of the device intrinsics in tests/host_field/host_shim.h. Both are evaluated on the
+same binary32 points over the scene's lowered tape (mm3e_scene_tape), and their (distance,
+material) pairs must agree bit for bit. This covers many seeded scenes without a GPU; the GPU
+tests check the same identity on the device (test_gpu_spec.py)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import mm3e_cuda
+from mm3e_cuda import scenes
+from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene, unbounded_mix_scene
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "atom-3d-engine_gb300", "csrc")
+SHIM = os.path.join(ROOT, "tests", "host_field", "host_shim.h")
+CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+
+MAIN = r"""
+#include <cstdio>
+#include <vector>
+namespace mm3e { namespace spec {
+#include "field.inc"
+}}
+using namespace mm3e;
+int main(int argc, char** argv) {
+    FILE* ft = std::fopen(argv[1], "rb");
+    std::vector<float4> tape_words(1 << 20);
+    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
+    std::fclose(ft);
+    (void)nt;
+    const Tape T = tape_view(reinterpret_cast<const unsigned char*>(tape_words.data()));
+    FILE* fp = std::fopen(argv[2], "rb");
+    std::vector<float> pts(3 << 20);
+    size_t n = std::fread(pts.data(), sizeof(float), pts.size(), fp) / 3;
+    std::fclose(fp);
+    size_t bad = 0;
+    for (size_t k = 0; k < n; ++k) {
+        V p{pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]};
+        Field a = spec::eval(T, p), b = world_eval(T, p);
+        if (__float_as_uint(a.d) != __float_as_uint(b.d) || a.m != b.m) {
+            if (bad < 5) std::printf("mismatch at (%.9g, %.9g, %.9g): %.9g/%u vs %.9g/%u\n", p.x, p.y, p.z, a.d, a.m, b.d, b.m);
+            bad += 1;
+        }
+    }
+    std::printf("points %zu mismatches %zu\n", n, bad);
+    return bad ? 1 : 0;
+}
+"""
+
+SCENES = {
+    "gallery": lambda: scenes.gallery_scene(64, 36),
+    "spheres": lambda: scenes.spheres_scene(64, 36),
+    "cornell": lambda: scenes.cornell_scene(64, 36),
+    "planes": lambda: planes_scene(64, 36),
+    "noncons": lambda: noncons_scene(21, 64, 36),
+    "smooth_chain": lambda: smooth_chain_scene(5, 64, 36),
+    "csg_zoo": lambda: csg_zoo_scene(2, 64, 36),
+    "unbounded_mix": lambda: unbounded_mix_scene(4, 64, 36),
+    **{f"procedural{k}": (lambda k=k: scenes.procedural_scene(k, 64, 36)) for k in (0, 3, 5, 8, 11, 12)},
+}
+
+
+def _points(scene, cam, rng, n=6000):
+    """Points along the camera's rays at random distances, and points in a box around the scene:
+    near surfaces, inside objects and far away."""
+    eye = np.array(cam.eye, np.float64)
+    fwd, right, up = (np.array(v, np.float64) for v in (cam.forward, cam.right, cam.up))
+    sx, sy = rng.uniform(-1, 1, n // 2), rng.uniform(-1, 1, n // 2)
+    d = fwd + np.outer(sx * cam.fov_scale * 1.7, right) + np.outer(sy * cam.fov_scale, up)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    t = rng.uniform(0, 25, n // 2) ** 1.0
+    on_rays = eye + d * t[:, None]
+    box = rng.uniform([-8, -2, -8], [8, 6, 8], (n - n // 2, 3))
+    return np.concatenate([on_rays, box]).astype(np.float32)
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_specialised_field_equals_interpreter_on_host(name, tmp_path):
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, cam = SCENES[name]()
+    src = mm3e_cuda.spec_source(scene)
+    body = src[src.index("namespace spec {") + len("namespace spec {"):src.index("struct Field_")]
+    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+    (tmp_path / "field.inc").write_text(body)
+    (tmp_path / "main.cpp").write_text(defines + '#include "device_math.cuh"\n' + MAIN)
+    exe = tmp_path / "field_check"
+    cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE, "-I", CSRC,
+           "-I", str(tmp_path), "-include", SHIM, str(tmp_path / "main.cpp"), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    _points(scene, cam, np.random.default_rng(abs(hash(name)) % (1 << 32))).tofile(tmp_path / "points.bin")
+    r = subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "points.bin")], capture_output=True,
+                       text=True)
+    print(name, r.stdout.strip().splitlines()[-1] if r.stdout.strip() else r.stderr[-500:])
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
