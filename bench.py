@@ -758,6 +758,9 @@ def run_ours(args):
         if dom_s:
             roofline["achieved"] = phase["fp32"] / dom_s / 1e12
             roofline["frac"] = roofline["achieved"] / peak
+            # the kernels are built with --fmad=false (binary32 parity with the reference), so an
+            # FP32 lane retires at most one add or multiply per cycle: half the FMA-counted peak
+            roofline["frac_of_unfused_issue_ceiling"] = roofline["achieved"] / (peak / 2.0)
             if clocks.get("sm_mhz"):
                 roofline["frac_at_run_clock"] = roofline["achieved"] / (sm * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12)
         roofline["algorithmic_fp32_per_frame"] = phase["fp32"]
