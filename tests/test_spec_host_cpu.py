@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import mm3e_cuda
+import oracle_py
 from mm3e_cuda import scenes
 from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene, unbounded_mix_scene
 
@@ -108,3 +109,64 @@ def test_specialised_field_equals_interpreter_on_host(name, tmp_path):
                        text=True)
     print(name, r.stdout.strip().splitlines()[-1] if r.stdout.strip() else r.stderr[-500:])
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+
+
+INTERP_MAIN = r"""
+#include <cstdio>
+#include <vector>
+using namespace mm3e;
+int main(int argc, char** argv) {
+    FILE* ft = std::fopen(argv[1], "rb");
+    std::vector<float4> tape_words(1 << 20);
+    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
+    std::fclose(ft);
+    (void)nt;
+    const Tape T = tape_view(reinterpret_cast<const unsigned char*>(tape_words.data()));
+    FILE* fp = std::fopen(argv[2], "rb");
+    std::vector<float> pts(3 << 20);
+    size_t n = std::fread(pts.data(), sizeof(float), pts.size(), fp) / 3;
+    std::fclose(fp);
+    FILE* fo = std::fopen(argv[3], "wb");
+    for (size_t k = 0; k < n; ++k) {
+        Field f = world_eval(T, V{pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]});
+        std::fwrite(&f.d, 4, 1, fo);
+        std::fwrite(&f.m, 4, 1, fo);
+    }
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def interpreter_exe(tmp_path_factory):
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    d = tmp_path_factory.mktemp("interp")
+    (d / "main.cpp").write_text('#include "device_math.cuh"\n' + INTERP_MAIN)
+    exe = d / "interp"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-include", SHIM, str(d / "main.cpp"), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_interpreter_field_equals_oracle_on_host(name, interpreter_exe, tmp_path):
+    """The device tape interpreter's world field (device_math.cuh world_eval), compiled for the
+    host, against the oracle's restatement of Scene::field (oracle_field): bit for bit, distance
+    and material, on the same points. On the host both call the same libm, so this pins the
+    device field code's operation order to the oracle's; on the GPU only CUDA's own sinf/cosf and
+    the like can differ, within the tolerance the GPU parity tests hold."""
+    scene, cam = SCENES[name]()
+    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    pts = _points(scene, cam, np.random.default_rng(abs(hash(name)) % (1 << 32)))
+    pts.tofile(tmp_path / "points.bin")
+    subprocess.run([str(interpreter_exe), str(tmp_path / "tape.bin"), str(tmp_path / "points.bin"),
+                    str(tmp_path / "out.bin")], check=True)
+    out = np.fromfile(tmp_path / "out.bin", np.uint32).reshape(-1, 2)
+    d, m = out[:, 0].view(np.float32), out[:, 1]
+    od, om = oracle_py.field(scene.desc(), pts)
+    same = (d.view(np.uint32) == od.view(np.uint32)) | (np.isnan(d) & np.isnan(od))
+    assert same.all(), (pts[~same][:3], d[~same][:3], od[~same][:3])
+    assert np.array_equal(m, om)
