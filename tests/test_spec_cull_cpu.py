@@ -61,7 +61,7 @@ MU = F(1.0 - 2.0 ** -19)
 
 
 def _lin_constants(c, r):
-    """spec.cpp lin_test's constants: -2c, mu |c|^2 rounded down, 2 M r and M r^2 rounded up."""
+    """spec_gen.cpp lin_test's constants: -2c, mu |c|^2 rounded down, 2 M r and M r^2 rounded up."""
     M = Fraction(1) + Fraction(1, 2 ** 14)
     cc = sum(Fraction(float(x)) ** 2 for x in c) * Fraction(float(MU))
     c2 = np.float32(float(cc))
@@ -280,7 +280,7 @@ def test_smooth_skip_holds_for_large_accumulators_and_small_blends():
 
 def test_axis_plane_is_the_plane_field_bit_for_bit():
     """An axis-aligned plane (+-1 on one axis, +0 on the others, identity rotation, offset other
-    than -0) is generated as fl(+-l_k + h) with l_k = (p_k - pos_k) inv (spec.cpp axis_plane).
+    than -0) is generated as fl(+-l_k + h) with l_k = (p_k - pos_k) inv (spec_gen.cpp axis_plane).
     Checked bit for bit against the field the interpreter takes, dot(l, n) + h with l the
     identity-rotated, scaled local point (vec.rs:24-26 order; rot_t_identity), on signed zeros,
     subnormals and ordinary coordinates, for every axis, sign, offset and scale tested."""
@@ -339,7 +339,7 @@ def test_linearised_pretest_implies_exact_cull():
 
 
 def test_enclosing_sphere_covers_every_test_inside():
-    """The enclosing sphere over a union run's sphere tests (spec.cpp enclosing_sphere) contains
+    """The enclosing sphere over a union run's sphere tests (spec_gen.cpp enclosing_sphere) contains
     every cluster sphere and every member bound sphere inside its block, in exact arithmetic, so
     a sample beyond it would be culled by each of them."""
     hexf = lambda h: np.array([int(h, 16)], np.uint32).view(F)[0]

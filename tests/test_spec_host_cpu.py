@@ -1,6 +1,6 @@
 """Scene-specialised fields against the tape interpreter, on the host.
 
-The specialised program (spec.cpp's generated field: inlined objects, generated CSG programs,
+The specialised program (spec_gen.cpp's generated field: inlined objects, generated CSG programs,
 axis planes, linearised and enclosing-sphere pre-tests, weak bounds and skips) and the
 interpreter's world_eval (WorldPlan::eval, accel.rs:209-252) compile as plain C++ with the host
 definitions of the device intrinsics in tests/host_field/host_shim.h. Both are evaluated on the

@@ -210,7 +210,7 @@ def _csg_scene(expr, mod, lead=None, combine=None):
 @pytest.mark.parametrize("expr", list(CSG_EXPRS))
 def test_csg_weak_bound_holds(expr, mod):
     """A CSG object that the reference leaves unbounded (bend, repeat) gets a weak bound from its
-    program's parts (csg_weak in spec.cpp); the bound holds against the oracle's field."""
+    program's parts (csg_weak in spec_gen.cpp); the bound holds against the oracle's field."""
     rng = np.random.default_rng(abs(hash((expr, mod))) % (1 << 32))
     anchor = Object(Prim.sphere(0.1), Transform((40.0, 40.0, 40.0)), 0)
     s = _csg_scene(CSG_EXPRS[expr](), mod)
