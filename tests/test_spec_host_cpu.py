@@ -170,3 +170,60 @@ def test_interpreter_field_equals_oracle_on_host(name, interpreter_exe, tmp_path
     same = (d.view(np.uint32) == od.view(np.uint32)) | (np.isnan(d) & np.isnan(od))
     assert same.all(), (pts[~same][:3], d[~same][:3], od[~same][:3])
     assert np.array_equal(m, om)
+
+
+SHADE_MAIN = r"""
+#include <cstdio>
+#include <vector>
+using namespace mm3e;
+// per input row: n(3) l(3) v(3) albedo(3) metallic roughness reflectance cos f0 x(3) -> brdf(3) fresnel aces(3)
+int main(int argc, char** argv) {
+    FILE* fi = std::fopen(argv[1], "rb");
+    std::vector<float> in(21 << 16);
+    size_t n = std::fread(in.data(), sizeof(float), in.size(), fi) / 20;
+    std::fclose(fi);
+    FILE* fo = std::fopen(argv[2], "wb");
+    for (size_t k = 0; k < n; ++k) {
+        const float* r = &in[20 * k];
+        V b = brdf(V{r[0], r[1], r[2]}, V{r[3], r[4], r[5]}, V{r[6], r[7], r[8]}, V{r[9], r[10], r[11]}, r[12], r[13], r[14]);
+        float f = fresnel_schlick(r[15], r[16]);
+        float a[3] = {aces1(r[17]), aces1(r[18]), aces1(r[19])};
+        float o[7] = {b.x, b.y, b.z, f, a[0], a[1], a[2]};
+        std::fwrite(o, sizeof(float), 7, fo);
+    }
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+def test_shading_formulas_equal_oracle_on_host(tmp_path):
+    """The device shading formulas (device_math.cuh brdf, fresnel_schlick and aces1; shade.rs:51-72
+    and post.rs ACES), compiled for the host, against the oracle's restatements (oracle_brdf,
+    oracle_fresnel, oracle_aces) bit for bit on random unit vectors, albedos, roughness and
+    metalness, and on tone-mapping inputs from 0 to 100."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    (tmp_path / "main.cpp").write_text('#include "device_math.cuh"\n' + SHADE_MAIN)
+    exe = tmp_path / "shade"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-include", SHIM, str(tmp_path / "main.cpp"), "-o", str(exe)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    rng = np.random.default_rng(9)
+    n = 4000
+
+    def unit(k):
+        v = rng.standard_normal((k, 3))
+        return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+    rows = np.concatenate([unit(n), unit(n), unit(n), rng.uniform(0, 1, (n, 3)), rng.choice([0.0, 1.0], (n, 1)),
+                           rng.uniform(0.0, 1.0, (n, 1)), rng.uniform(0.0, 1.0, (n, 1)), rng.uniform(-0.2, 1.2, (n, 1)),
+                           rng.uniform(0.0, 1.0, (n, 1)), rng.uniform(0.0, 100.0, (n, 3)) ** rng.uniform(0.3, 1.0, (n, 1))],
+                          axis=1).astype(np.float32)
+    rows.tofile(tmp_path / "in.bin")
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
+    out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(-1, 7)
+    ref = np.array([oracle_py.brdf(rw[0:3], rw[3:6], rw[6:9], rw[9:12], rw[12], rw[13], rw[14])
+                    + (oracle_py.fresnel(rw[15], rw[16]),) + oracle_py.aces(rw[17:20]) for rw in rows], np.float32)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), np.argwhere(out.view(np.uint32) != ref.view(np.uint32))[:5]
