@@ -227,3 +227,104 @@ def test_shading_formulas_equal_oracle_on_host(tmp_path):
     ref = np.array([oracle_py.brdf(rw[0:3], rw[3:6], rw[6:9], rw[9:12], rw[12], rw[13], rw[14])
                     + (oracle_py.fresnel(rw[15], rw[16]),) + oracle_py.aces(rw[17:20]) for rw in rows], np.float32)
     assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), np.argwhere(out.view(np.uint32) != ref.view(np.uint32))[:5]
+
+
+STUBS = os.path.join(ROOT, "tests", "host_field", "host_kernel_stubs.h")
+
+MARCH_MAIN = r"""
+#include <cstdio>
+#include <vector>
+using namespace mm3e;
+using namespace mm3e::wave;
+template <class FP> static void march_all(WaveArgs& a, const unsigned char* tape, size_t n) {
+    for (size_t i = 0; i < n; ++i) {
+        MLane L;
+        L.item = (uint32_t)i;
+        L.phase = M_IDLE;
+        LaneTape<TM_MULTI> LT;
+        LT.p = tape;
+        if (m_start<TM_MULTI, FP>(L, LT, a))
+            while (L.phase != M_IDLE) m_step<TM_MULTI, FP>(L, LT, a);
+    }
+}
+int main(int argc, char** argv) {
+    FILE* ft = std::fopen(argv[1], "rb");
+    std::vector<float4> tape_words(1 << 20);
+    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
+    std::fclose(ft);
+    (void)nt;
+    const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
+    FILE* fr = std::fopen(argv[2], "rb");
+    std::vector<float> rays(6 << 16);
+    size_t n = std::fread(rays.data(), sizeof(float), rays.size(), fr) / 6;
+    std::fclose(fr);
+    std::vector<float4> qo(n), qd(n), hn(n);
+    std::vector<uint2> hm(n);
+    for (size_t i = 0; i < n; ++i) {
+        qo[i] = make_float4(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2], __uint_as_float((uint32_t)i));
+        qd[i] = make_float4(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5], 0.0f);
+    }
+    WaveArgs a{};
+    a.job0.tape = tape;
+    a.src = SRC_QUEUE;
+    a.b.q_o = qo.data();
+    a.b.q_d = qd.data();
+    a.b.h_n = hn.data();
+    a.b.h_m = hm.data();
+    FILE* fo = std::fopen(argv[3], "wb");
+    march_all<InterpField>(a, tape, n);
+    std::fwrite(hn.data(), sizeof(float4), n, fo);
+    std::fwrite(hm.data(), sizeof(uint2), n, fo);
+    march_all<spec::Field_>(a, tape, n);
+    std::fwrite(hn.data(), sizeof(float4), n, fo);
+    std::fwrite(hm.data(), sizeof(uint2), n, fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "csg_zoo", "unbounded_mix", "procedural3", "procedural8"])
+def test_march_state_machine_equals_oracle_on_host(name, tmp_path):
+    """The device march (march_kernels.cuh m_start / m_step: enhanced sphere tracing with its
+    rollback, gap-cover and tetrahedral-normal phases, march.rs:120-223), compiled for the host and
+    driven ray by ray over both the tape interpreter's field and the scene's generated field,
+    against the oracle's march (oracle_march_rays): hit or miss, material, steps, and t and the
+    normal of every hit, bit for bit, on rays from the scene's camera."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, cam = SCENES[name]()
+    src = mm3e_cuda.spec_source(scene)
+    ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
+    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+    (tmp_path / "main.cpp").write_text(defines + '#include "march_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
+                                       "\n}}\n" + MARCH_MAIN)
+    exe = tmp_path / "march"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    rng = np.random.default_rng(abs(hash(name)) % (1 << 32))
+    n = 3000
+    eye = np.array(cam.eye, np.float32)
+    fwd, right, up = (np.array(v, np.float64) for v in (cam.forward, cam.right, cam.up))
+    d = fwd + np.outer(rng.uniform(-1, 1, n) * cam.fov_scale * 1.7, right) + np.outer(rng.uniform(-1, 1, n) * cam.fov_scale, up)
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    rays = np.concatenate([np.repeat(eye[None], n, 0), d], axis=1).astype(np.float32)
+    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    rays.tofile(tmp_path / "rays.bin")
+    subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "rays.bin"), str(tmp_path / "out.bin")],
+                   check=True)
+    raw = np.fromfile(tmp_path / "out.bin", np.uint8)
+    per = n * 16 + n * 8
+    ot, om, os_, on = oracle_py.march_rays(scene.desc(), rays, threads=2, normals=True)
+    hit = om != 0xFFFFFFFF
+    for k, label in enumerate(("interpreter", "specialised")):
+        blk = raw[k * per:(k + 1) * per]
+        hn = blk[:n * 16].view(np.float32).reshape(n, 4)
+        hm = blk[n * 16:].view(np.uint32).reshape(n, 2)
+        assert np.array_equal(hm[:, 0], om), label
+        assert np.array_equal(hm[:, 1], os_), label
+        assert np.array_equal(hn[hit, 3].view(np.uint32), ot[hit].astype(np.float32).view(np.uint32)), label
+        assert np.array_equal(hn[hit, :3].view(np.uint32), on[hit].astype(np.float32).view(np.uint32)), label
+    assert hit.mean() > 0.2
