@@ -211,6 +211,56 @@ int oracle_march_rays(const mm3e_scene_desc* d, const float* rays6, size_t n, in
     return 0;
 }
 
+// Soft-shadow factor, in binary32, of every (ray, light) at the ray's hit, cast as shade_hit casts
+// it (lib.rs:1315-1333): lifted origin hit.pos + normal * max(2 normal_h, 0.01), toward the
+// light, max_t = min(light distance, max_dist). shadow[i * n_lights + l] is -1 where no shadow ray
+// is cast (a miss, a light behind the surface, shadows off); n_lights is the scene's light count.
+int oracle_soft_shadows(const mm3e_scene_desc* d, const float* rays6, size_t n, unsigned threads, float* shadow) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    bool dual_safe = scene_dual_safe(s);
+    const size_t nl = s.lights.size();
+    for_row_bands(0, (uint32_t)n, threads, [&](uint32_t a, uint32_t b, size_t) {
+        World<float> w(s);
+        for (uint32_t i = a; i < b; ++i) {
+            Ray<float> r{v3f<float>(rays6 + 6 * i), v3f<float>(rays6 + 6 * i + 3)};
+            Hit<float> hit = march_scene(s, w, dual_safe, r);
+            for (size_t l = 0; l < nl; ++l) {
+                float out = -1.0f;
+                const auto& light = s.lights[l];
+                V3<float> l_dir;
+                float l_dist;
+                if (hit.hit && s.shadows) {
+                    light.toward(hit.pos, l_dir, l_dist);
+                    if (lambert(hit.normal, l_dir) > 0.0f) {
+                        float max_t = o_min(l_dist, s.marcher.max_dist);
+                        float lift = o_max(s.marcher.normal_h * 2.0f, 0.01f);
+                        out = s.marcher.soft_shadow(w, hit.pos + scale(hit.normal, lift), l_dir, max_t,
+                                                    light.shadow_k(l_dist));
+                    }
+                }
+                shadow[i * nl + l] = out;
+            }
+        }
+    });
+    return 0;
+}
+
+// Ambient occlusion, in binary32, at every ray's hit, as shade_hit takes it (lib.rs:1300-1304,
+// march.rs:264-280); -1 where the ray misses or the scene has AO off.
+int oracle_ambient_occlusion(const mm3e_scene_desc* d, const float* rays6, size_t n, unsigned threads, float* occ) {
+    Scene<float> s = scene_from_desc<float>(*d);
+    bool dual_safe = scene_dual_safe(s);
+    for_row_bands(0, (uint32_t)n, threads, [&](uint32_t a, uint32_t b, size_t) {
+        World<float> w(s);
+        for (uint32_t i = a; i < b; ++i) {
+            Ray<float> r{v3f<float>(rays6 + 6 * i), v3f<float>(rays6 + 6 * i + 3)};
+            Hit<float> hit = march_scene(s, w, dual_safe, r);
+            occ[i] = hit.hit && s.ao ? s.marcher.ambient_occlusion(w, hit.pos, hit.normal) : -1.0f;
+        }
+    });
+    return 0;
+}
+
 // World field at points (accelerated WorldPlan, or the linear reference fold).
 int oracle_field(const mm3e_scene_desc* d, const float* pts3, size_t n, int linear, float* dist, uint32_t* mat) {
     Scene<float> s = scene_from_desc<float>(*d);

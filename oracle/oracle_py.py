@@ -30,6 +30,8 @@ def lib():
         l.oracle_primary_hits.argtypes = [vp, vp, C.c_uint, P(C.c_float), P(C.c_uint32), P(C.c_uint32), P(C.c_float)]
         l.oracle_march_rays.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_int, C.c_uint, P(C.c_double),
                                         P(C.c_uint32), P(C.c_uint32), P(C.c_double)]
+        l.oracle_soft_shadows.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_uint, P(C.c_float)]
+        l.oracle_ambient_occlusion.argtypes = [vp, P(C.c_float), C.c_size_t, C.c_uint, P(C.c_float)]
         l.oracle_sdf.argtypes = [C.c_uint32, P(C.c_float), C.c_float, C.c_float, C.c_float]
         l.oracle_sdf.restype = C.c_float
         l.oracle_combine.argtypes = [C.c_uint32, C.c_float, C.c_uint32, C.c_float, C.c_uint32, C.c_float,
@@ -134,6 +136,24 @@ def march_rays(handle, rays6, use_double=False, threads=None, normals=False):
     if normals:
         return t, m, s, nrm.reshape(n, 3)
     return t, m, s
+
+
+def soft_shadows(handle, rays6, threads=None):
+    """Soft-shadow factor of every (ray, light) at the ray's binary32 hit, shape (n, n_lights);
+    -1 where no shadow ray is cast."""
+    rays6 = np.ascontiguousarray(rays6, np.float32).reshape(-1, 6)
+    n, nl = len(rays6), handle.desc.n_lights
+    out = np.zeros(max(n * nl, 1), np.float32)
+    lib().oracle_soft_shadows(C.addressof(handle.desc), _f(rays6), n, threads or threads_default(), _f(out))
+    return out[:n * nl].reshape(n, nl)
+
+
+def ambient_occlusion(handle, rays6, threads=None):
+    """Ambient occlusion at every ray's binary32 hit; -1 on a miss or with AO off."""
+    rays6 = np.ascontiguousarray(rays6, np.float32).reshape(-1, 6)
+    out = np.zeros(max(len(rays6), 1), np.float32)
+    lib().oracle_ambient_occlusion(C.addressof(handle.desc), _f(rays6), len(rays6), threads or threads_default(), _f(out))
+    return out[:len(rays6)]
 
 
 def sdf(kind, params, p):

@@ -328,3 +328,129 @@ def test_march_state_machine_equals_oracle_on_host(name, tmp_path):
         assert np.array_equal(hn[hit, 3].view(np.uint32), ot[hit].astype(np.float32).view(np.uint32)), label
         assert np.array_equal(hn[hit, :3].view(np.uint32), on[hit].astype(np.float32).view(np.uint32)), label
     assert hit.mean() > 0.2
+
+
+SHADOW_MAIN = r"""
+#include <cstdio>
+#include <vector>
+using namespace mm3e;
+using namespace mm3e::wave;
+template <class FP> static void march_all(WaveArgs& a, const unsigned char* tape, size_t n) {
+    for (size_t i = 0; i < n; ++i) {
+        MLane L;
+        L.item = (uint32_t)i;
+        L.phase = M_IDLE;
+        LaneTape<TM_MULTI> LT;
+        LT.p = tape;
+        if (m_start<TM_MULTI, FP>(L, LT, a))
+            while (L.phase != M_IDLE) m_step<TM_MULTI, FP>(L, LT, a);
+    }
+}
+template <class FP> static void shadow_all(WaveArgs& a, const unsigned char* tape, size_t n) {
+    // Items run light-major, as the persistent pass hands them out; s_start maps each to its slot.
+    for (size_t i = 0; i < n * a.lights_max; ++i) {
+        SLane S;
+        S.item = (uint32_t)i;
+        LaneTape<TM_MULTI> LT;
+        LT.p = tape;
+        if (s_start<TM_MULTI, FP>(S, LT, a, (uint32_t)n))
+            while (S.item != NIL) s_step<TM_MULTI, FP>(S, LT, a);
+    }
+}
+int main(int argc, char** argv) {
+    FILE* ft = std::fopen(argv[1], "rb");
+    std::vector<float4> tape_words(1 << 20);
+    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
+    std::fclose(ft);
+    (void)nt;
+    const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
+    FILE* fr = std::fopen(argv[2], "rb");
+    std::vector<float> rays(6 << 16);
+    size_t n = std::fread(rays.data(), sizeof(float), rays.size(), fr) / 6;
+    std::fclose(fr);
+    const uint32_t nl = (uint32_t)std::atoi(argv[4]);
+    std::vector<float4> qo(n), qd(n), hn(n);
+    std::vector<uint2> hm(n);
+    std::vector<float> sh(n * nl), occ(n);
+    for (size_t i = 0; i < n; ++i) {
+        qo[i] = make_float4(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2], __uint_as_float((uint32_t)i));
+        qd[i] = make_float4(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5], 0.0f);
+    }
+    WaveArgs a{};
+    a.job0.tape = tape;
+    a.src = SRC_QUEUE;
+    a.lights_max = nl;
+    a.b.q_o = qo.data();
+    a.b.q_d = qd.data();
+    a.b.h_n = hn.data();
+    a.b.h_m = hm.data();
+    a.b.shadow = sh.data();
+    a.b.occ = occ.data();
+    FILE* fo = std::fopen(argv[3], "wb");
+    march_all<InterpField>(a, tape, n);
+    shadow_all<InterpField>(a, tape, n);
+    for (size_t i = 0; i < n; ++i) ao_slot<InterpField>(a, (uint32_t)i);
+    std::fwrite(sh.data(), sizeof(float), sh.size(), fo);
+    std::fwrite(occ.data(), sizeof(float), n, fo);
+    march_all<spec::Field_>(a, tape, n);
+    shadow_all<spec::Field_>(a, tape, n);
+    for (size_t i = 0; i < n; ++i) ao_slot<spec::Field_>(a, (uint32_t)i);
+    std::fwrite(sh.data(), sizeof(float), sh.size(), fo);
+    std::fwrite(occ.data(), sizeof(float), n, fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "procedural0", "procedural3", "procedural8", "procedural11"])
+def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
+    """The device soft-shadow march (march_kernels.cuh s_start / s_step: the lifted origin, the
+    light's direction, distance and k, the jittered start and the min(k h / t) fold with its
+    division skip, march.rs:227-259 and lib.rs:1315-1333), compiled for the host and run over the
+    device march's own hits with both the tape interpreter's field and the scene's generated field,
+    against the oracle's soft shadow at its own hits (oracle_soft_shadows): every (ray, light)
+    factor bit for bit, and -1 on the same pairs where no shadow ray is cast. The host sinf is the
+    oracle's, so the jitter is bit-equal here; on the device it is within sinf's error bound.
+    The AO pass (ao_slot, march.rs:264-280) runs over the same hits against oracle_ambient_occlusion,
+    bit for bit, and leaves 1 on a miss."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, cam = SCENES[name]()
+    nl = scene.desc().desc.n_lights
+    assert nl > 0
+    src = mm3e_cuda.spec_source(scene)
+    ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
+    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+    (tmp_path / "main.cpp").write_text(defines + '#include <cstdlib>\n#include "march_kernels.cuh"\n'
+                                       'namespace mm3e { namespace spec {\n' + ns + "\n}}\n" + SHADOW_MAIN)
+    exe = tmp_path / "shadow"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    rng = np.random.default_rng(abs(hash(name)) % (1 << 32))
+    n = 2000
+    eye = np.array(cam.eye, np.float32)
+    fwd, right, up = (np.array(v, np.float64) for v in (cam.forward, cam.right, cam.up))
+    d = fwd + np.outer(rng.uniform(-1, 1, n) * cam.fov_scale * 1.7, right) + np.outer(rng.uniform(-1, 1, n) * cam.fov_scale, up)
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    rays = np.concatenate([np.repeat(eye[None], n, 0), d], axis=1).astype(np.float32)
+    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    rays.tofile(tmp_path / "rays.bin")
+    subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "rays.bin"), str(tmp_path / "out.bin"),
+                    str(nl)], check=True)
+    out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, n * nl + n)
+    ref = oracle_py.soft_shadows(scene.desc(), rays, threads=2)
+    ref_occ = oracle_py.ambient_occlusion(scene.desc(), rays, threads=2)
+    cast = ref >= 0
+    lit = ref_occ >= 0
+    assert lit.mean() > 0.2
+    for k, label in enumerate(("interpreter", "specialised")):
+        dev, occ = out[k, :n * nl].reshape(n, nl), out[k, n * nl:]
+        assert np.array_equal(occ[lit].view(np.uint32), ref_occ[lit].view(np.uint32)), label
+        assert np.array_equal(dev >= 0, cast), label
+        assert np.array_equal(dev[cast].view(np.uint32), ref[cast].view(np.uint32)), \
+            (label, np.argwhere(dev.view(np.uint32) != ref.view(np.uint32))[:5])
+    assert cast.mean() > 0.1
+    assert ((ref[cast] > 0) & (ref[cast] < 1)).any() and (ref[cast] == 0).any()
