@@ -454,3 +454,156 @@ def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
             (label, np.argwhere(dev.view(np.uint32) != ref.view(np.uint32))[:5])
     assert cast.mean() > 0.1
     assert ((ref[cast] > 0) & (ref[cast] < 1)).any() and (ref[cast] == 0).any()
+
+
+FRAME_MAIN = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+using namespace mm3e;
+using namespace mm3e::wave;
+// One frame through the device pass sequence, pass by pass and item by item: the march of each
+// level (camera samples, then the reflection queue), the reflection rays of the next level, AO,
+// soft shadows, shading, and at the end the resolve of every pixel slot.
+template <class FP>
+static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, uint32_t h, uint32_t aa,
+                  std::vector<float4>& hdr) {
+    const uint32_t wlog = 3;
+    const TapeHeader& H = *tape_view(tape).h;
+    FrameJob J{};
+    J.tape = tape;
+    J.cam = cam;
+    J.width = w;
+    J.height = h;
+    J.aa = aa;
+    J.spp = aa * aa;
+    J.tiles_x = (w + 7u) / 8u;
+    J.n_slots = J.tiles_x * ((h + 3u) / 4u) * 32u;
+    J.n_samples = J.n_slots * J.spp;
+    J.n_pixels = w * h;
+    J.n_lights = H.n_lights;
+    const uint32_t ns = J.n_samples, nl = H.n_lights, levels = H.bounces + 1u;
+    std::vector<float4> q_o(ns), q_d(ns), nq_o(ns), nq_d(ns), h_n(ns), term(ns), lvl((size_t)2 * ns * levels);
+    std::vector<uint2> h_m(ns);
+    std::vector<float> occ(ns), shadow((size_t)ns * (nl ? nl : 1u));
+    hdr.assign(J.n_pixels, make_float4(0.f, 0.f, 0.f, 0.f));
+    uint32_t nq_count = 0;
+    WaveArgs a{};
+    a.job0 = J;
+    a.n_jobs = 1;
+    a.cap = ns;
+    a.lights_max = nl;
+    a.tile_wlog = wlog;
+    a.b = WaveBuffers{q_o.data(), q_d.data(), h_n.data(), h_m.data(), occ.data(), shadow.data(), nq_o.data(),
+                      nq_d.data(), &nq_count, lvl.data(), term.data(), hdr.data(), nullptr};
+    const bool ao = (H.flags & SF_AO) && H.ao_samples > 0;
+    const bool shadows = (H.flags & SF_SHADOWS) && H.shadow_steps > 0 && nl > 0;
+    uint32_t n = ns;
+    for (uint32_t level = 0; level < levels && n > 0; ++level) {
+        a.level = level;
+        a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
+        a.n_items = n;
+        for (uint32_t i = 0; i < n; ++i) {
+            MLane L;
+            L.item = i;
+            L.phase = M_IDLE;
+            LaneTape<TM_MULTI> LT;
+            LT.p = tape;
+            if (m_start<TM_MULTI, FP>(L, LT, a))
+                while (L.phase != M_IDLE) m_step<TM_MULTI, FP>(L, LT, a);
+        }
+        nq_count = 0;
+        if (level + 1 < levels)
+            for (uint32_t i = 0; i < n; ++i) reflect_slots(a, i, true);
+        if (ao)
+            for (uint32_t i = 0; i < n; ++i) ao_slot<FP>(a, i);
+        if (shadows)
+            for (uint32_t i = 0; i < n * nl; ++i) {
+                SLane S;
+                S.item = i;
+                LaneTape<TM_MULTI> LT;
+                LT.p = tape;
+                if (s_start<TM_MULTI, FP>(S, LT, a, n))
+                    while (S.item != NIL) s_step<TM_MULTI, FP>(S, LT, a);
+            }
+        for (uint32_t i = 0; i < n; ++i) shade_slots(a, i, true);
+        for (uint32_t i = 0; i < nq_count; ++i) {
+            q_o[i] = nq_o[i];
+            q_d[i] = nq_d[i];
+        }
+        n = nq_count;
+    }
+    for (uint32_t s = 0; s < J.n_slots; ++s) resolve_slot(a, s, 1u);
+}
+int main(int argc, char** argv) {
+    FILE* ft = std::fopen(argv[1], "rb");
+    std::vector<float4> tape_words(1 << 20);
+    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
+    std::fclose(ft);
+    (void)nt;
+    const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
+    float c[13];
+    FILE* fc = std::fopen(argv[2], "rb");
+    size_t nc = std::fread(c, sizeof(float), 13, fc);
+    std::fclose(fc);
+    (void)nc;
+    CameraArgs cam;
+    for (int k = 0; k < 3; ++k) {
+        cam.eye[k] = c[k];
+        cam.fwd[k] = c[3 + k];
+        cam.right[k] = c[6 + k];
+        cam.up[k] = c[9 + k];
+    }
+    cam.fov_scale = c[12];
+    const uint32_t w = (uint32_t)std::atoi(argv[4]), h = (uint32_t)std::atoi(argv[5]), aa = (uint32_t)std::atoi(argv[6]);
+    std::vector<float4> hdr;
+    FILE* fo = std::fopen(argv[3], "wb");
+    frame<InterpField>(tape, cam, w, h, aa, hdr);
+    std::fwrite(hdr.data(), sizeof(float4), hdr.size(), fo);
+    frame<spec::Field_>(tape, cam, w, h, aa, hdr);
+    std::fwrite(hdr.data(), sizeof(float4), hdr.size(), fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "noncons", "smooth_chain", "csg_zoo", "unbounded_mix",
+                                  "procedural0", "procedural3", "procedural8", "procedural11"])
+def test_frame_equals_oracle_render_on_host(name, tmp_path):
+    """A whole frame through the device pass sequence (march_kernels.cuh and shade_kernels.cuh:
+    camera samples, march, reflection queue, AO, soft shadows, shade_hit, the reflection fold and
+    the AA average; lib.rs:1223-1360), compiled for the host and run pass by pass over both the
+    tape interpreter's field and the scene's generated field, against the oracle's render
+    (oracle_render's HDR radiance, before post): every pixel bit for bit. The scenes cover
+    reflections, 2x2 AA, fog, checker albedo, lights and their shadows, and CSG. On the device
+    only CUDA's transcendental functions (sinf, expf, powf, ...) differ from these."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, cam = SCENES[name]()
+    d = scene.desc().desc
+    assert not d.gi and d.n_volumes == 0  # device payloads, not in the host tape
+    src = mm3e_cuda.spec_source(scene)
+    ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
+    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+    (tmp_path / "main.cpp").write_text(defines + '#include "shade_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
+                                       "\n}}\n" + FRAME_MAIN)
+    exe = tmp_path / "frame"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    np.array(list(cam.eye) + list(cam.forward) + list(cam.right) + list(cam.up) + [cam.fov_scale],
+             np.float32).tofile(tmp_path / "cam.bin")
+    w, h = d.width, d.height
+    subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "cam.bin"), str(tmp_path / "out.bin"), str(w),
+                    str(h), str(max(d.aa, 1))], check=True)
+    out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, h, w, 4)
+    _, ref = oracle_py.render(scene.desc(), cam, threads=2, want_hdr=True)
+    assert ref.std() > 0.1 and len(np.unique(ref.reshape(-1, 3), axis=0)) > w * h // 2
+    for k, label in enumerate(("interpreter", "specialised")):
+        dev = np.ascontiguousarray(out[k, :, :, :3])
+        bad = np.argwhere((dev.view(np.uint32) != ref.view(np.uint32)).any(axis=2))
+        assert len(bad) == 0, (label, len(bad), [(tuple(p), dev[tuple(p)].tolist(), ref[tuple(p)].tolist())
+                                                 for p in bad[:3]])
