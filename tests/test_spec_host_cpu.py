@@ -10,6 +10,7 @@ tests check the same identity on the device (test_gpu_spec.py)."""
 import os
 import shutil
 import subprocess
+from math import radians
 
 import numpy as np
 import pytest
@@ -17,6 +18,7 @@ import pytest
 import mm3e_cuda
 import oracle_py
 from mm3e_cuda import scenes
+from mm3e_cuda.scene import GiVolume, Material, Object, Prim, Scene, SdfVolume, Transform, directional, look_at
 from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene, unbounded_mix_scene
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -556,6 +558,22 @@ int main(int argc, char** argv) {
     }
     cam.fov_scale = c[12];
     const uint32_t w = (uint32_t)std::atoi(argv[4]), h = (uint32_t)std::atoi(argv[5]), aa = (uint32_t)std::atoi(argv[6]);
+    // Payloads the device reads by address (the GI probe cubes, each SDF volume's samples) are
+    // not in the tape's bytes: point the header and the volume records at host copies.
+    TapeHeader* H = reinterpret_cast<TapeHeader*>(tape_words.data());
+    std::vector<std::vector<float4>> payloads;
+    for (int k = 7; k < argc; ++k) {
+        FILE* fp = std::fopen(argv[k], "rb");
+        std::vector<float4> buf(1 << 20);
+        size_t nb = std::fread(buf.data(), 1, buf.size() * sizeof(float4), fp);
+        std::fclose(fp);
+        buf.resize((nb + sizeof(float4) - 1) / sizeof(float4));
+        payloads.push_back(std::move(buf));
+    }
+    size_t next = 0;
+    if (H->gi_nx) H->gi_cubes = payloads.at(next++).data();
+    DevVolume* vols = reinterpret_cast<DevVolume*>(reinterpret_cast<unsigned char*>(H) + H->off_volumes);
+    for (uint32_t v = 0; v < H->n_volumes; ++v) vols[v].data = reinterpret_cast<const float*>(payloads.at(next++).data());
     std::vector<float4> hdr;
     FILE* fo = std::fopen(argv[3], "wb");
     frame<InterpField>(tape, cam, w, h, aa, hdr);
@@ -568,8 +586,38 @@ int main(int argc, char** argv) {
 """
 
 
-@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "noncons", "smooth_chain", "csg_zoo", "unbounded_mix",
-                                  "procedural0", "procedural3", "procedural8", "procedural11"])
+def _cornell_gi_scene():
+    """The Cornell room with a GI probe volume baked by the oracle (6x6x6 probes, 4 samples)."""
+    scene, cam = scenes.cornell_scene(64, 36)
+    mn, size, dims, cubes = oracle_py.bake_gi(scene.desc(), (6, 6, 6), 4)
+    scene.gi = GiVolume(mn, size, dims, cubes)
+    return scene, cam
+
+
+def _volume_scene():
+    """A UV sphere baked to an SDF volume by the oracle (resolution 24, padding 0.25), a second,
+    scaled instance of the volume and a box, on a plane, under a soft sun."""
+    s = Scene(64, 36)
+    grey = s.material(Material.solid((0.8, 0.8, 0.8), roughness=0.5))
+    red = s.material(Material.solid((0.85, 0.12, 0.10), roughness=0.4, metallic=0.3))
+    pos, tri = scenes.uv_sphere_mesh(12, 18, 1.0)
+    vid = s.volume(SdfVolume(*oracle_py.bake_mesh_sdf(pos, tri, 24, 0.25)))
+    s.add(Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, grey))
+    s.add(Object(Prim.volume(vid), Transform.at((-1.0, 1.0, 0.0)), red))
+    s.add(Object(Prim.volume(vid), Transform((1.4, 0.7, 0.5), scale=0.7), grey))
+    s.add(Object(Prim.box((0.4, 0.4, 0.4)), Transform.at((0.3, 0.4, -1.5)), red))
+    sun = directional((0.45, 0.8, -0.4), (2.2, 2.1, 2.0)).soft(1.0 / 16.0)
+    s.sun_dir = sun.vec
+    s.light(sun)
+    return s, look_at((0.0, 2.0, -6.0), (0.0, 0.8, 0.0), (0.0, 1.0, 0.0), radians(45.0))
+
+
+FRAME_SCENES = {**SCENES, "cornell_gi": _cornell_gi_scene, "volumes": _volume_scene}
+
+
+@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "noncons", "smooth_chain",
+                                  "csg_zoo", "unbounded_mix", "procedural0", "procedural3", "procedural8",
+                                  "procedural11"])
 def test_frame_equals_oracle_render_on_host(name, tmp_path):
     """A whole frame through the device pass sequence (march_kernels.cuh and shade_kernels.cuh:
     camera samples, march, reflection queue, AO, soft shadows, shade_hit, the reflection fold and
@@ -580,9 +628,8 @@ def test_frame_equals_oracle_render_on_host(name, tmp_path):
     only CUDA's transcendental functions (sinf, expf, powf, ...) differ from these."""
     if not shutil.which("g++"):
         pytest.skip("no host C++ compiler")
-    scene, cam = SCENES[name]()
+    scene, cam = FRAME_SCENES[name]()
     d = scene.desc().desc
-    assert not d.gi and d.n_volumes == 0  # device payloads, not in the host tape
     src = mm3e_cuda.spec_source(scene)
     ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
     defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
@@ -596,9 +643,17 @@ def test_frame_equals_oracle_render_on_host(name, tmp_path):
     (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
     np.array(list(cam.eye) + list(cam.forward) + list(cam.right) + list(cam.up) + [cam.fov_scale],
              np.float32).tofile(tmp_path / "cam.bin")
+    payloads = []
+    if scene.gi is not None:  # float4 per face, 6 faces per probe
+        cubes = scene.gi.cubes.reshape(-1, 6, 3)
+        payloads.append(np.concatenate([cubes, np.zeros(cubes.shape[:2] + (1,), np.float32)], axis=2))
+    payloads += [v.data for v in scene.volumes]
+    for k, arr in enumerate(payloads):
+        np.ascontiguousarray(arr, np.float32).tofile(tmp_path / f"payload{k}.bin")
     w, h = d.width, d.height
     subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "cam.bin"), str(tmp_path / "out.bin"), str(w),
-                    str(h), str(max(d.aa, 1))], check=True)
+                    str(h), str(max(d.aa, 1))] + [str(tmp_path / f"payload{k}.bin") for k in range(len(payloads))],
+                   check=True)
     out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, h, w, 4)
     _, ref = oracle_py.render(scene.desc(), cam, threads=2, want_hdr=True)
     assert ref.std() > 0.1 and len(np.unique(ref.reshape(-1, 3), axis=0)) > w * h // 2
