@@ -468,8 +468,8 @@ using namespace mm3e::wave;
 // level (camera samples, then the reflection queue), the reflection rays of the next level, AO,
 // soft shadows, shading, and at the end the resolve of every pixel slot.
 template <class FP>
-static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, uint32_t h, uint32_t aa,
-                  std::vector<float4>& hdr) {
+static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, uint32_t h, uint32_t aa, float lens,
+                  float focus, std::vector<float4>& hdr, std::vector<float4>& fg) {
     const uint32_t wlog = 3;
     const TapeHeader& H = *tape_view(tape).h;
     FrameJob J{};
@@ -484,11 +484,19 @@ static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, 
     J.n_samples = J.n_slots * J.spp;
     J.n_pixels = w * h;
     J.n_lights = H.n_lights;
+    const bool film = lens >= 0.0f;  // film.rs render_film: thin-lens samples, coverage, foreground
+    J.lens_radius = film ? lens : 0.0f;
+    J.focus_distance = focus;
     const uint32_t ns = J.n_samples, nl = H.n_lights, levels = H.bounces + 1u;
-    std::vector<float4> q_o(ns), q_d(ns), nq_o(ns), nq_d(ns), h_n(ns), term(ns), lvl((size_t)2 * ns * levels);
-    std::vector<uint2> h_m(ns);
-    std::vector<float> occ(ns), shadow((size_t)ns * (nl ? nl : 1u));
+    std::vector<float4> q_o(ns), q_d(ns), nq_o(ns), nq_d(ns), term(ns), lvl((size_t)2 * ns * levels);
+    // Hit records per level: the primary level's stay for the resolve (film coverage), as the
+    // device keeps them apart from the reflection levels' buffers.
+    std::vector<std::vector<float4>> h_n(levels, std::vector<float4>(ns));
+    std::vector<std::vector<uint2>> h_m(levels, std::vector<uint2>(ns));
+    std::vector<std::vector<float>> occ(levels, std::vector<float>(ns)),
+        shadow(levels, std::vector<float>((size_t)ns * (nl ? nl : 1u)));
     hdr.assign(J.n_pixels, make_float4(0.f, 0.f, 0.f, 0.f));
+    fg.assign(J.n_pixels, make_float4(0.f, 0.f, 0.f, 0.f));
     uint32_t nq_count = 0;
     WaveArgs a{};
     a.job0 = J;
@@ -496,14 +504,19 @@ static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, 
     a.cap = ns;
     a.lights_max = nl;
     a.tile_wlog = wlog;
-    a.b = WaveBuffers{q_o.data(), q_d.data(), h_n.data(), h_m.data(), occ.data(), shadow.data(), nq_o.data(),
-                      nq_d.data(), &nq_count, lvl.data(), term.data(), hdr.data(), nullptr};
+    a.b = WaveBuffers{q_o.data(), q_d.data(), nullptr, nullptr, nullptr, nullptr, nq_o.data(),
+                      nq_d.data(), &nq_count, lvl.data(), term.data(), hdr.data(), fg.data()};
+    a.film = film ? 1u : 0u;
     const bool ao = (H.flags & SF_AO) && H.ao_samples > 0;
     const bool shadows = (H.flags & SF_SHADOWS) && H.shadow_steps > 0 && nl > 0;
     uint32_t n = ns;
     for (uint32_t level = 0; level < levels && n > 0; ++level) {
         a.level = level;
         a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
+        a.b.h_n = h_n[level].data();
+        a.b.h_m = h_m[level].data();
+        a.b.occ = occ[level].data();
+        a.b.shadow = shadow[level].data();
         a.n_items = n;
         for (uint32_t i = 0; i < n; ++i) {
             MLane L;
@@ -535,6 +548,8 @@ static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, 
         }
         n = nq_count;
     }
+    a.b.h_n = h_n[0].data();
+    a.b.h_m = h_m[0].data();
     for (uint32_t s = 0; s < J.n_slots; ++s) resolve_slot(a, s, 1u);
 }
 int main(int argc, char** argv) {
@@ -558,11 +573,12 @@ int main(int argc, char** argv) {
     }
     cam.fov_scale = c[12];
     const uint32_t w = (uint32_t)std::atoi(argv[4]), h = (uint32_t)std::atoi(argv[5]), aa = (uint32_t)std::atoi(argv[6]);
+    const float lens = std::strtof(argv[7], nullptr), focus = std::strtof(argv[8], nullptr);
     // Payloads the device reads by address (the GI probe cubes, each SDF volume's samples) are
     // not in the tape's bytes: point the header and the volume records at host copies.
     TapeHeader* H = reinterpret_cast<TapeHeader*>(tape_words.data());
     std::vector<std::vector<float4>> payloads;
-    for (int k = 7; k < argc; ++k) {
+    for (int k = 9; k < argc; ++k) {
         FILE* fp = std::fopen(argv[k], "rb");
         std::vector<float4> buf(1 << 20);
         size_t nb = std::fread(buf.data(), 1, buf.size() * sizeof(float4), fp);
@@ -574,12 +590,14 @@ int main(int argc, char** argv) {
     if (H->gi_nx) H->gi_cubes = payloads.at(next++).data();
     DevVolume* vols = reinterpret_cast<DevVolume*>(reinterpret_cast<unsigned char*>(H) + H->off_volumes);
     for (uint32_t v = 0; v < H->n_volumes; ++v) vols[v].data = reinterpret_cast<const float*>(payloads.at(next++).data());
-    std::vector<float4> hdr;
+    std::vector<float4> hdr, fg;
     FILE* fo = std::fopen(argv[3], "wb");
-    frame<InterpField>(tape, cam, w, h, aa, hdr);
+    frame<InterpField>(tape, cam, w, h, aa, lens, focus, hdr, fg);
     std::fwrite(hdr.data(), sizeof(float4), hdr.size(), fo);
-    frame<spec::Field_>(tape, cam, w, h, aa, hdr);
+    std::fwrite(fg.data(), sizeof(float4), fg.size(), fo);
+    frame<spec::Field_>(tape, cam, w, h, aa, lens, focus, hdr, fg);
     std::fwrite(hdr.data(), sizeof(float4), hdr.size(), fo);
+    std::fwrite(fg.data(), sizeof(float4), fg.size(), fo);
     std::fclose(fo);
     return 0;
 }
@@ -615,20 +633,9 @@ def _volume_scene():
 FRAME_SCENES = {**SCENES, "cornell_gi": _cornell_gi_scene, "volumes": _volume_scene}
 
 
-@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "noncons", "smooth_chain",
-                                  "csg_zoo", "unbounded_mix", "procedural0", "procedural3", "procedural8",
-                                  "procedural11"])
-def test_frame_equals_oracle_render_on_host(name, tmp_path):
-    """A whole frame through the device pass sequence (march_kernels.cuh and shade_kernels.cuh:
-    camera samples, march, reflection queue, AO, soft shadows, shade_hit, the reflection fold and
-    the AA average; lib.rs:1223-1360), compiled for the host and run pass by pass over both the
-    tape interpreter's field and the scene's generated field, against the oracle's render
-    (oracle_render's HDR radiance, before post): every pixel bit for bit. The scenes cover
-    reflections, 2x2 AA, fog, checker albedo, lights and their shadows, and CSG. On the device
-    only CUDA's transcendental functions (sinf, expf, powf, ...) differ from these."""
-    if not shutil.which("g++"):
-        pytest.skip("no host C++ compiler")
-    scene, cam = FRAME_SCENES[name]()
+def _host_frames(scene, cam, tmp_path, lens=-1.0, focus=1.0):
+    """Run the frame harness over the scene: (2, h, w, 4) HDR and (2, h, w, 4) foreground, for the
+    interpreter's field and the generated one."""
     d = scene.desc().desc
     src = mm3e_cuda.spec_source(scene)
     ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
@@ -652,9 +659,29 @@ def test_frame_equals_oracle_render_on_host(name, tmp_path):
         np.ascontiguousarray(arr, np.float32).tofile(tmp_path / f"payload{k}.bin")
     w, h = d.width, d.height
     subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "cam.bin"), str(tmp_path / "out.bin"), str(w),
-                    str(h), str(max(d.aa, 1))] + [str(tmp_path / f"payload{k}.bin") for k in range(len(payloads))],
-                   check=True)
-    out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, h, w, 4)
+                    str(h), str(max(d.aa, 1)), repr(float(lens)), repr(float(focus))] +
+                   [str(tmp_path / f"payload{k}.bin") for k in range(len(payloads))], check=True)
+    out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, 2, h, w, 4)
+    return out[:, 0], out[:, 1]
+
+
+@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "noncons", "smooth_chain",
+                                  "csg_zoo", "unbounded_mix", "procedural0", "procedural3", "procedural8",
+                                  "procedural11"])
+def test_frame_equals_oracle_render_on_host(name, tmp_path):
+    """A whole frame through the device pass sequence (march_kernels.cuh and shade_kernels.cuh:
+    camera samples, march, reflection queue, AO, soft shadows, shade_hit, the reflection fold and
+    the AA average; lib.rs:1223-1360), compiled for the host and run pass by pass over both the
+    tape interpreter's field and the scene's generated field, against the oracle's render
+    (oracle_render's HDR radiance, before post): every pixel bit for bit. The scenes cover
+    reflections, 2x2 AA, fog, checker albedo, lights and their shadows, and CSG. On the device
+    only CUDA's transcendental functions (sinf, expf, powf, ...) differ from these."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, cam = FRAME_SCENES[name]()
+    d = scene.desc().desc
+    w, h = d.width, d.height
+    out, _ = _host_frames(scene, cam, tmp_path)
     _, ref = oracle_py.render(scene.desc(), cam, threads=2, want_hdr=True)
     assert ref.std() > 0.1 and len(np.unique(ref.reshape(-1, 3), axis=0)) > w * h // 2
     for k, label in enumerate(("interpreter", "specialised")):
@@ -662,3 +689,28 @@ def test_frame_equals_oracle_render_on_host(name, tmp_path):
         bad = np.argwhere((dev.view(np.uint32) != ref.view(np.uint32)).any(axis=2))
         assert len(bad) == 0, (label, len(bad), [(tuple(p), dev[tuple(p)].tolist(), ref[tuple(p)].tolist())
                                                  for p in bad[:3]])
+
+
+@pytest.mark.parametrize("name,aa,lens,focus", [("gallery", 3, 0.08, 6.0), ("spheres", 2, 0.15, 5.0),
+                                                ("csg_zoo", 2, 0.0, 1.0), ("cornell_gi", 1, 0.1, 4.0),
+                                                ("procedural3", 2, 0.05, 8.0)])
+def test_film_equals_oracle_on_host(name, aa, lens, focus, tmp_path):
+    """render_film's samples (film.rs:147-196: the thin-lens ray of each AA sample through the
+    aperture grid, camera.rs:71-102; coverage and the premultiplied foreground of primary hits)
+    through the device pass sequence (march_kernels.cuh lens_ray, shade_kernels.cuh resolve_slot
+    in film mode), compiled for the host, against the oracle's render_film: beauty, alpha and
+    foreground bit for bit, for both fields. The cases cover a 3x3 and 2x2 aperture grid, a
+    pinhole with AA, and a lens at one sample (the centre ray)."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, cam = FRAME_SCENES[name]()
+    scene.aa = aa
+    hdr, fg = _host_frames(scene, cam, tmp_path, lens, focus)
+    ref = oracle_py.render_film(scene.desc(), cam, lens, focus, threads=2)
+    assert 0.0 < ref["alpha"].mean() < 1.0 and ref["beauty"].std() > 0.1
+    for k, label in enumerate(("interpreter", "specialised")):
+        for got, want, what in ((hdr[k, :, :, :3], ref["beauty"], "beauty"), (hdr[k, :, :, 3], ref["alpha"], "alpha"),
+                                (fg[k, :, :, :3], ref["foreground"], "foreground")):
+            got = np.ascontiguousarray(got)
+            assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
+                (label, what, int((got.view(np.uint32) != want.view(np.uint32)).sum()))
