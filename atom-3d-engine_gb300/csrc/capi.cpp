@@ -363,9 +363,10 @@ int render_to_device(mm3e_scene* s, const mm3e_camera* cam, const mm3e_dyn_spher
         CK(run_beauty(p, s->buf, s->tuning(), c->stream, c->sm_count, log));
         return MM3E_OK;
     }
-    const TapeHeader* th = reinterpret_cast<const TapeHeader*>(s->low.blob.data());
+    // The AO display value of every hit comes from the AO pass, which also writes the value of a
+    // marcher without AO samples (1, march.rs:266), so it runs whenever the mode is AO.
     WaveArgs a;
-    int rc = march_centers(s, cam, tape, tape_bytes, mode == MM3E_MODE_AO && th->ao_samples > 0, log, a);
+    int rc = march_centers(s, cam, tape, tape_bytes, mode == MM3E_MODE_AO, log, a);
     if (rc) return rc;
     a.aov_mode = mode;
     float4* out = format == MM3E_FB_RGBA_F32 ? static_cast<float4*>(dout) : s->buf.hdr;

@@ -1,8 +1,10 @@
 // shade_kernels.cuh — per-slot bodies of the shading, reflection-emit and resolve passes of the
 // wavefront render path (shade_hit, lib.rs:1286-1360; trace, lib.rs:1265-1282; the AA average,
-// lib.rs:1223-1243). The kernels that run them over a pass's slots are in wavefront.cu; the
-// bodies take a WaveArgs and one slot, so a host loop can drive them slot by slot as well.
+// lib.rs:1223-1243), of the AOV display modes, and of the GI bake's gather shading and per-face
+// average. The kernels that run them over a pass's slots are in wavefront.cu; the bodies take
+// their arguments and one slot, so a host loop can drive them slot by slot as well.
 #pragma once
+#include "../../include/mm3e_cuda.h"
 #include "march_kernels.cuh"
 
 namespace mm3e {
@@ -169,6 +171,93 @@ __device__ __forceinline__ void resolve_slot(const WaveArgs& a, uint32_t slot, u
     } else {
         a.b.hdr[px] = make_float4(o.x, o.y, o.z, 1.0f);
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// GI bake: Scene::gather (lib.rs:686-711) at a gather ray's hit, and the per-face average
+// (GiVolume::bake, gi.rs:78-86)
+// ------------------------------------------------------------------------------------------
+// Emissive plus unshadowed direct light at the hit, or the diffuse sky on a miss.
+__device__ __forceinline__ void gather_slot(const WaveArgs& a, uint32_t slot, float4* radiance) {
+    const Tape T = tape_view(a.job0.tape);
+    const TapeHeader& h = *T.h;
+    float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
+    V rd{d4.x, d4.y, d4.z};
+    uint2 hm = a.b.h_m[slot];
+    V c;
+    if (hm.x == NIL) {
+        c = sky_diffuse(rd, ld3(h.sun_dir));
+    } else {
+        float4 hn4 = a.b.h_n[slot];
+        V hp = V{o4.x, o4.y, o4.z} + scale(rd, hn4.w);
+        V hn{hn4.x, hn4.y, hn4.z};
+        const DevMaterial& m = T.mat[hm.x % h.n_materials];
+        V albedo = surface_albedo(m, hp);
+        c = ld3(m.emissive);
+        V view = scale(rd, -1.0f);
+        for (uint32_t li = 0; li < h.n_lights; ++li) {
+            const DevLight& lt = T.light[li];
+            V ldir;
+            float ldist;
+            light_toward(lt, hp, ldir, ldist);
+            if (fmaxf(dot(hn, ldir), 0.0f) > 0.0f) {
+                V out = brdf(hn, ldir, view, albedo, m.metallic, m.roughness, m.specular);
+                c = c + scale(cmul(out, ld3(lt.color)), light_atten(lt, ldist));
+            }
+        }
+    }
+    radiance[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+}
+
+// Weighted average of one probe face's gather radiances (idx = probe * 6 + face), summed in
+// direction order.
+__device__ __forceinline__ void gi_reduce_slot(const float4* __restrict__ rad, const float4* __restrict__ dirs,
+                                               uint32_t dpf, uint32_t idx, float4* __restrict__ cubes) {
+    uint32_t face = idx % 6u;
+    V acc{0.f, 0.f, 0.f};
+    float wsum = 0.0f;
+    for (uint32_t d = 0; d < dpf; ++d) {
+        float4 r = rad[(size_t)idx * dpf + d];
+        float w = dirs[face * dpf + d].w;
+        acc = acc + scale(V{r.x, r.y, r.z}, w);
+        wsum = wsum + w;
+    }
+    V c = scale(acc, 1.0f / fmaxf(wsum, 1e-4f));
+    cubes[idx] = make_float4(c.x, c.y, c.z, 0.0f);
+}
+
+// ------------------------------------------------------------------------------------------
+// AOV display value (lib.rs:1185-1217) of a pixel-centre hit of job 0 (row-major slots)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void aov_slot(const WaveArgs& a, uint32_t slot, float4* out) {
+    const Tape T = tape_view(a.job0.tape);
+    const TapeHeader& h = *T.h;
+    uint2 hm = a.b.h_m[slot];
+    float4 hn4 = a.b.h_n[slot];
+    bool hit = hm.x != NIL;
+    V n{hn4.x, hn4.y, hn4.z};
+    V v{0.f, 0.f, 0.f};
+    switch (a.aov_mode) {
+        case MM3E_MODE_NORMAL: v = hit ? scale(n, 0.5f) + splat(0.5f) : V{0.f, 0.f, 0.f}; break;
+        case MM3E_MODE_DEPTH: v = splat(1.0f - clampf(hn4.w / h.max_dist, 0.0f, 1.0f)); break;
+        case MM3E_MODE_AO: v = hit ? splat(a.b.occ[slot]) : splat(1.0f); break;
+        case MM3E_MODE_STEPS: {
+            float t = clampf((float)hm.y / (float)h.max_steps, 0.0f, 1.0f);
+            v = V{clampf(t * 3.0f - 1.5f, 0.f, 1.f), clampf(1.0f - fabsf(t * 3.0f - 1.3f), 0.f, 1.f),
+                  clampf(1.0f - t * 2.2f, 0.f, 1.f)};
+            break;
+        }
+        default: {
+            if (hit) {
+                float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
+                V hp = V{o4.x, o4.y, o4.z} + scale(V{d4.x, d4.y, d4.z}, hn4.w);
+                v = surface_albedo(T.mat[hm.x % h.n_materials], hp);
+            }
+            break;
+        }
+    }
+    v = clamp01(v);
+    out[slot] = make_float4(v.x, v.y, v.z, 1.0f);
 }
 
 }  // namespace wave

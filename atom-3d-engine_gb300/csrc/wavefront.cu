@@ -59,71 +59,15 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_resolve(const __grid_constant
 // AOV display values (lib.rs:1185-1217) for pixel-centre hits of job 0 (row-major slots).
 __global__ void __launch_bounds__(SHADE_THREADS) k_aov(const __grid_constant__ WaveArgs a, float4* out) {
     if (pass_failed(a)) return;
-    const Tape T = tape_view(a.job0.tape);
-    const TapeHeader& h = *T.h;
     uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= a.job0.width * a.job0.height) return;
-    uint2 hm = a.b.h_m[slot];
-    float4 hn4 = a.b.h_n[slot];
-    bool hit = hm.x != NIL;
-    V n{hn4.x, hn4.y, hn4.z};
-    V v{0.f, 0.f, 0.f};
-    switch (a.aov_mode) {
-        case MM3E_MODE_NORMAL: v = hit ? scale(n, 0.5f) + splat(0.5f) : V{0.f, 0.f, 0.f}; break;
-        case MM3E_MODE_DEPTH: v = splat(1.0f - clampf(hn4.w / h.max_dist, 0.0f, 1.0f)); break;
-        case MM3E_MODE_AO: v = hit ? splat(a.b.occ[slot]) : splat(1.0f); break;
-        case MM3E_MODE_STEPS: {
-            float t = clampf((float)hm.y / (float)h.max_steps, 0.0f, 1.0f);
-            v = V{clampf(t * 3.0f - 1.5f, 0.f, 1.f), clampf(1.0f - fabsf(t * 3.0f - 1.3f), 0.f, 1.f),
-                  clampf(1.0f - t * 2.2f, 0.f, 1.f)};
-            break;
-        }
-        default: {
-            if (hit) {
-                float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
-                V hp = V{o4.x, o4.y, o4.z} + scale(V{d4.x, d4.y, d4.z}, hn4.w);
-                v = surface_albedo(T.mat[hm.x % h.n_materials], hp);
-            }
-            break;
-        }
-    }
-    v = clamp01(v);
-    out[slot] = make_float4(v.x, v.y, v.z, 1.0f);
+    if (slot < a.job0.width * a.job0.height) aov_slot(a, slot, out);
 }
 
-// Scene::gather (lib.rs:686-711): emissive + unshadowed direct light, or the diffuse sky.
+// Scene::gather (lib.rs:686-711) at every gather ray's hit.
 __global__ void __launch_bounds__(SHADE_THREADS) k_gather_shade(const __grid_constant__ WaveArgs a, float4* radiance) {
     if (pass_failed(a)) return;
-    const Tape T = tape_view(a.job0.tape);
-    const TapeHeader& h = *T.h;
     uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= a.n_items) return;
-    float4 o4 = a.b.q_o[slot], d4 = a.b.q_d[slot];
-    V rd{d4.x, d4.y, d4.z};
-    uint2 hm = a.b.h_m[slot];
-    V c;
-    if (hm.x == NIL) {
-        c = sky_diffuse(rd, ld3(h.sun_dir));
-    } else {
-        float4 hn4 = a.b.h_n[slot];
-        V hp = V{o4.x, o4.y, o4.z} + scale(rd, hn4.w);
-        V hn{hn4.x, hn4.y, hn4.z};
-        const DevMaterial& m = T.mat[hm.x % h.n_materials];
-        V albedo = surface_albedo(m, hp);
-        c = ld3(m.emissive);
-        V view = scale(rd, -1.0f);
-        for (uint32_t li = 0; li < h.n_lights; ++li) {
-            const DevLight& lt = T.light[li];
-            V ldir;
-            float ldist;
-            light_toward(lt, hp, ldir, ldist);
-            if (fmaxf(dot(hn, ldir), 0.0f) > 0.0f) {
-                V out = brdf(hn, ldir, view, albedo, m.metallic, m.roughness, m.specular);
-                c = c + scale(cmul(out, ld3(lt.color)), light_atten(lt, ldist));
-            }
-        }
-    }
-    radiance[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+    if (slot < a.n_items) gather_slot(a, slot, radiance);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -358,22 +302,11 @@ __global__ void k_field(const unsigned char* __restrict__ tape, const float* __r
     mat[i] = f.m;
 }
 
-// GiVolume::bake per-face average (gi.rs:78-86).
+// GiVolume::bake per-face average (gi.rs:78-86), one thread per probe face.
 __global__ void k_gi_reduce(const float4* __restrict__ rad, const float4* __restrict__ dirs, uint32_t dpf,
                             uint32_t probes, float4* __restrict__ cubes) {
     uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;  // probe*6 + face
-    if (idx >= probes * 6u) return;
-    uint32_t face = idx % 6u;
-    V acc{0.f, 0.f, 0.f};
-    float wsum = 0.0f;
-    for (uint32_t d = 0; d < dpf; ++d) {
-        float4 r = rad[(size_t)idx * dpf + d];
-        float w = dirs[face * dpf + d].w;
-        acc = acc + scale(V{r.x, r.y, r.z}, w);
-        wsum = wsum + w;
-    }
-    V c = scale(acc, 1.0f / fmaxf(wsum, 1e-4f));
-    cubes[idx] = make_float4(c.x, c.y, c.z, 0.0f);
+    if (idx < probes * 6u) gi_reduce_slot(rad, dirs, dpf, idx, cubes);
 }
 
 typedef void (*WaveKernel)(const WaveArgs);

@@ -6,10 +6,15 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <math.h>
+#include <string>
+#include <vector>
 #include <cuda_runtime.h>
+// (Standard headers come before the __noinline__ stand-in below, which their attributes spell.)
 
 inline float __int_as_float(int x) { float f; std::memcpy(&f, &x, 4); return f; }
 inline float __uint_as_float(unsigned x) { float f; std::memcpy(&f, &x, 4); return f; }

@@ -85,6 +85,19 @@ def test_aov_modes(gpu_ctx, mode):
     _check_image(f"aov{mode}", gpu, ref)
 
 
+def test_aov_ao_without_samples(gpu_ctx):
+    """The AO display mode of a marcher without AO samples shows 1 at every pixel: a miss shows 1,
+    and so does a hit, since ambient_occlusion returns 1 when ao_samples is 0 (march.rs:264-267)."""
+    scene, cam = scenes.demo_scene()
+    scene.mode = abi.MODE_AO
+    scene.marcher.ao_samples = 0
+    compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)
+    gpu = compiled.render(cam, fmt=abi.FB_RGBA_F32)
+    ref = oracle_py.render(scene.desc(), cam)
+    assert np.array_equal(ref, np.ones_like(ref))
+    assert np.array_equal(gpu, ref)
+
+
 def test_render_linear_hdr(gpu_ctx):
     scene, cam = scenes.spheres_scene(160, 90)
     compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)

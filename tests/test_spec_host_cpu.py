@@ -17,7 +17,7 @@ import pytest
 
 import mm3e_cuda
 import oracle_py
-from mm3e_cuda import scenes
+from mm3e_cuda import abi, scenes
 from mm3e_cuda.scene import GiVolume, Material, Object, Prim, Scene, SdfVolume, Transform, directional, look_at
 from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene, unbounded_mix_scene
 
@@ -714,3 +714,237 @@ def test_film_equals_oracle_on_host(name, aa, lens, focus, tmp_path):
             got = np.ascontiguousarray(got)
             assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), \
                 (label, what, int((got.view(np.uint32) != want.view(np.uint32)).sum()))
+
+
+GI_MAIN = r"""
+#include <cstring>
+#include <vector>
+#include "lower.h"
+using namespace mm3e;
+using namespace mm3e::wave;
+// The device GI bake (mm3e_bake_gi) pass by pass: the product's probe grid and gather directions
+// (gi_setup), the SRC_GATHER march of every (probe, face, direction) ray, the gather shading of
+// its hit, and the per-face weighted average. Cubes out as (probe, face, rgb).
+template <class FP>
+static void bake(const GiSetup& g, const unsigned char* tape, float* cubes18) {
+    const uint64_t probes = (uint64_t)g.nx * g.ny * g.nz, items = probes * 6u * g.dirs_per_face;
+    std::vector<float4> q_o(items), q_d(items), h_n(items), rad(items), dirs(g.dirs.size() / 4), cubes(probes * 6u);
+    std::vector<uint2> h_m(items);
+    std::memcpy(dirs.data(), g.dirs.data(), g.dirs.size() * sizeof(float));
+    WaveArgs a{};
+    a.job0.tape = tape;
+    a.src = SRC_GATHER;
+    a.n_items = (uint32_t)items;
+    a.cap = (uint32_t)items;
+    a.b.q_o = q_o.data();
+    a.b.q_d = q_d.data();
+    a.b.h_n = h_n.data();
+    a.b.h_m = h_m.data();
+    std::memcpy(a.gi_lo, g.lo, 12);
+    std::memcpy(a.gi_cell, g.cell, 12);
+    a.gi_nx = g.nx;
+    a.gi_ny = g.ny;
+    a.gi_nz = g.nz;
+    a.dirs_per_face = g.dirs_per_face;
+    a.gather_dirs = dirs.data();
+    for (uint64_t i = 0; i < items; ++i) {
+        MLane L;
+        L.item = (uint32_t)i;
+        L.phase = M_IDLE;
+        LaneTape<TM_MULTI> LT;
+        LT.p = tape;
+        if (m_start<TM_MULTI, FP>(L, LT, a))
+            while (L.phase != M_IDLE) m_step<TM_MULTI, FP>(L, LT, a);
+    }
+    for (uint64_t i = 0; i < items; ++i) gather_slot(a, (uint32_t)i, rad.data());
+    for (uint64_t i = 0; i < probes * 6u; ++i) gi_reduce_slot(rad.data(), dirs.data(), g.dirs_per_face, (uint32_t)i, cubes.data());
+    for (uint64_t i = 0; i < probes * 6u; ++i) {
+        cubes18[3 * i] = cubes[i].x;
+        cubes18[3 * i + 1] = cubes[i].y;
+        cubes18[3 * i + 2] = cubes[i].z;
+    }
+}
+extern "C" int host_bake_gi(const mm3e_scene_desc* d, const unsigned char* tape_bytes, size_t tape_len, uint32_t nx,
+                            uint32_t ny, uint32_t nz, uint32_t samples, int specialised, float* lo_size6,
+                            uint32_t* dims3, float* cubes18) {
+    GiSetup g;
+    if (!gi_setup(*d, nx, ny, nz, samples, g)) return 0;
+    std::vector<float4> words((tape_len + 15) / 16);
+    std::memcpy(words.data(), tape_bytes, tape_len);
+    const unsigned char* tape = reinterpret_cast<const unsigned char*>(words.data());
+    std::memcpy(lo_size6, g.lo, 12);
+    std::memcpy(lo_size6 + 3, g.size, 12);
+    dims3[0] = g.nx;
+    dims3[1] = g.ny;
+    dims3[2] = g.nz;
+    if (specialised) bake<spec::Field_>(g, tape, cubes18);
+    else bake<InterpField>(g, tape, cubes18);
+    return 1;
+}
+"""
+
+
+@pytest.mark.parametrize("name,dims,samples", [("cornell", (6, 5, 4), 5), ("gallery", (5, 4, 5), 5),
+                                               ("spheres", (4, 4, 4), 1), ("procedural8", (4, 3, 4), 5)])
+def test_gi_bake_equals_oracle_on_host(name, dims, samples, tmp_path):
+    """The device GI bake (mm3e_bake_gi: gi_setup's probe grid and directions, lower.cpp; the
+    SRC_GATHER march, march_kernels.cuh; gather_slot and gi_reduce_slot, shade_kernels.cuh;
+    Scene::bake_gi_unchecked, lib.rs:668-711, gi.rs:38-125), compiled for the host with the
+    product's own set-up code and run over both the interpreter's field and the generated one,
+    against the oracle's bake_gi on the same descriptor: grid bounds, dims and every cube face
+    bit for bit. On the device only CUDA's transcendental functions differ."""
+    import ctypes as C
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scene, _ = SCENES[name]()
+    src = mm3e_cuda.spec_source(scene)
+    ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
+    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+    (tmp_path / "main.cpp").write_text(defines + '#include "shade_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
+                                       "\n}}\n" + GI_MAIN)
+    lib_path = tmp_path / "libhostgi.so"
+    flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-fPIC", "-I", CUDA_INCLUDE, "-I", CSRC]
+    r = subprocess.run(["g++"] + flags + ["-c", os.path.join(CSRC, "lower.cpp"), "-o", str(tmp_path / "lower.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run(["g++"] + flags + ["-include", SHIM, "-include", STUBS, "-shared", str(tmp_path / "main.cpp"),
+                                          str(tmp_path / "lower.o"), "-o", str(lib_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lib = C.CDLL(str(lib_path))
+    handle = scene.desc()
+    tape = mm3e_cuda.scene_tape(scene)
+    mn, size, rdims, ref = oracle_py.bake_gi(handle, dims, samples)
+    n = rdims[0] * rdims[1] * rdims[2]
+    for specialised in (0, 1):
+        lo_size = np.zeros(6, np.float32)
+        got_dims = np.zeros(3, np.uint32)
+        cubes = np.zeros(n * 18, np.float32)
+        ok = lib.host_bake_gi(C.c_void_p(C.addressof(handle.desc)), tape, C.c_size_t(len(tape)), *[C.c_uint32(v) for v in dims],
+                              C.c_uint32(samples), C.c_int(specialised), lo_size.ctypes.data_as(C.c_void_p),
+                              got_dims.ctypes.data_as(C.c_void_p), cubes.ctypes.data_as(C.c_void_p))
+        assert ok == 1
+        assert tuple(got_dims) == tuple(rdims)
+        assert np.array_equal(lo_size.view(np.uint32), np.array(list(mn) + list(size), np.float32).view(np.uint32))
+        assert np.array_equal(cubes.view(np.uint32), ref.view(np.uint32)), \
+            (specialised, int((cubes.view(np.uint32) != ref.view(np.uint32)).sum()), n * 18)
+    assert ref.std() > 0.01
+
+
+AOV_MAIN = r"""
+using namespace mm3e;
+using namespace mm3e::wave;
+// An AOV frame as the device runs it: the pixel-centre march (SRC_CENTER), the AO pass in the AO
+// mode, and the display value of every pixel.
+template <class FP> static void aov(const unsigned char* tape, const CameraArgs& cam, uint32_t w, uint32_t h,
+                                    uint32_t mode, std::vector<float4>& out) {
+    const uint32_t n = w * h;
+    std::vector<float4> q_o(n), q_d(n), h_n(n);
+    std::vector<uint2> h_m(n);
+    std::vector<float> occ(n, -7.0f);
+    out.assign(n, make_float4(0.f, 0.f, 0.f, 0.f));
+    WaveArgs a{};
+    a.job0.tape = tape;
+    a.job0.cam = cam;
+    a.job0.width = w;
+    a.job0.height = h;
+    a.src = SRC_CENTER;
+    a.n_items = n;
+    a.cap = n;
+    a.aov_mode = mode;
+    a.b.q_o = q_o.data();
+    a.b.q_d = q_d.data();
+    a.b.h_n = h_n.data();
+    a.b.h_m = h_m.data();
+    a.b.occ = occ.data();
+    for (uint32_t i = 0; i < n; ++i) {
+        MLane L;
+        L.item = i;
+        L.phase = M_IDLE;
+        LaneTape<TM_MULTI> LT;
+        LT.p = tape;
+        if (m_start<TM_MULTI, FP>(L, LT, a))
+            while (L.phase != M_IDLE) m_step<TM_MULTI, FP>(L, LT, a);
+    }
+    if (mode == MM3E_MODE_AO)
+        for (uint32_t i = 0; i < n; ++i) ao_slot<FP>(a, i);
+    for (uint32_t i = 0; i < n; ++i) aov_slot(a, i, out.data());
+}
+int main(int argc, char** argv) {
+    FILE* ft = std::fopen(argv[1], "rb");
+    std::vector<float4> tape_words(1 << 20);
+    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
+    std::fclose(ft);
+    (void)nt;
+    const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
+    float c[13];
+    FILE* fc = std::fopen(argv[2], "rb");
+    size_t nc = std::fread(c, sizeof(float), 13, fc);
+    std::fclose(fc);
+    (void)nc;
+    CameraArgs cam;
+    for (int k = 0; k < 3; ++k) {
+        cam.eye[k] = c[k];
+        cam.fwd[k] = c[3 + k];
+        cam.right[k] = c[6 + k];
+        cam.up[k] = c[9 + k];
+    }
+    cam.fov_scale = c[12];
+    const uint32_t w = (uint32_t)std::atoi(argv[4]), h = (uint32_t)std::atoi(argv[5]), mode = (uint32_t)std::atoi(argv[6]);
+    std::vector<float4> out;
+    FILE* fo = std::fopen(argv[3], "wb");
+    aov<InterpField>(tape, cam, w, h, mode, out);
+    std::fwrite(out.data(), sizeof(float4), out.size(), fo);
+    aov<spec::Field_>(tape, cam, w, h, mode, out);
+    std::fwrite(out.data(), sizeof(float4), out.size(), fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+@pytest.mark.parametrize("name", ["gallery", "csg_zoo", "procedural8"])
+def test_aov_modes_equal_oracle_on_host(name, tmp_path):
+    """The AOV display modes (lib.rs:1178-1218: normal, depth, AO, step heat map, albedo) as the
+    device computes them (the SRC_CENTER march, the AO pass, shade_kernels.cuh aov_slot), compiled
+    for the host, against the oracle's render in each mode: every pixel bit for bit, for both
+    fields, and in the AO mode also with no AO samples (a white frame)."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    base, cam = FRAME_SCENES[name]()
+    cases = [(m, None) for m in (abi.MODE_NORMAL, abi.MODE_DEPTH, abi.MODE_AO, abi.MODE_STEPS, abi.MODE_ALBEDO)]
+    cases.append((abi.MODE_AO, 0))
+    np.array(list(cam.eye) + list(cam.forward) + list(cam.right) + list(cam.up) + [cam.fov_scale],
+             np.float32).tofile(tmp_path / "cam.bin")
+    exes = {}  # by generated source: it bakes the marcher's settings (AO samples among them), not the mode
+    for mode, ao_samples in cases:
+        scene = base.copy()
+        scene.mode = mode
+        if ao_samples is not None:
+            scene.marcher.ao_samples = ao_samples
+        src = mm3e_cuda.spec_source(scene)
+        if src not in exes:
+            ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
+            defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+            k = len(exes)
+            (tmp_path / f"main{k}.cpp").write_text(defines + '#include "shade_kernels.cuh"\nnamespace mm3e { namespace spec {\n' +
+                                                   ns + "\n}}\n" + AOV_MAIN)
+            exes[src] = tmp_path / f"aov{k}"
+            r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I",
+                                CUDA_INCLUDE, "-I", CSRC, "-include", SHIM, "-include", STUBS,
+                                str(tmp_path / f"main{k}.cpp"), "-o", str(exes[src])], capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr[-3000:]
+        exe = exes[src]
+        (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+        d = scene.desc().desc
+        w, h = d.width, d.height
+        subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "cam.bin"), str(tmp_path / "out.bin"),
+                        str(w), str(h), str(mode)], check=True)
+        out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, h, w, 4)
+        ref = oracle_py.render(scene.desc(), cam)
+        if ao_samples == 0:
+            assert np.array_equal(ref, np.ones_like(ref))
+        else:
+            assert ref[..., :3].std() > 0.01, mode
+        for k, label in enumerate(("interpreter", "specialised")):
+            assert np.array_equal(out[k].view(np.uint32), ref.view(np.uint32)), \
+                (label, mode, int((out[k].view(np.uint32) != ref.view(np.uint32)).any(axis=2).sum()))
