@@ -37,7 +37,9 @@ __device__ __forceinline__ void shade_slots(const WaveArgs& a, uint32_t slot, bo
             const DevMaterial& m = T.mat[hm.x % h.n_materials];
             V albedo = surface_albedo(m, hp);
             V view = scale(rd, -1.0f);
-            float occ = (h.flags & SF_AO) ? a.b.occ[slot] : 1.0f;
+            // The AO pass runs where the scene has AO and AO samples; without samples
+            // ambient_occlusion is 1 (march.rs:266), as without AO.
+            float occ = ((h.flags & SF_AO) && h.ao_samples > 0u) ? a.b.occ[slot] : 1.0f;
             V gi = V{0.f, 0.f, 0.f};
             if (h.flags & SF_GI) gi = gi_sample(h, hp, hn);
             V amb = ibl_irradiance(hn, ld3(h.sun_dir), ld3(h.sky_ambient)) + gi + ld3(h.ambient);

@@ -50,6 +50,25 @@ def test_batch_equals_plain_frames_host_outputs():
         ctx.close()
 
 
+def test_batch_without_ao_samples_equals_plain_frames():
+    """A batch whose only AO scene has no AO samples runs no AO pass; its frames shade with AO 1,
+    as the plain frames do (and the oracle, test_gpu_parity.py)."""
+    ctx = mm3e_cuda.Context(0)
+    try:
+        items = []
+        for k, (w, h) in enumerate([(64, 36), (40, 30), (33, 17)]):
+            s, cam = scenes.gallery_scene(w, h) if k != 1 else scenes.procedural_scene(5, w, h)
+            s.marcher.ao_samples = 0
+            items.append((mm3e_cuda.CompiledScene(ctx, s), cam, w, h))
+        outs = [np.zeros((h, w, 4), np.uint8) for _, _, w, h in items]
+        jobs = ctx.make_jobs([(cs, cam, 0, 0, abi.FB_RGBA8, None, o) for (cs, cam, _, _), o in zip(items, outs)])
+        ctx.render_batch(jobs)
+        for (cs, cam, w, h), o in zip(items, outs):
+            assert np.array_equal(o, _plain(cs, cam)), f"batched frame differs from the plain frame ({w}x{h})"
+    finally:
+        ctx.close()
+
+
 def test_batch_device_outputs_graphs_and_small_waves():
     torch = pytest.importorskip("torch")
     ctx = mm3e_cuda.Context(0)

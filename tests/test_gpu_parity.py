@@ -98,6 +98,15 @@ def test_aov_ao_without_samples(gpu_ctx):
     assert np.array_equal(gpu, ref)
 
 
+def test_ao_without_samples_parity(gpu_ctx):
+    """A scene with AO on but no AO samples shades with AO 1 (march.rs:264-267), as the oracle
+    does; the AO pass does not run for it."""
+    scene, cam = scenes.gallery_scene(160, 90)
+    scene.marcher.ao_samples = 0
+    compiled, gpu, ref = _render_pair(gpu_ctx, scene, cam)
+    _check_image("gallery_no_ao_samples", gpu, ref)
+
+
 def test_render_linear_hdr(gpu_ctx):
     scene, cam = scenes.spheres_scene(160, 90)
     compiled = mm3e_cuda.CompiledScene(gpu_ctx, scene)

@@ -630,7 +630,15 @@ def _volume_scene():
     return s, look_at((0.0, 2.0, -6.0), (0.0, 0.8, 0.0), (0.0, 1.0, 0.0), radians(45.0))
 
 
-FRAME_SCENES = {**SCENES, "cornell_gi": _cornell_gi_scene, "volumes": _volume_scene}
+def _no_ao_samples_scene():
+    """The gallery with AO on but no AO samples: ambient_occlusion then returns 1 (march.rs:266)."""
+    s, cam = scenes.gallery_scene(64, 36)
+    s.marcher.ao_samples = 0
+    return s, cam
+
+
+FRAME_SCENES = {**SCENES, "cornell_gi": _cornell_gi_scene, "volumes": _volume_scene,
+                "no_ao_samples": _no_ao_samples_scene}
 
 
 def _host_frames(scene, cam, tmp_path, lens=-1.0, focus=1.0):
@@ -665,9 +673,9 @@ def _host_frames(scene, cam, tmp_path, lens=-1.0, focus=1.0):
     return out[:, 0], out[:, 1]
 
 
-@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "noncons", "smooth_chain",
-                                  "csg_zoo", "unbounded_mix", "procedural0", "procedural3", "procedural8",
-                                  "procedural11"])
+@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "no_ao_samples", "noncons",
+                                  "smooth_chain", "csg_zoo", "unbounded_mix", "procedural0", "procedural3",
+                                  "procedural8", "procedural11"])
 def test_frame_equals_oracle_render_on_host(name, tmp_path):
     """A whole frame through the device pass sequence (march_kernels.cuh and shade_kernels.cuh:
     camera samples, march, reflection queue, AO, soft shadows, shade_hit, the reflection fold and
