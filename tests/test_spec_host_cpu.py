@@ -641,42 +641,78 @@ FRAME_SCENES = {**SCENES, "cornell_gi": _cornell_gi_scene, "volumes": _volume_sc
                 "no_ao_samples": _no_ao_samples_scene}
 
 
-def _host_frames(scene, cam, tmp_path, lens=-1.0, focus=1.0):
-    """Run the frame harness over the scene: (2, h, w, 4) HDR and (2, h, w, 4) foreground, for the
-    interpreter's field and the generated one."""
-    d = scene.desc().desc
+def _build_frame_harness(scene, work):
+    """Compile the frame harness with the scene's generated field into `work`; its path."""
     src = mm3e_cuda.spec_source(scene)
     ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
     defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
-    (tmp_path / "main.cpp").write_text(defines + '#include "shade_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
-                                       "\n}}\n" + FRAME_MAIN)
-    exe = tmp_path / "frame"
+    (work / "main.cpp").write_text(defines + '#include "shade_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
+                                   "\n}}\n" + FRAME_MAIN)
+    exe = work / "frame"
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
+                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(work / "main.cpp"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    return exe
+
+
+def _run_frame_harness(exe, scene, cam, work, lens=-1.0, focus=1.0):
+    """Run a built frame harness: (2, h, w, 4) HDR and (2, h, w, 4) foreground, for the
+    interpreter's field and the generated one."""
+    d = scene.desc().desc
+    (work / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
     np.array(list(cam.eye) + list(cam.forward) + list(cam.right) + list(cam.up) + [cam.fov_scale],
-             np.float32).tofile(tmp_path / "cam.bin")
+             np.float32).tofile(work / "cam.bin")
     payloads = []
     if scene.gi is not None:  # float4 per face, 6 faces per probe
         cubes = scene.gi.cubes.reshape(-1, 6, 3)
         payloads.append(np.concatenate([cubes, np.zeros(cubes.shape[:2] + (1,), np.float32)], axis=2))
     payloads += [v.data for v in scene.volumes]
     for k, arr in enumerate(payloads):
-        np.ascontiguousarray(arr, np.float32).tofile(tmp_path / f"payload{k}.bin")
+        np.ascontiguousarray(arr, np.float32).tofile(work / f"payload{k}.bin")
     w, h = d.width, d.height
-    subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "cam.bin"), str(tmp_path / "out.bin"), str(w),
+    subprocess.run([str(exe), str(work / "tape.bin"), str(work / "cam.bin"), str(work / "out.bin"), str(w),
                     str(h), str(max(d.aa, 1)), repr(float(lens)), repr(float(focus))] +
-                   [str(tmp_path / f"payload{k}.bin") for k in range(len(payloads))], check=True)
-    out = np.fromfile(tmp_path / "out.bin", np.float32).reshape(2, 2, h, w, 4)
+                   [str(work / f"payload{k}.bin") for k in range(len(payloads))], check=True)
+    out = np.fromfile(work / "out.bin", np.float32).reshape(2, 2, h, w, 4)
     return out[:, 0], out[:, 1]
 
 
-@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "no_ao_samples", "noncons",
-                                  "smooth_chain", "csg_zoo", "unbounded_mix", "procedural0", "procedural3",
-                                  "procedural8", "procedural11"])
-def test_frame_equals_oracle_render_on_host(name, tmp_path):
+FRAME_CASES = ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "no_ao_samples", "noncons", "smooth_chain",
+               "csg_zoo", "unbounded_mix", "procedural0", "procedural3", "procedural8", "procedural11"]
+FILM_CASES = [("gallery", 3, 0.08, 6.0), ("spheres", 2, 0.15, 5.0), ("csg_zoo", 2, 0.0, 1.0), ("cornell_gi", 1, 0.1, 4.0),
+              ("procedural3", 2, 0.05, 8.0)]
+
+
+def _film_scene(name, aa):
+    scene, cam = FRAME_SCENES[name]()
+    scene.aa = aa
+    return scene, cam
+
+
+@pytest.fixture(scope="module")
+def frame_harnesses(tmp_path_factory):
+    """Frame harnesses of every whole-frame and film case, compiled in parallel, by generated
+    source (the same source builds once)."""
+    from concurrent.futures import ThreadPoolExecutor
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    scenes_ = [FRAME_SCENES[n]()[0] for n in FRAME_CASES] + [_film_scene(n, aa)[0] for n, aa, _, _ in FILM_CASES]
+    by_src = {}
+    for sc in scenes_:
+        by_src.setdefault(mm3e_cuda.spec_source(sc), sc)
+    root = tmp_path_factory.mktemp("frame_harness")
+    works = []
+    for k in range(len(by_src)):
+        (root / str(k)).mkdir()
+        works.append(root / str(k))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+        exes = list(pool.map(_build_frame_harness, by_src.values(), works))
+    return dict(zip(by_src, exes))
+
+
+@pytest.mark.parametrize("name", FRAME_CASES)
+def test_frame_equals_oracle_render_on_host(name, frame_harnesses, tmp_path):
     """A whole frame through the device pass sequence (march_kernels.cuh and shade_kernels.cuh:
     camera samples, march, reflection queue, AO, soft shadows, shade_hit, the reflection fold and
     the AA average; lib.rs:1223-1360), compiled for the host and run pass by pass over both the
@@ -684,12 +720,10 @@ def test_frame_equals_oracle_render_on_host(name, tmp_path):
     (oracle_render's HDR radiance, before post): every pixel bit for bit. The scenes cover
     reflections, 2x2 AA, fog, checker albedo, lights and their shadows, and CSG. On the device
     only CUDA's transcendental functions (sinf, expf, powf, ...) differ from these."""
-    if not shutil.which("g++"):
-        pytest.skip("no host C++ compiler")
     scene, cam = FRAME_SCENES[name]()
     d = scene.desc().desc
     w, h = d.width, d.height
-    out, _ = _host_frames(scene, cam, tmp_path)
+    out, _ = _run_frame_harness(frame_harnesses[mm3e_cuda.spec_source(scene)], scene, cam, tmp_path)
     _, ref = oracle_py.render(scene.desc(), cam, threads=2, want_hdr=True)
     assert ref.std() > 0.1 and len(np.unique(ref.reshape(-1, 3), axis=0)) > w * h // 2
     for k, label in enumerate(("interpreter", "specialised")):
@@ -699,21 +733,16 @@ def test_frame_equals_oracle_render_on_host(name, tmp_path):
                                                  for p in bad[:3]])
 
 
-@pytest.mark.parametrize("name,aa,lens,focus", [("gallery", 3, 0.08, 6.0), ("spheres", 2, 0.15, 5.0),
-                                                ("csg_zoo", 2, 0.0, 1.0), ("cornell_gi", 1, 0.1, 4.0),
-                                                ("procedural3", 2, 0.05, 8.0)])
-def test_film_equals_oracle_on_host(name, aa, lens, focus, tmp_path):
+@pytest.mark.parametrize("name,aa,lens,focus", FILM_CASES)
+def test_film_equals_oracle_on_host(name, aa, lens, focus, frame_harnesses, tmp_path):
     """render_film's samples (film.rs:147-196: the thin-lens ray of each AA sample through the
     aperture grid, camera.rs:71-102; coverage and the premultiplied foreground of primary hits)
     through the device pass sequence (march_kernels.cuh lens_ray, shade_kernels.cuh resolve_slot
     in film mode), compiled for the host, against the oracle's render_film: beauty, alpha and
     foreground bit for bit, for both fields. The cases cover a 3x3 and 2x2 aperture grid, a
     pinhole with AA, and a lens at one sample (the centre ray)."""
-    if not shutil.which("g++"):
-        pytest.skip("no host C++ compiler")
-    scene, cam = FRAME_SCENES[name]()
-    scene.aa = aa
-    hdr, fg = _host_frames(scene, cam, tmp_path, lens, focus)
+    scene, cam = _film_scene(name, aa)
+    hdr, fg = _run_frame_harness(frame_harnesses[mm3e_cuda.spec_source(scene)], scene, cam, tmp_path, lens, focus)
     ref = oracle_py.render_film(scene.desc(), cam, lens, focus, threads=2)
     assert 0.0 < ref["alpha"].mean() < 1.0 and ref["beauty"].std() > 0.1
     for k, label in enumerate(("interpreter", "specialised")):
@@ -956,3 +985,64 @@ def test_aov_modes_equal_oracle_on_host(name, tmp_path):
         for k, label in enumerate(("interpreter", "specialised")):
             assert np.array_equal(out[k].view(np.uint32), ref.view(np.uint32)), \
                 (label, mode, int((out[k].view(np.uint32) != ref.view(np.uint32)).any(axis=2).sum()))
+
+
+SCENE_EDGES = {  # Scene / Marcher settings at their edges, each applied to the 48x27 gallery
+    "aa0": {"aa": 0},
+    "aa4": {"aa": 4},
+    "steps0": {"max_steps": 0},
+    "steps1": {"max_steps": 1},
+    "steps7": {"max_steps": 7},
+    "shadow_steps0": {"shadow_steps": 0},
+    "shadow_steps1": {"shadow_steps": 1},
+    "ao1": {"ao_samples": 1},
+    "ao2": {"ao_samples": 2},
+    "near_far": {"max_dist": 3.0},
+    "eps0": {"eps": 0.0},
+    "eps_big": {"eps": 0.05},
+    "relaxed": {"step_scale": 0.6},
+    "over_relaxed": {"step_scale": 1.6},
+    "lod": {"lod_footprint": 0.002},
+    "secant": {"secant": True},
+    "subitize": {"subitize": 0.5},
+    "secant_subitize_over": {"secant": True, "subitize": 0.3, "step_scale": 1.3},
+    "normal_h0": {"normal_h": 0.0},
+    "normal_h_big": {"normal_h": 0.05},
+    "bounces3": {"bounces": 3},
+    "bounces0": {"bounces": 0},
+    "no_shadows_no_ao": {"shadows": False, "ao": False},
+    "no_fog": {"fog_density": 0.0},
+}
+
+
+def test_frame_at_setting_edges_equals_oracle_on_host(tmp_path):
+    """Whole frames at the edges of the scene's and the marcher's settings (AA 0 and 4, no or one
+    march step, no shadow steps, one or two AO samples, a near far plane, zero and large epsilon,
+    relaxed and over-relaxed steps, LOD, secant and subitize boosts, zero normal offsets, 0 and 3
+    bounces, shadows, AO and fog off), through the device pass sequence over both fields, against
+    the oracle's render bit for bit. The generated field folds these settings into constants, so
+    this also checks every folded form against the interpreter's reading of the header. The
+    harnesses compile in parallel."""
+    from concurrent.futures import ThreadPoolExecutor
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    cases = {}
+    for edge, settings in SCENE_EDGES.items():
+        scene, cam = scenes.gallery_scene(48, 27)
+        for key, value in settings.items():
+            setattr(scene if hasattr(scene, key) else scene.marcher, key, value)
+        work = tmp_path / edge
+        work.mkdir()
+        cases[edge] = (scene, cam, work)
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+        exes = dict(zip(cases, pool.map(lambda c: _build_frame_harness(c[0], c[2]), cases.values())))
+    failed = {}
+    for edge, (scene, cam, work) in cases.items():
+        out, _ = _run_frame_harness(exes[edge], scene, cam, work)
+        _, ref = oracle_py.render(scene.desc(), cam, threads=2, want_hdr=True)
+        for k, label in enumerate(("interpreter", "specialised")):
+            dev = np.ascontiguousarray(out[k, :, :, :3])
+            bad = int((dev.view(np.uint32) != ref.view(np.uint32)).any(axis=2).sum())
+            if bad:
+                failed[(edge, label)] = bad
+    assert not failed, failed
