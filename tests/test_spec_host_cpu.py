@@ -637,8 +637,42 @@ def _no_ao_samples_scene():
     return s, cam
 
 
+def _shading_zoo_scene():
+    """Every primitive kind, with materials at their edges (metallic 0 and 1, roughness 0 and 1,
+    specular 0 and 1, reflectivity 1, emissive-only, checker, material ids past the table that
+    wrap around), lit by a directional light, a point light, a sphere light, a light inside an
+    object and a dim light far away, with a coloured sky and two reflection bounces."""
+    from mm3e_cuda.scene import Light
+    s = Scene(64, 36)
+    s.bounces = 2
+    s.aa = 1
+    s.sky_ambient = (0.3, 0.35, 0.5)
+    s.ambient = (0.03, 0.02, 0.01)
+    s.sun_dir = (0.2, 0.9, -0.3)
+    mats = [Material((0.8, 0.8, 0.8), roughness=0.0, metallic=1.0, reflectivity=1.0),
+            Material((0.7, 0.2, 0.1), roughness=1.0, specular=0.0),
+            Material((0.1, 0.6, 0.3), roughness=0.0, specular=1.0, metallic=0.0),
+            Material((0.0, 0.0, 0.0), emissive=(3.0, 2.0, 0.5)),
+            Material((0.9, 0.9, 0.9), checker=True, roughness=0.6),
+            Material((0.2, 0.3, 0.9), metallic=0.5, roughness=0.02, reflectivity=0.4)]
+    s.materials = list(mats)
+    s.add(Object(Prim.plane((0.0, 1.0, 0.0), 0.0), Transform.IDENTITY, 4))
+    prims = [Prim.sphere(0.5), Prim.box((0.4, 0.3, 0.5)), Prim.round_box((0.3, 0.3, 0.3), 0.1),
+             Prim.torus(0.4, 0.12), Prim.cylinder(0.4, 0.3), Prim.capsule((0.0, -0.3, 0.0), (0.0, 0.3, 0.0), 0.2),
+             Prim.cone(0.4, 0.1, 0.5), Prim.ellipsoid((0.5, 0.3, 0.4)), Prim.octahedron(0.5), Prim.hex_prism(0.35, 0.3)]
+    for k, pr in enumerate(prims):
+        x, z = -3.0 + 1.5 * (k % 5), 1.0 + 1.6 * (k // 5)
+        s.add(Object(pr, Transform((x, 0.6, z)), k % 6 if k < 6 else 6 + k))  # ids from 6 wrap around
+    s.light(directional((0.4, 0.8, -0.5), (1.5, 1.4, 1.3)).soft(0.05))
+    s.light(Light.point((1.0, 2.5, -1.0), (4.0, 3.0, 2.0)))
+    s.light(Light.sphere((-2.0, 1.5, 0.5), (3.0, 3.0, 4.0), 0.3))
+    s.light(Light.point((-3.0, 0.6, 1.0), (5.0, 5.0, 5.0)))  # inside the sphere at x = -3
+    s.light(Light.point((40.0, 30.0, 60.0), (0.5, 0.5, 0.5)))
+    return s, look_at((0.0, 3.0, -5.5), (0.0, 0.5, 1.5), (0.0, 1.0, 0.0), radians(55.0))
+
+
 FRAME_SCENES = {**SCENES, "cornell_gi": _cornell_gi_scene, "volumes": _volume_scene,
-                "no_ao_samples": _no_ao_samples_scene}
+                "no_ao_samples": _no_ao_samples_scene, "shading_zoo": _shading_zoo_scene}
 
 
 def _build_frame_harness(scene, work):
@@ -678,7 +712,8 @@ def _run_frame_harness(exe, scene, cam, work, lens=-1.0, focus=1.0):
     return out[:, 0], out[:, 1]
 
 
-FRAME_CASES = ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "no_ao_samples", "noncons", "smooth_chain",
+FRAME_CASES = ["gallery", "spheres", "cornell", "cornell_gi", "volumes", "no_ao_samples", "shading_zoo", "noncons",
+               "smooth_chain",
                "csg_zoo", "unbounded_mix", "procedural0", "procedural3", "procedural8", "procedural11"]
 FILM_CASES = [("gallery", 3, 0.08, 6.0), ("spheres", 2, 0.15, 5.0), ("csg_zoo", 2, 0.0, 1.0), ("cornell_gi", 1, 0.1, 4.0),
               ("procedural3", 2, 0.05, 8.0)]
