@@ -10,6 +10,7 @@ tests check the same identity on the device (test_gpu_spec.py)."""
 import os
 import shutil
 import subprocess
+import zlib
 from math import radians
 
 import numpy as np
@@ -23,10 +24,12 @@ from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chai
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "atom-3d-engine_gb300", "csrc")
-SHIM = os.path.join(ROOT, "tests", "host_field", "host_shim.h")
+HOST_DIR = os.path.join(ROOT, "tests", "host_field")
+SHIM = os.path.join(HOST_DIR, "host_shim.h")
 CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
 
 MAIN = r"""
+#include "host_io.h"
 #include <cstdio>
 #include <vector>
 namespace mm3e { namespace spec {
@@ -34,16 +37,10 @@ namespace mm3e { namespace spec {
 }}
 using namespace mm3e;
 int main(int argc, char** argv) {
-    FILE* ft = std::fopen(argv[1], "rb");
-    std::vector<float4> tape_words(1 << 20);
-    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
-    std::fclose(ft);
-    (void)nt;
+    std::vector<float4> tape_words = read_words(argv[1]);
     const Tape T = tape_view(reinterpret_cast<const unsigned char*>(tape_words.data()));
-    FILE* fp = std::fopen(argv[2], "rb");
-    std::vector<float> pts(3 << 20);
-    size_t n = std::fread(pts.data(), sizeof(float), pts.size(), fp) / 3;
-    std::fclose(fp);
+    const std::vector<float> pts = read_floats(argv[2]);
+    const size_t n = pts.size() / 3;
     size_t bad = 0;
     for (size_t k = 0; k < n; ++k) {
         V p{pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]};
@@ -101,12 +98,12 @@ def test_specialised_field_equals_interpreter_on_host(name, tmp_path):
     (tmp_path / "field.inc").write_text(body)
     (tmp_path / "main.cpp").write_text(defines + '#include "device_math.cuh"\n' + MAIN)
     exe = tmp_path / "field_check"
-    cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE, "-I", CSRC,
+    cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE, "-I", CSRC, "-I", HOST_DIR,
            "-I", str(tmp_path), "-include", SHIM, str(tmp_path / "main.cpp"), "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
-    _points(scene, cam, np.random.default_rng(abs(hash(name)) % (1 << 32))).tofile(tmp_path / "points.bin")
+    _points(scene, cam, np.random.default_rng(zlib.crc32(name.encode()))).tofile(tmp_path / "points.bin")
     r = subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "points.bin")], capture_output=True,
                        text=True)
     print(name, r.stdout.strip().splitlines()[-1] if r.stdout.strip() else r.stderr[-500:])
@@ -114,20 +111,15 @@ def test_specialised_field_equals_interpreter_on_host(name, tmp_path):
 
 
 INTERP_MAIN = r"""
+#include "host_io.h"
 #include <cstdio>
 #include <vector>
 using namespace mm3e;
 int main(int argc, char** argv) {
-    FILE* ft = std::fopen(argv[1], "rb");
-    std::vector<float4> tape_words(1 << 20);
-    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
-    std::fclose(ft);
-    (void)nt;
+    std::vector<float4> tape_words = read_words(argv[1]);
     const Tape T = tape_view(reinterpret_cast<const unsigned char*>(tape_words.data()));
-    FILE* fp = std::fopen(argv[2], "rb");
-    std::vector<float> pts(3 << 20);
-    size_t n = std::fread(pts.data(), sizeof(float), pts.size(), fp) / 3;
-    std::fclose(fp);
+    const std::vector<float> pts = read_floats(argv[2]);
+    const size_t n = pts.size() / 3;
     FILE* fo = std::fopen(argv[3], "wb");
     for (size_t k = 0; k < n; ++k) {
         Field f = world_eval(T, V{pts[3 * k], pts[3 * k + 1], pts[3 * k + 2]});
@@ -148,7 +140,7 @@ def interpreter_exe(tmp_path_factory):
     (d / "main.cpp").write_text('#include "device_math.cuh"\n' + INTERP_MAIN)
     exe = d / "interp"
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-include", SHIM, str(d / "main.cpp"), "-o", str(exe)], capture_output=True, text=True)
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, str(d / "main.cpp"), "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     return exe
 
@@ -162,7 +154,7 @@ def test_interpreter_field_equals_oracle_on_host(name, interpreter_exe, tmp_path
     the like can differ, within the tolerance the GPU parity tests hold."""
     scene, cam = SCENES[name]()
     (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
-    pts = _points(scene, cam, np.random.default_rng(abs(hash(name)) % (1 << 32)))
+    pts = _points(scene, cam, np.random.default_rng(zlib.crc32(name.encode())))
     pts.tofile(tmp_path / "points.bin")
     subprocess.run([str(interpreter_exe), str(tmp_path / "tape.bin"), str(tmp_path / "points.bin"),
                     str(tmp_path / "out.bin")], check=True)
@@ -209,7 +201,7 @@ def test_shading_formulas_equal_oracle_on_host(tmp_path):
     (tmp_path / "main.cpp").write_text('#include "device_math.cuh"\n' + SHADE_MAIN)
     exe = tmp_path / "shade"
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-include", SHIM, str(tmp_path / "main.cpp"), "-o", str(exe)], capture_output=True,
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, str(tmp_path / "main.cpp"), "-o", str(exe)], capture_output=True,
                        text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     rng = np.random.default_rng(9)
@@ -231,9 +223,10 @@ def test_shading_formulas_equal_oracle_on_host(tmp_path):
     assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), np.argwhere(out.view(np.uint32) != ref.view(np.uint32))[:5]
 
 
-STUBS = os.path.join(ROOT, "tests", "host_field", "host_kernel_stubs.h")
+STUBS = os.path.join(HOST_DIR, "host_kernel_stubs.h")
 
 MARCH_MAIN = r"""
+#include "host_io.h"
 #include <cstdio>
 #include <vector>
 using namespace mm3e;
@@ -250,16 +243,10 @@ template <class FP> static void march_all(WaveArgs& a, const unsigned char* tape
     }
 }
 int main(int argc, char** argv) {
-    FILE* ft = std::fopen(argv[1], "rb");
-    std::vector<float4> tape_words(1 << 20);
-    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
-    std::fclose(ft);
-    (void)nt;
+    std::vector<float4> tape_words = read_words(argv[1]);
     const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
-    FILE* fr = std::fopen(argv[2], "rb");
-    std::vector<float> rays(6 << 16);
-    size_t n = std::fread(rays.data(), sizeof(float), rays.size(), fr) / 6;
-    std::fclose(fr);
+    const std::vector<float> rays = read_floats(argv[2]);
+    const size_t n = rays.size() / 6;
     std::vector<float4> qo(n), qd(n), hn(n);
     std::vector<uint2> hm(n);
     for (size_t i = 0; i < n; ++i) {
@@ -303,10 +290,10 @@ def test_march_state_machine_equals_oracle_on_host(name, tmp_path):
                                        "\n}}\n" + MARCH_MAIN)
     exe = tmp_path / "march"
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    rng = np.random.default_rng(abs(hash(name)) % (1 << 32))
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
     n = 3000
     eye = np.array(cam.eye, np.float32)
     fwd, right, up = (np.array(v, np.float64) for v in (cam.forward, cam.right, cam.up))
@@ -333,6 +320,7 @@ def test_march_state_machine_equals_oracle_on_host(name, tmp_path):
 
 
 SHADOW_MAIN = r"""
+#include "host_io.h"
 #include <cstdio>
 #include <vector>
 using namespace mm3e;
@@ -360,16 +348,10 @@ template <class FP> static void shadow_all(WaveArgs& a, const unsigned char* tap
     }
 }
 int main(int argc, char** argv) {
-    FILE* ft = std::fopen(argv[1], "rb");
-    std::vector<float4> tape_words(1 << 20);
-    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
-    std::fclose(ft);
-    (void)nt;
+    std::vector<float4> tape_words = read_words(argv[1]);
     const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
-    FILE* fr = std::fopen(argv[2], "rb");
-    std::vector<float> rays(6 << 16);
-    size_t n = std::fread(rays.data(), sizeof(float), rays.size(), fr) / 6;
-    std::fclose(fr);
+    const std::vector<float> rays = read_floats(argv[2]);
+    const size_t n = rays.size() / 6;
     const uint32_t nl = (uint32_t)std::atoi(argv[4]);
     std::vector<float4> qo(n), qd(n), hn(n);
     std::vector<uint2> hm(n);
@@ -428,10 +410,10 @@ def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
                                        'namespace mm3e { namespace spec {\n' + ns + "\n}}\n" + SHADOW_MAIN)
     exe = tmp_path / "shadow"
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    rng = np.random.default_rng(abs(hash(name)) % (1 << 32))
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
     n = 2000
     eye = np.array(cam.eye, np.float32)
     fwd, right, up = (np.array(v, np.float64) for v in (cam.forward, cam.right, cam.up))
@@ -459,6 +441,7 @@ def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
 
 
 FRAME_MAIN = r"""
+#include "host_io.h"
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -553,39 +536,16 @@ static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, 
     for (uint32_t s = 0; s < J.n_slots; ++s) resolve_slot(a, s, 1u);
 }
 int main(int argc, char** argv) {
-    FILE* ft = std::fopen(argv[1], "rb");
-    std::vector<float4> tape_words(1 << 20);
-    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
-    std::fclose(ft);
-    (void)nt;
+    std::vector<float4> tape_words = read_words(argv[1]);
     const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
-    float c[13];
-    FILE* fc = std::fopen(argv[2], "rb");
-    size_t nc = std::fread(c, sizeof(float), 13, fc);
-    std::fclose(fc);
-    (void)nc;
-    CameraArgs cam;
-    for (int k = 0; k < 3; ++k) {
-        cam.eye[k] = c[k];
-        cam.fwd[k] = c[3 + k];
-        cam.right[k] = c[6 + k];
-        cam.up[k] = c[9 + k];
-    }
-    cam.fov_scale = c[12];
+    const CameraArgs cam = read_camera(argv[2]);
     const uint32_t w = (uint32_t)std::atoi(argv[4]), h = (uint32_t)std::atoi(argv[5]), aa = (uint32_t)std::atoi(argv[6]);
     const float lens = std::strtof(argv[7], nullptr), focus = std::strtof(argv[8], nullptr);
     // Payloads the device reads by address (the GI probe cubes, each SDF volume's samples) are
     // not in the tape's bytes: point the header and the volume records at host copies.
     TapeHeader* H = reinterpret_cast<TapeHeader*>(tape_words.data());
     std::vector<std::vector<float4>> payloads;
-    for (int k = 9; k < argc; ++k) {
-        FILE* fp = std::fopen(argv[k], "rb");
-        std::vector<float4> buf(1 << 20);
-        size_t nb = std::fread(buf.data(), 1, buf.size() * sizeof(float4), fp);
-        std::fclose(fp);
-        buf.resize((nb + sizeof(float4) - 1) / sizeof(float4));
-        payloads.push_back(std::move(buf));
-    }
+    for (int k = 9; k < argc; ++k) payloads.push_back(read_words(argv[k]));
     size_t next = 0;
     if (H->gi_nx) H->gi_cubes = payloads.at(next++).data();
     DevVolume* vols = reinterpret_cast<DevVolume*>(reinterpret_cast<unsigned char*>(H) + H->off_volumes);
@@ -684,7 +644,7 @@ def _build_frame_harness(scene, work):
                                    "\n}}\n" + FRAME_MAIN)
     exe = work / "frame"
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-include", SHIM, "-include", STUBS, str(work / "main.cpp"), "-o", str(exe)],
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(work / "main.cpp"), "-o", str(exe)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     return exe
@@ -875,7 +835,7 @@ def test_gi_bake_equals_oracle_on_host(name, dims, samples, tmp_path):
     (tmp_path / "main.cpp").write_text(defines + '#include "shade_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
                                        "\n}}\n" + GI_MAIN)
     lib_path = tmp_path / "libhostgi.so"
-    flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-fPIC", "-I", CUDA_INCLUDE, "-I", CSRC]
+    flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-fPIC", "-I", CUDA_INCLUDE, "-I", CSRC, "-I", HOST_DIR]
     r = subprocess.run(["g++"] + flags + ["-c", os.path.join(CSRC, "lower.cpp"), "-o", str(tmp_path / "lower.o")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -903,6 +863,7 @@ def test_gi_bake_equals_oracle_on_host(name, dims, samples, tmp_path):
 
 
 AOV_MAIN = r"""
+#include "host_io.h"
 using namespace mm3e;
 using namespace mm3e::wave;
 // An AOV frame as the device runs it: the pixel-centre march (SRC_CENTER), the AO pass in the AO
@@ -942,25 +903,9 @@ template <class FP> static void aov(const unsigned char* tape, const CameraArgs&
     for (uint32_t i = 0; i < n; ++i) aov_slot(a, i, out.data());
 }
 int main(int argc, char** argv) {
-    FILE* ft = std::fopen(argv[1], "rb");
-    std::vector<float4> tape_words(1 << 20);
-    size_t nt = std::fread(tape_words.data(), 1, tape_words.size() * sizeof(float4), ft);
-    std::fclose(ft);
-    (void)nt;
+    std::vector<float4> tape_words = read_words(argv[1]);
     const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
-    float c[13];
-    FILE* fc = std::fopen(argv[2], "rb");
-    size_t nc = std::fread(c, sizeof(float), 13, fc);
-    std::fclose(fc);
-    (void)nc;
-    CameraArgs cam;
-    for (int k = 0; k < 3; ++k) {
-        cam.eye[k] = c[k];
-        cam.fwd[k] = c[3 + k];
-        cam.right[k] = c[6 + k];
-        cam.up[k] = c[9 + k];
-    }
-    cam.fov_scale = c[12];
+    const CameraArgs cam = read_camera(argv[2]);
     const uint32_t w = (uint32_t)std::atoi(argv[4]), h = (uint32_t)std::atoi(argv[5]), mode = (uint32_t)std::atoi(argv[6]);
     std::vector<float4> out;
     FILE* fo = std::fopen(argv[3], "wb");
@@ -1002,7 +947,7 @@ def test_aov_modes_equal_oracle_on_host(name, tmp_path):
                                                    ns + "\n}}\n" + AOV_MAIN)
             exes[src] = tmp_path / f"aov{k}"
             r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I",
-                                CUDA_INCLUDE, "-I", CSRC, "-include", SHIM, "-include", STUBS,
+                                CUDA_INCLUDE, "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS,
                                 str(tmp_path / f"main{k}.cpp"), "-o", str(exes[src])], capture_output=True, text=True)
             assert r.returncode == 0, r.stderr[-3000:]
         exe = exes[src]
