@@ -219,6 +219,31 @@ def test_valid_csg_accepted_and_tape_sized():
     assert n.value > 0 and n.value % 16 == 0
 
 
+def test_scene_tape_bytes_on_the_host():
+    """mm3e_scene_tape: the lowered tape without a device. Its size equals mm3e_scene_tape_bytes,
+    it starts with the tape header (magic, byte count), lowering is deterministic, a short buffer
+    takes a prefix, a NULL buffer only reports the size, and an invalid scene is rejected."""
+    s, _ = scenes.canonical_asset_scene()
+    h = s.desc()
+    n = C.c_size_t()
+    assert lib().mm3e_scene_tape_bytes(h.ptr, C.byref(n)) == abi.OK
+    size = C.c_size_t()
+    assert lib().mm3e_scene_tape(h.ptr, None, 0, C.byref(size)) == abi.OK
+    assert size.value == n.value
+    buf = (C.c_uint8 * n.value)()
+    assert lib().mm3e_scene_tape(h.ptr, buf, n.value, C.byref(size)) == abi.OK
+    tape = bytes(buf)
+    magic, nbytes = np.frombuffer(tape[:8], np.uint32)
+    assert magic == 0x4D334554 and nbytes == n.value
+    assert mm3e_cuda.scene_tape(s) == tape
+    short = (C.c_uint8 * 64)()
+    assert lib().mm3e_scene_tape(h.ptr, short, 64, C.byref(size)) == abi.OK
+    assert bytes(short) == tape[:64] and size.value == n.value
+    bad, _ = scenes.canonical_scene()
+    bad.materials = []
+    assert lib().mm3e_scene_tape(bad.desc().ptr, None, 0, C.byref(size)) == abi.ERR_INVALID
+
+
 def test_context_without_gpu_fails_cleanly():
     try:
         import torch
