@@ -1,7 +1,7 @@
 // Host stand-ins for the device-only builtins that march_kernels.cuh references, so that its
-// per-lane march state machine (m_start / m_step) compiles as plain C++ and a host loop can drive
-// it ray by ray (tests/test_spec_host_cpu.py). The stand-ins serve only code that the host loop
-// never runs (the persistent loop's warp-aggregated refill, the tape staging). Test
+// per-lane march state machine (m_start / m_step) and the other kernels' bodies compile as plain
+// C++ and a host loop can drive them item by item (tests/test_spec_host_cpu.py): one thread of one
+// block, so a warp vote sees one lane and an atomic is a plain read-modify-write. Test
 // infrastructure only.
 #pragma once
 struct HostDim3 { unsigned x = 0, y = 0, z = 0; };
@@ -15,3 +15,8 @@ inline unsigned atomicAdd(unsigned* p, unsigned v) { unsigned o = *p; *p += v; r
 inline size_t __cvta_generic_to_shared(const void*) { return 0; }
 inline void __nanosleep(unsigned) {}
 inline unsigned atomicOr(unsigned* p, unsigned v) { unsigned o = *p; *p |= v; return o; }
+inline unsigned long long atomicMin(unsigned long long* p, unsigned long long v) {
+    unsigned long long o = *p;
+    if (v < o) *p = v;
+    return o;
+}

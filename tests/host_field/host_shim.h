@@ -28,6 +28,12 @@ inline int __float2int_rz(float x) {
     if (x <= -2147483648.0f) return (-2147483647 - 1);
     return (int)x;
 }
+// Truncation toward zero to an unsigned integer, saturating, NaN -> 0.
+inline unsigned __float2uint_rz(float x) {
+    if (!(x > 0.0f)) return 0u;
+    if (x >= 4294967296.0f) return 4294967295u;
+    return (unsigned)x;
+}
 // fl_up(a + b): the binary64 sum and its exact error (Knuth's two-sum) pick the smallest binary32
 // value at or above the exact sum.
 inline float __fadd_ru(float a, float b) {
@@ -43,6 +49,12 @@ template <class T> inline T __ldg(const T* p) { return *p; }
 using std::isfinite;
 using std::isnan;
 using std::signbit;
+#ifndef __launch_bounds__
+#define __launch_bounds__(...)
+#endif
+#ifndef __grid_constant__
+#define __grid_constant__
+#endif
 #ifndef __noinline__
 #define __noinline__ __attribute__((noinline))
 #endif

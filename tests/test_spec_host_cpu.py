@@ -19,7 +19,8 @@ import pytest
 import mm3e_cuda
 import oracle_py
 from mm3e_cuda import abi, scenes
-from mm3e_cuda.scene import GiVolume, Material, Object, Prim, Scene, SdfVolume, Transform, directional, look_at
+from mm3e_cuda.scene import (GiVolume, Material, Object, Prim, Scene, SdfVolume, Transform, directional, look_at,
+                             orbit_camera)
 from field_scenes import csg_zoo_scene, noncons_scene, planes_scene, smooth_chain_scene, unbounded_mix_scene
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -442,14 +443,14 @@ def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
 
 FRAME_MAIN = r"""
 #include "host_io.h"
+#include "host_passes.h"
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
 using namespace mm3e;
 using namespace mm3e::wave;
-// One frame through the device pass sequence, pass by pass and item by item: the march of each
-// level (camera samples, then the reflection queue), the reflection rays of the next level, AO,
-// soft shadows, shading, and at the end the resolve of every pixel slot.
+// One frame through the device pass sequence (host_passes.h), then the resolve of every pixel
+// slot.
 template <class FP>
 static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, uint32_t h, uint32_t aa, float lens,
                   float focus, std::vector<float4>& hdr, std::vector<float4>& fg) {
@@ -470,70 +471,17 @@ static void frame(const unsigned char* tape, const CameraArgs& cam, uint32_t w, 
     const bool film = lens >= 0.0f;  // film.rs render_film: thin-lens samples, coverage, foreground
     J.lens_radius = film ? lens : 0.0f;
     J.focus_distance = focus;
-    const uint32_t ns = J.n_samples, nl = H.n_lights, levels = H.bounces + 1u;
-    std::vector<float4> q_o(ns), q_d(ns), nq_o(ns), nq_d(ns), term(ns), lvl((size_t)2 * ns * levels);
-    // Hit records per level: the primary level's stay for the resolve (film coverage), as the
-    // device keeps them apart from the reflection levels' buffers.
-    std::vector<std::vector<float4>> h_n(levels, std::vector<float4>(ns));
-    std::vector<std::vector<uint2>> h_m(levels, std::vector<uint2>(ns));
-    std::vector<std::vector<float>> occ(levels, std::vector<float>(ns)),
-        shadow(levels, std::vector<float>((size_t)ns * (nl ? nl : 1u)));
-    hdr.assign(J.n_pixels, make_float4(0.f, 0.f, 0.f, 0.f));
-    fg.assign(J.n_pixels, make_float4(0.f, 0.f, 0.f, 0.f));
-    uint32_t nq_count = 0;
+    HostFrame F;
+    F.init(J.n_samples, H.bounces + 1u, H.n_lights, J.n_pixels);
     WaveArgs a{};
     a.job0 = J;
     a.n_jobs = 1;
-    a.cap = ns;
-    a.lights_max = nl;
     a.tile_wlog = wlog;
-    a.b = WaveBuffers{q_o.data(), q_d.data(), nullptr, nullptr, nullptr, nullptr, nq_o.data(),
-                      nq_d.data(), &nq_count, lvl.data(), term.data(), hdr.data(), fg.data()};
     a.film = film ? 1u : 0u;
-    const bool ao = (H.flags & SF_AO) && H.ao_samples > 0;
-    const bool shadows = (H.flags & SF_SHADOWS) && H.shadow_steps > 0 && nl > 0;
-    uint32_t n = ns;
-    for (uint32_t level = 0; level < levels && n > 0; ++level) {
-        a.level = level;
-        a.src = level == 0 ? SRC_SAMPLES : SRC_QUEUE;
-        a.b.h_n = h_n[level].data();
-        a.b.h_m = h_m[level].data();
-        a.b.occ = occ[level].data();
-        a.b.shadow = shadow[level].data();
-        a.n_items = n;
-        for (uint32_t i = 0; i < n; ++i) {
-            MLane L;
-            L.item = i;
-            L.phase = M_IDLE;
-            LaneTape<TM_MULTI> LT;
-            LT.p = tape;
-            if (m_start<TM_MULTI, FP>(L, LT, a))
-                while (L.phase != M_IDLE) m_step<TM_MULTI, FP>(L, LT, a);
-        }
-        nq_count = 0;
-        if (level + 1 < levels)
-            for (uint32_t i = 0; i < n; ++i) reflect_slots(a, i, true);
-        if (ao)
-            for (uint32_t i = 0; i < n; ++i) ao_slot<FP>(a, i);
-        if (shadows)
-            for (uint32_t i = 0; i < n * nl; ++i) {
-                SLane S;
-                S.item = i;
-                LaneTape<TM_MULTI> LT;
-                LT.p = tape;
-                if (s_start<TM_MULTI, FP>(S, LT, a, n))
-                    while (S.item != NIL) s_step<TM_MULTI, FP>(S, LT, a);
-            }
-        for (uint32_t i = 0; i < n; ++i) shade_slots(a, i, true);
-        for (uint32_t i = 0; i < nq_count; ++i) {
-            q_o[i] = nq_o[i];
-            q_d[i] = nq_d[i];
-        }
-        n = nq_count;
-    }
-    a.b.h_n = h_n[0].data();
-    a.b.h_m = h_m[0].data();
+    host_levels<FP>(a, tape, SRC_SAMPLES, J.n_samples, F);
     for (uint32_t s = 0; s < J.n_slots; ++s) resolve_slot(a, s, 1u);
+    hdr = F.hdr;
+    fg = F.fg;
 }
 int main(int argc, char** argv) {
     std::vector<float4> tape_words = read_words(argv[1]);
@@ -1026,3 +974,165 @@ def test_frame_at_setting_edges_equals_oracle_on_host(tmp_path):
             if bad:
                 failed[(edge, label)] = bad
     assert not failed, failed
+
+
+PREVIEW_MAIN = r"""
+#include "host_io.h"
+#include "host_passes.h"
+using namespace mm3e;
+using namespace mm3e::wave;
+using namespace mm3e::preview;
+// The preview path as the device runs it (mm3e_render_gbuffer, mm3e_reproject): an aa-1 frame
+// without post packed into a G-buffer with its primary hits and the movers' tags; the forward
+// warp of that G-buffer into the new camera; the cheap row fill; and the hybrid re-render of the
+// warp's holes through the pass sequence (the holes' rays as the primary level's queue) and
+// their resolve. The kernels run as one thread of one block: each grid-stride loop visits every
+// item in order, and the row fill (one thread per row) runs row by row.
+template <class FP>
+static void run_preview(const unsigned char* tape, const CameraArgs& c0, const CameraArgs& c1, uint32_t w, uint32_t h,
+                    const std::vector<float>& movers, const std::vector<float>& deltas, FILE* fo) {
+    const uint32_t wlog = 3, n = w * h;
+    const TapeHeader& H = *tape_view(tape).h;
+    FrameJob J{};
+    J.tape = tape;
+    J.cam = c0;
+    J.width = w;
+    J.height = h;
+    J.aa = 1;
+    J.spp = 1;
+    J.tiles_x = (w + 7u) / 8u;
+    J.n_slots = J.tiles_x * ((h + 3u) / 4u) * 32u;
+    J.n_samples = J.n_slots;
+    J.n_pixels = n;
+    J.n_lights = H.n_lights;
+    HostFrame F;
+    F.init(J.n_samples, H.bounces + 1u, H.n_lights, n);
+    WaveArgs a{};
+    a.job0 = J;
+    a.n_jobs = 1;
+    a.tile_wlog = wlog;
+    host_levels<FP>(a, tape, SRC_SAMPLES, J.n_samples, F);
+    for (uint32_t s = 0; s < J.n_slots; ++s) resolve_slot(a, s, 1u);
+    std::vector<uchar4> color(n);
+    std::vector<float> depth(n);
+    std::vector<int32_t> obj(n);
+    k_gbuffer_pack(a, J.n_slots, reinterpret_cast<const float4*>(movers.data()), (uint32_t)(movers.size() / 4),
+                   color.data(), depth.data(), obj.data());
+    std::fwrite(color.data(), sizeof(uchar4), n, fo);
+    std::fwrite(depth.data(), sizeof(float), n, fo);
+    std::fwrite(obj.data(), sizeof(int32_t), n, fo);
+    // forward warp, then the cheap fill
+    std::vector<unsigned long long> keys(n, ~0ull);
+    std::vector<uchar4> warped(n), cheap(n);
+    std::vector<unsigned char> filled(n), cheap_filled(n);
+    k_warp_keys(c0, c1, w, h, depth.data(), obj.data(), deltas.data(), (uint32_t)(deltas.size() / 3), keys.data());
+    k_warp_apply(n, keys.data(), color.data(), warped.data(), filled.data());
+    cheap = warped;
+    cheap_filled = filled;
+    for (uint32_t y = 0; y < h; ++y) {
+        blockIdx.x = y;
+        k_row_fill(w, h, cheap.data(), cheap_filled.data());
+    }
+    blockIdx.x = 0;
+    std::fwrite(cheap.data(), sizeof(uchar4), n, fo);
+    // hybrid: the holes' rays through the pass sequence, then their resolve into the warped frame
+    HostFrame G;
+    G.init(n, H.bounces + 1u, H.n_lights, n);
+    std::vector<uint32_t> hole_pix(n);
+    uint32_t count = 0;
+    k_hole_rays(c1, w, h, filled.data(), G.q_o[0].data(), G.q_d[0].data(), hole_pix.data(), &count);
+    WaveArgs b{};
+    b.job0 = J;
+    b.job0.cam = c1;
+    b.n_jobs = 1;
+    b.tile_wlog = wlog;
+    host_levels<FP>(b, tape, SRC_QUEUE, count, G);
+    b.n_items = n;
+    std::vector<uchar4> hybrid = warped;
+    k_hole_resolve(b, &count, hole_pix.data(), hybrid.data());
+    std::fwrite(hybrid.data(), sizeof(uchar4), n, fo);
+}
+int main(int argc, char** argv) {
+    blockDim.x = 1;
+    gridDim.x = 1;
+    std::vector<float4> tape_words = read_words(argv[1]);
+    const unsigned char* tape = reinterpret_cast<const unsigned char*>(tape_words.data());
+    const CameraArgs c0 = read_camera(argv[2]), c1 = read_camera(argv[3]);
+    const uint32_t w = (uint32_t)std::atoi(argv[5]), h = (uint32_t)std::atoi(argv[6]);
+    const std::vector<float> movers = read_floats(argv[7]), deltas = read_floats(argv[8]);
+    FILE* fo = std::fopen(argv[4], "wb");
+    run_preview<InterpField>(tape, c0, c1, w, h, movers, deltas, fo);
+    run_preview<spec::Field_>(tape, c0, c1, w, h, movers, deltas, fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+def _cam_bin(cam, path):
+    np.array(list(cam.eye) + list(cam.forward) + list(cam.right) + list(cam.up) + [cam.fov_scale],
+             np.float32).tofile(path)
+
+
+PREVIEW_CASES = {  # scene, movers (x, y, z, radius), per-mover deltas
+    "demo": (lambda: scenes.demo_scene(), [(-1.2, 1.0, 0.0, 1.3), (1.2, 0.6, 0.0, 0.8)], [(0.3, -0.2, 0.1), (0.0, 0.4, 0.0)]),
+    "spheres": (lambda: scenes.spheres_scene(64, 36), [(0.0, 1.0, 0.0, 1.0), (-2.2, 1.0, 0.0, 1.0)], [(1.5, 0.0, 0.0)]),
+    "gallery": (lambda: scenes.gallery_scene(64, 36), [], []),
+    "hero_aa2_b2": (lambda: scenes.hero_scene(48, 27, 2, 2), [(0.0, 1.0, 0.0, 1.0)], [(0.0, 0.0, 0.0)]),
+}
+
+
+@pytest.mark.parametrize("name", list(PREVIEW_CASES))
+def test_preview_path_equals_oracle_on_host(name, tmp_path):
+    """The preview path (reproject_kernels.cuh: k_gbuffer_pack, k_warp_keys / k_warp_apply,
+    k_row_fill, k_hole_rays, k_hole_resolve; lib.rs:951-1080, reproject.rs:55-146) with the
+    pass sequence of host_passes.h, compiled for the host over both fields, against the oracle's
+    render_gbuffer, reproject and reproject_hybrid: the G-buffer's colour, depth and object tags,
+    the cheap reprojection and the hybrid frame, all bit for bit."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    make, movers, deltas = PREVIEW_CASES[name]
+    scene, _ = make()
+    c0 = orbit_camera((0.0, 0.8, 0.3), 7.0, 0.5, 0.3, radians(52.0))
+    c1 = orbit_camera((0.0, 0.8, 0.3), 7.0, 0.62, 0.3, radians(52.0))
+    src = mm3e_cuda.spec_source(scene)
+    ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
+    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+    (tmp_path / "main.cpp").write_text(defines + '#include "shade_kernels.cuh"\n#include "reproject_kernels.cuh"\n'
+                                       'namespace mm3e { namespace spec {\n' + ns + "\n}}\n" + PREVIEW_MAIN)
+    exe = tmp_path / "preview"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
+    _cam_bin(c0, tmp_path / "c0.bin")
+    _cam_bin(c1, tmp_path / "c1.bin")
+    np.array(movers, np.float32).reshape(-1).tofile(tmp_path / "movers.bin")
+    np.array(deltas, np.float32).reshape(-1).tofile(tmp_path / "deltas.bin")
+    d = scene.desc().desc
+    w, h = d.width, d.height
+    subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "c0.bin"), str(tmp_path / "c1.bin"),
+                    str(tmp_path / "out.bin"), str(w), str(h), str(tmp_path / "movers.bin"), str(tmp_path / "deltas.bin")],
+                   check=True)
+    raw = np.fromfile(tmp_path / "out.bin", np.uint8)
+    n = w * h
+    per = n * 4 * 3 + n * 4 * 2
+    g = oracle_py.render_gbuffer(scene.desc(), c0, movers=movers)
+    cheap = oracle_py.reproject(g, c0, c1, deltas)
+    hybrid = oracle_py.reproject(g, c0, c1, deltas, hybrid_handle=scene.desc())
+    holes = ~oracle_py.reproject_filled(g, c0, c1, deltas).astype(bool)
+    assert holes.any() and (~holes).any()
+    assert np.isfinite(g["depth"]).any() and (movers == [] or (g["obj"] >= 0).any())
+    for k, label in enumerate(("interpreter", "specialised")):
+        blk = raw[k * per:(k + 1) * per]
+        color = blk[:n * 4].reshape(h, w, 4)
+        depth = blk[n * 4:n * 8].view(np.float32).reshape(h, w)
+        obj = blk[n * 8:n * 12].view(np.int32).reshape(h, w)
+        got_cheap = blk[n * 12:n * 16].reshape(h, w, 4)
+        got_hybrid = blk[n * 16:n * 20].reshape(h, w, 4)
+        assert np.array_equal(color, g["color"]), (label, "colour", int((color != g["color"]).any(-1).sum()))
+        assert np.array_equal(depth.view(np.uint32), g["depth"].view(np.uint32)), (label, "depth")
+        assert np.array_equal(obj, g["obj"]), (label, "objects")
+        assert np.array_equal(got_cheap, cheap), (label, "cheap", int((got_cheap != cheap).any(-1).sum()))
+        assert np.array_equal(got_hybrid, hybrid), (label, "hybrid", int((got_hybrid != hybrid).any(-1).sum()))
