@@ -440,21 +440,59 @@ def render_linear(scene, camera, ctx=None):
     return CompiledScene(ctx or default_context(), scene).render_linear(camera)
 
 
-def to_rgba8(fb):
-    """Framebuffer::to_rgba8 over black (framebuffer.rs:308-319) for an RGBA f32 frame."""
+def _flatten_u8(fb, background):
+    """Straight alpha over `background` and the u8 quantisation of Framebuffer's encoders
+    (framebuffer.rs:84-91,103-111,117-125): per channel (clamp(c * a + bg * (1 - a), 0, 1) * 255
+    + 0.5) as u8, a = clamp(alpha, 0, 1), every step in binary32; a NaN channel gives 0, as Rust's
+    `as u8` does. Returns (..., 3) uint8 RGB."""
     fb = np.asarray(fb, dtype=np.float32)
-    a = np.clip(fb[..., 3:4], 0.0, 1.0).astype(np.float32)
-    rgb = (fb[..., :3] * a + np.float32(0.0) * (np.float32(1.0) - a)).astype(np.float32)
-    q = (np.clip(rgb, 0.0, 1.0) * np.float32(255.0) + np.float32(0.5)).astype(np.float32)
-    out = np.empty(fb.shape[:-1] + (4,), np.uint8)
-    out[..., :3] = np.floor(q).astype(np.uint8)
+    bg = np.asarray(background, dtype=np.float32)[:3]
+    with np.errstate(invalid="ignore"):
+        a = np.clip(fb[..., 3:4], np.float32(0.0), np.float32(1.0)).astype(np.float32)
+        rgb = (fb[..., :3] * a + bg * (np.float32(1.0) - a)).astype(np.float32)
+        q = (np.clip(rgb, np.float32(0.0), np.float32(1.0)) * np.float32(255.0) + np.float32(0.5)).astype(np.float32)
+        q = np.where(np.isnan(q), np.float32(0.0), q)
+    return np.floor(q).astype(np.uint8)
+
+
+def to_rgba8(fb, background=(0.0, 0.0, 0.0, 1.0)):
+    """Framebuffer::to_rgba8 (framebuffer.rs:102-113): opaque RGBA8 over `background` (black by
+    default) for an (h, w, 4) RGBA f32 frame."""
+    rgb = _flatten_u8(fb, background)
+    out = np.empty(rgb.shape[:-1] + (4,), np.uint8)
+    out[..., :3] = rgb
     out[..., 3] = 255
     return out
 
 
+def to_u32(fb, background=(0.0, 0.0, 0.0, 1.0)):
+    """Framebuffer::to_u32 (framebuffer.rs:115-127): opaque 0x00RRGGBB pixels, (h, w) uint32."""
+    rgb = _flatten_u8(fb, background).astype(np.uint32)
+    return (rgb[..., 0] << 16) | (rgb[..., 1] << 8) | rgb[..., 2]
+
+
+def to_bmp(fb, background=(0.0, 0.0, 0.0, 1.0)):
+    """Framebuffer::to_bmp (framebuffer.rs:54-99): a 24-bit bottom-up BMP (14-byte file header,
+    40-byte info header at 2835 pixels per metre, BGR rows padded to 4 bytes), as bytes."""
+    rgb = _flatten_u8(fb, background)
+    h, w = rgb.shape[:2]
+    pad = (4 - (w * 3) % 4) % 4
+    row_bytes = w * 3 + pad
+    pixel_bytes = row_bytes * h
+    file_size = 54 + pixel_bytes
+    if file_size > 0xFFFFFFFF:
+        raise ValueError("BMP file too large for 32-bit BMP header")
+    header = (b"BM" + np.array([file_size, 0, 54, 40], "<u4").tobytes() + np.array([w, h], "<i4").tobytes() +
+              np.array([1, 24], "<u2").tobytes() + np.array([0, pixel_bytes], "<u4").tobytes() +
+              np.array([2835, 2835], "<i4").tobytes() + np.array([0, 0], "<u4").tobytes())
+    rows = np.zeros((h, row_bytes), np.uint8)
+    rows[:, :w * 3] = rgb[::-1, :, ::-1].reshape(h, w * 3)
+    return header + rows.tobytes()
+
+
 __all__ = [
     "abi", "lib", "NativeLibraryMissing", "RenderError", "Context", "CompiledScene", "CudaRenderer", "render",
-    "render_linear", "validate", "to_rgba8", "Scene", "Object", "Prim", "Material", "Light", "directional", "Marcher",
+    "render_linear", "validate", "to_rgba8", "to_u32", "to_bmp", "Scene", "Object", "Prim", "Material", "Light", "directional", "Marcher",
     "Post", "Transform", "Expr", "SdfVolume", "GiVolume", "DynSphere", "look_at", "orbit_camera", "mat3_from_euler",
     "quat_to_mat3", "normalize_f32", "radians",
 ]
