@@ -761,7 +761,7 @@ std::string spec_source(const std::vector<unsigned char>& blob, uint32_t block, 
             if (any_noncons)
                 os << "        if (bnc) acc = walk_" << s << "(T, p, acc);\n        else acc = Field{bd, bm};\n";
             else
-                os << "        acc = Field{bd, bm};\n";
+                os << "        (void)bnc;  // no member can undercut its bound\n        acc = Field{bd, bm};\n";
         } else {
             os << "        acc = walk_" << s << "(T, p, acc);\n";
         }
