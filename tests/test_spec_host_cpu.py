@@ -1136,3 +1136,70 @@ def test_preview_path_equals_oracle_on_host(name, tmp_path):
         assert np.array_equal(obj, g["obj"]), (label, "objects")
         assert np.array_equal(got_cheap, cheap), (label, "cheap", int((got_cheap != cheap).any(-1).sum()))
         assert np.array_equal(got_hybrid, hybrid), (label, "hybrid", int((got_hybrid != hybrid).any(-1).sum()))
+
+
+def _random_case(rng):
+    """A seeded random scene (procedural, CSG zoo, unbounded mix, non-conservative, smooth chain,
+    gallery or hero), random scene and marcher settings, and a random orbit camera."""
+    kind = rng.choice(["proc", "proc", "csg", "unb", "nc", "sc", "gallery", "hero"])
+    w, h = rng.choice([(40, 24), (33, 17), (48, 27)])
+    if kind == "proc":
+        s, cam = scenes.procedural_scene(rng.randrange(1000), w, h)
+    elif kind == "csg":
+        s, cam = csg_zoo_scene(rng.randrange(50), w, h)
+    elif kind == "unb":
+        s, cam = unbounded_mix_scene(rng.randrange(50), w, h)
+    elif kind == "nc":
+        s, cam = noncons_scene(rng.randrange(50), w, h)
+    elif kind == "sc":
+        s, cam = smooth_chain_scene(rng.randrange(2, 9), w, h)
+    elif kind == "gallery":
+        s, cam = scenes.gallery_scene(w, h)
+    else:
+        s, cam = scenes.hero_scene(w, h, 2, 2)
+    choices = {"aa": [1, 2, 3], "bounces": [0, 1, 2, 3], "step_scale": [0.5, 0.8, 1.0, 1.2, 1.6],
+               "secant": [False, True], "subitize": [0.0, 0.2, 0.6], "lod_footprint": [0.0, 0.001, 0.006],
+               "eps": [0.0, 0.0001, 0.002, 0.02], "max_steps": [8, 32, 96, 256], "shadow_steps": [0, 3, 16, 96],
+               "ao_samples": [0, 1, 2, 8], "normal_h": [0.0, 0.0002, 0.01], "max_dist": [5.0, 30.0, 500.0],
+               "fog_density": [0.0, 0.05, 0.3], "shadows": [False, True], "ao": [False, True]}
+    settings = {k: rng.choice(v) for k, v in choices.items() if rng.random() < 0.35}
+    for key, value in settings.items():
+        setattr(s if hasattr(s, key) else s.marcher, key, value)
+    if rng.random() < 0.5:
+        cam = orbit_camera((rng.uniform(-1, 1), rng.uniform(0, 1.5), rng.uniform(-1, 1)), rng.uniform(2.0, 12.0),
+                           rng.uniform(-3.1, 3.1), rng.uniform(-0.4, 1.2), radians(rng.uniform(25, 80)))
+    return kind, settings, s, cam
+
+
+def test_random_configurations_equal_oracle_on_host(tmp_path):
+    """Eight seeded random configurations (scene kind, scene and marcher settings, camera), whole
+    frames through the device pass sequence over both fields against the oracle's render, bit for
+    bit; the odd ones also in film mode with a random thin lens against render_film."""
+    import random
+    from concurrent.futures import ThreadPoolExecutor
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    cases = []
+    for k in range(8):
+        rng = random.Random(20261204 + k)
+        kind, settings, s, cam = _random_case(rng)
+        lens, focus = (rng.choice([0.02, 0.1, 0.4]), rng.choice([0.5, 3.0, 7.0, 20.0])) if k % 2 else (-1.0, 1.0)
+        work = tmp_path / str(k)
+        work.mkdir()
+        cases.append((kind, settings, s, cam, work, lens, focus))
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+        exes = list(pool.map(lambda c: _build_frame_harness(c[2], c[4]), cases))
+    failed = []
+    for (kind, settings, s, cam, work, lens, focus), exe in zip(cases, exes):
+        hdr, fg = _run_frame_harness(exe, s, cam, work, lens, focus)
+        if lens < 0:
+            _, ref = oracle_py.render(s.desc(), cam, threads=2, want_hdr=True)
+            pairs = [(hdr[j, :, :, :3], ref) for j in range(2)]
+        else:
+            r = oracle_py.render_film(s.desc(), cam, lens, focus, threads=2)
+            pairs = [p for j in range(2) for p in ((hdr[j, :, :, :3], r["beauty"]), (hdr[j, :, :, 3], r["alpha"]),
+                                                   (fg[j, :, :, :3], r["foreground"]))]
+        bad = [int((np.ascontiguousarray(g).view(np.uint32) != w_.view(np.uint32)).sum()) for g, w_ in pairs]
+        if any(bad):
+            failed.append((kind, settings, lens, focus, bad))
+    assert not failed, failed
