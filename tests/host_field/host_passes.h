@@ -51,15 +51,15 @@ struct HostFrame {
     }
 };
 
-// Every level of one pass sequence over `tape`: level 0 takes `n0` items from `src0` (the jobs'
-// camera samples, or a queue already in F.q_o[0] / F.q_d[0]). Leaves `a` bound to level 0.
+// Every level of one pass sequence: level 0 takes `n0` items from `src0` (the jobs' camera
+// samples, or a queue already in F.q_o[0] / F.q_d[0]); the AO and shadow passes run when `ao` /
+// `shadows` say so (for a job table: when any job needs them). `tape` is the lanes' first tape
+// (each item then takes its own job's). Leaves `a` bound to level 0.
 template <class FP>
-void host_levels(mm3e::WaveArgs& a, const unsigned char* tape, uint32_t src0, uint32_t n0, HostFrame& F) {
+void host_levels_with(mm3e::WaveArgs& a, const unsigned char* tape, uint32_t src0, uint32_t n0, HostFrame& F, bool ao,
+                      bool shadows) {
     using namespace mm3e;
     using namespace mm3e::wave;
-    const TapeHeader& H = *tape_view(tape).h;
-    const bool ao = (H.flags & SF_AO) && H.ao_samples > 0;
-    const bool shadows = (H.flags & SF_SHADOWS) && H.shadow_steps > 0 && F.nl > 0;
     uint32_t n = n0;
     for (uint32_t level = 0; level < F.levels && n > 0; ++level) {
         F.bind(a, level);
@@ -93,4 +93,13 @@ void host_levels(mm3e::WaveArgs& a, const unsigned char* tape, uint32_t src0, ui
         n = F.nq_count;
     }
     F.bind(a, 0);
+}
+
+// One scene's pass sequence: its AO and shadow passes run as the engine's plan decides.
+template <class FP>
+void host_levels(mm3e::WaveArgs& a, const unsigned char* tape, uint32_t src0, uint32_t n0, HostFrame& F) {
+    using namespace mm3e;
+    const TapeHeader& H = *tape_view(tape).h;
+    host_levels_with<FP>(a, tape, src0, n0, F, (H.flags & SF_AO) && H.ao_samples > 0,
+                         (H.flags & SF_SHADOWS) && H.shadow_steps > 0 && F.nl > 0);
 }

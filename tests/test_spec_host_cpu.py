@@ -1203,3 +1203,106 @@ def test_random_configurations_equal_oracle_on_host(tmp_path):
         if any(bad):
             failed.append((kind, settings, lens, focus, bad))
     assert not failed, failed
+
+
+BATCH_MAIN = r"""
+#include "host_io.h"
+#include "host_passes.h"
+using namespace mm3e;
+using namespace mm3e::wave;
+// One wave of the batched form (mm3e_render_batch): a device-style job table of scenes with
+// their own tapes, cameras and sizes, laid out as the batch engine lays it out (each job's
+// samples, pixel slots and pixels after the previous job's), run as one pass sequence through
+// the tape interpreter, then the resolve of every job's pixel slots.
+int main(int argc, char** argv) {
+    const uint32_t wlog = 3, nj = (uint32_t)std::atoi(argv[2]);
+    std::vector<std::vector<float4>> tapes(nj);
+    std::vector<FrameJob> jobs(nj);
+    JobTotals tot{nj, 0, 0, 0};
+    uint32_t levels = 1, lights = 0;
+    bool ao = false, shadows = false;
+    for (uint32_t k = 0; k < nj; ++k) {
+        tapes[k] = read_words(argv[3 + 4 * k]);
+        const unsigned char* tape = reinterpret_cast<const unsigned char*>(tapes[k].data());
+        const TapeHeader& H = *tape_view(tape).h;
+        FrameJob& J = jobs[k];
+        J = FrameJob{};
+        J.tape = tape;
+        J.cam = read_camera(argv[4 + 4 * k]);
+        J.width = (uint32_t)std::atoi(argv[5 + 4 * k]);
+        J.height = (uint32_t)std::atoi(argv[6 + 4 * k]);
+        J.aa = H.aa;
+        J.spp = H.aa * H.aa;
+        J.tiles_x = (J.width + 7u) / 8u;
+        J.n_slots = J.tiles_x * ((J.height + 3u) / 4u) * 32u;
+        J.n_samples = J.n_slots * J.spp;
+        J.n_pixels = J.width * J.height;
+        J.n_lights = H.n_lights;
+        J.sample_base = tot.n_samples;
+        J.slot_base = tot.n_slots;
+        J.pixel_base = tot.n_pixels;
+        tot.n_samples += J.n_samples;
+        tot.n_slots += J.n_slots;
+        tot.n_pixels += J.n_pixels;
+        levels = levels > H.bounces + 1u ? levels : H.bounces + 1u;
+        lights = lights > H.n_lights ? lights : H.n_lights;
+        ao = ao || ((H.flags & SF_AO) && H.ao_samples > 0);
+        shadows = shadows || ((H.flags & SF_SHADOWS) && H.shadow_steps > 0 && H.n_lights > 0);
+    }
+    HostFrame F;
+    F.init(tot.n_samples, levels, lights, tot.n_pixels);
+    WaveArgs a{};
+    a.job0 = jobs[0];
+    a.jobs = jobs.data();
+    a.totals = &tot;
+    a.n_jobs = nj;
+    a.tile_wlog = wlog;
+    host_levels_with<InterpField>(a, jobs[0].tape, SRC_SAMPLES, tot.n_samples, F, ao, shadows);
+    for (uint32_t s = 0; s < tot.n_slots; ++s) resolve_slot(a, s, nj);
+    FILE* fo = std::fopen(argv[1], "wb");
+    std::fwrite(F.hdr.data(), sizeof(float4), F.hdr.size(), fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+
+def test_batched_wave_equals_oracle_on_host(tmp_path):
+    """A batched wave (the job-table path of march_kernels.cuh and shade_kernels.cuh: the job of a
+    sample by binary search over the table, each lane's own job's tape, AO for AO jobs only, the
+    per-job resolve) over scenes of different kinds, sizes, AA, bounce and light counts, with and
+    without AO and shadows, compiled for the host and run as one pass sequence through the tape
+    interpreter: every job's HDR pixels equal the oracle's render of its scene bit for bit."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    jobs = [scenes.gallery_scene(40, 24), scenes.spheres_scene(33, 17), scenes.hero_scene(24, 20, 2, 2),
+            scenes.procedural_scene(3, 16, 9), _no_ao_samples_scene(), csg_zoo_scene(2, 20, 12),
+            scenes.procedural_scene(8, 1, 1), scenes.cornell_scene(20, 20)]
+    no_shadow, _ = jobs[1]
+    no_shadow.shadows = False
+    no_ao, _ = jobs[3]
+    no_ao.ao = False
+    (tmp_path / "main.cpp").write_text('#include "shade_kernels.cuh"\n' + BATCH_MAIN)
+    exe = tmp_path / "batch"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
+                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    args = [str(exe), str(tmp_path / "out.bin"), str(len(jobs))]
+    for k, (s, cam) in enumerate(jobs):
+        (tmp_path / f"tape{k}.bin").write_bytes(mm3e_cuda.scene_tape(s))
+        _cam_bin(cam, tmp_path / f"cam{k}.bin")
+        d = s.desc().desc
+        args += [str(tmp_path / f"tape{k}.bin"), str(tmp_path / f"cam{k}.bin"), str(d.width), str(d.height)]
+    subprocess.run(args, check=True)
+    hdr = np.fromfile(tmp_path / "out.bin", np.float32).reshape(-1, 4)
+    base = 0
+    for k, (s, cam) in enumerate(jobs):
+        d = s.desc().desc
+        n = d.width * d.height
+        got = np.ascontiguousarray(hdr[base:base + n, :3]).reshape(d.height, d.width, 3)
+        _, ref = oracle_py.render(s.desc(), cam, threads=2, want_hdr=True)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), \
+            (k, int((got.view(np.uint32) != ref.view(np.uint32)).any(axis=2).sum()), n)
+        base += n
+    assert base == len(hdr)
