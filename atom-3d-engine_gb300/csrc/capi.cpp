@@ -80,21 +80,6 @@ int cuda_fail(mm3e_ctx* c, cudaError_t e, const char* what) {
                 std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Gaussian kernel of post.rs:331-345 in binary32 (host libm expf, as the reference).
-std::vector<float> gaussian_kernel(uint32_t radius) {
-    int32_t r = (int32_t)(radius > 1 ? radius : 1);
-    float sigma = std::fmax((float)r / 2.0f, 1e-3f);
-    std::vector<float> k;
-    float sum = 0.0f;
-    for (int32_t i = -r; i <= r; ++i) {
-        float v = expf((float)(-(i * i)) / (2.0f * sigma * sigma));
-        k.push_back(v);
-        sum = sum + v;
-    }
-    for (auto& v : k) v = v / sum;
-    return k;
-}
-
 void fill_camera(CameraArgs& a, const mm3e_camera& c) {
     std::memcpy(a.eye, c.eye, 12);
     std::memcpy(a.fwd, c.forward, 12);

@@ -63,7 +63,6 @@ struct SceneCopy {
 int fail(mm3e_ctx* c, int code, const std::string& msg);
 int cuda_fail(mm3e_ctx* c, cudaError_t e, const char* what);
 void fill_camera(CameraArgs& a, const mm3e_camera& c);
-std::vector<float> gaussian_kernel(uint32_t radius);
 
 }  // namespace mm3e
 

@@ -390,6 +390,21 @@ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 }  // namespace
 
+// Gaussian kernel of post.rs:331-345 in binary32 (host libm expf, as the reference).
+std::vector<float> gaussian_kernel(uint32_t radius) {
+    int32_t r = (int32_t)(radius > 1 ? radius : 1);
+    float sigma = std::fmax((float)r / 2.0f, 1e-3f);
+    std::vector<float> k;
+    float sum = 0.0f;
+    for (int32_t i = -r; i <= r; ++i) {
+        float v = expf((float)(-(i * i)) / (2.0f * sigma * sigma));
+        k.push_back(v);
+        sum = sum + v;
+    }
+    for (auto& v : k) v = v / sum;
+    return k;
+}
+
 bool gi_setup(const mm3e_scene_desc& d, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t samples, GiSetup& out) {
     float inf = INFINITY;
     V lo{inf, inf, inf}, hi{-inf, -inf, -inf};

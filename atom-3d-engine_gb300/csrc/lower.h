@@ -42,6 +42,9 @@ int validate_dynamic(const mm3e_scene_desc& d, const mm3e_dyn_sphere* dyn, size_
 int lower_scene(const mm3e_scene_desc& d, const mm3e_dyn_sphere* dyn, size_t n_dyn, LoweredScene& out,
                 std::string& err);
 
+// Normalised Gaussian bloom weights of radius max(radius, 1): 2r + 1 taps (post.rs:331-345).
+std::vector<float> gaussian_kernel(uint32_t radius);
+
 // GI bake set-up (Scene::bake_gi_unchecked, lib.rs:668-682; gi.rs:38-72,192-203): probe grid
 // bounds from the objects' world bounding spheres padded by 1.5, the cell size, and the
 // per-face gather directions with their weights (axis first, then four 45-degree tilts).

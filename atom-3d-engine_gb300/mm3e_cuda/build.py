@@ -24,7 +24,7 @@ GENCODE = "arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["wavefront.cu", "noalloc.cu", "mesh_bake.cu", "reproject.cu"]
 CPP_SOURCES = ["lower.cpp", "capi.cpp", "engine.cpp", "batch.cpp", "mesh.cpp", "server.cpp", "spec.cpp", "spec_gen.cpp", "scene_io.cpp"]
-HEADERS = ["tape.h", "lower.h", "kernels.h", "device_math.cuh", "noalloc.h", "engine.h", "capi_internal.h", "batch.h", "mesh.h", "server.h", "march_kernels.cuh", "shade_kernels.cuh", "reproject_kernels.cuh", "spec.h"]
+HEADERS = ["tape.h", "lower.h", "kernels.h", "device_math.cuh", "noalloc.h", "engine.h", "capi_internal.h", "batch.h", "mesh.h", "server.h", "march_kernels.cuh", "shade_kernels.cuh", "post_kernels.cuh", "reproject_kernels.cuh", "spec.h"]
 
 
 def _cudart_dir():

@@ -5,13 +5,16 @@
 // truncation. Test infrastructure only.
 #pragma once
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <math.h>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 #include <cuda_runtime.h>
 // (Standard headers come before the __noinline__ stand-in below, which their attributes spell.)

@@ -1,4 +1,4 @@
-"""Index arithmetic of the fused bloom kernels (k_bloom_h / k_bloom_v in wavefront.cu), replayed
+"""Index arithmetic of the fused bloom kernels (k_bloom_h / k_bloom_v in post_kernels.cuh), replayed
 on the CPU: blur4's four outputs read each tap once, and every output still sums the reference's
 taps (post.rs:348-368) in kernel order with the right weights; every shared-memory window read
 of the horizontal pass stays inside the window, whatever the job layout, radius or row width."""

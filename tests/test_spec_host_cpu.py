@@ -1306,3 +1306,117 @@ def test_batched_wave_equals_oracle_on_host(tmp_path):
             (k, int((got.view(np.uint32) != ref.view(np.uint32)).any(axis=2).sum()), n)
         base += n
     assert base == len(hdr)
+
+
+POST_MAIN = r"""
+#include "host_io.h"
+#include "lower.h"
+#include "march_kernels.cuh"  // its dynamic shared memory is extern: before __shared__ turns static
+#undef __shared__
+#define __shared__ static
+#include "post_kernels.cuh"
+using namespace mm3e;
+using namespace mm3e::wave;
+// The post of one frame as launch_post runs it, on a given HDR image: without bloom the resolve
+// kernel; with bloom the fused bright-pass + horizontal blur (blocks of POST_THREADS threads
+// sharing a window) and the vertical blur + resolve. Arguments: hdr, out, w, h, exposure, bloom,
+// threshold, intensity, radius, format (0 RGBA8, 1 RGBA f32).
+int main(int argc, char** argv) {
+    const std::vector<float> hdr3 = read_floats(argv[1]);
+    const uint32_t w = (uint32_t)std::atoi(argv[3]), h = (uint32_t)std::atoi(argv[4]), n = w * h;
+    const float exposure = std::strtof(argv[5], nullptr), threshold = std::strtof(argv[7], nullptr);
+    const float intensity = std::strtof(argv[8], nullptr);
+    const bool bloom = std::atoi(argv[6]) != 0 && intensity > 0.0f;
+    const uint32_t radius = (uint32_t)std::atoi(argv[9]), format = std::atoi(argv[10]) ? MM3E_FB_RGBA_F32 : MM3E_FB_RGBA8;
+    const std::vector<float> weights = gaussian_kernel(bloom ? radius : 1u);  // as upload_post_kernel
+    std::vector<float4> hdr(n), blur(n), out32(n);
+    std::vector<uchar4> out8(n);
+    for (uint32_t i = 0; i < n; ++i) hdr[i] = make_float4(hdr3[3 * i], hdr3[3 * i + 1], hdr3[3 * i + 2], 1.0f);
+    FrameJob J{};
+    J.width = w;
+    J.height = h;
+    J.n_pixels = n;
+    J.bloom_w = weights.data();
+    J.bloom_radius = (uint32_t)(weights.size() / 2);
+    J.flags = bloom ? JF_BLOOM : 0u;
+    J.threshold = threshold;
+    J.intensity = intensity;
+    J.exposure = exposure;
+    J.format = format;
+    J.out = format == MM3E_FB_RGBA8 ? (void*)out8.data() : (void*)out32.data();
+    PostArgs p{};
+    p.job0 = J;
+    p.n_jobs = 1;
+    p.n_pixels = n;
+    p.any_bloom = bloom ? 1 : 0;
+    p.hdr = hdr.data();
+    p.blur_h = blur.data();
+    const unsigned T = POST_THREADS;
+    if (!bloom) {
+        host_launch((n + T - 1) / T, T, [&] { k_resolve_post(p); });
+    } else {
+        host_launch((n + BLOOM_SEG - 1) / BLOOM_SEG, T, [&] { k_bloom_h(p); });
+        const uint32_t groups = w * ((h + 3u) / 4u);
+        host_launch((groups + T - 1) / T, T, [&] { k_bloom_v<true>(p); });
+    }
+    FILE* fo = std::fopen(argv[2], "wb");
+    if (format == MM3E_FB_RGBA8) std::fwrite(out8.data(), sizeof(uchar4), n, fo);
+    else std::fwrite(out32.data(), sizeof(float4), n, fo);
+    std::fclose(fo);
+    return 0;
+}
+"""
+
+POST_CASES = [  # w, h, bloom radius, threshold, intensity, exposure, format (0 RGBA8, 1 RGBA f32)
+    (64, 36, 12, 0.8, 0.6, 1.0, 0), (64, 36, 12, 0.8, 0.6, 1.0, 1), (1, 1, 12, 0.5, 0.6, 1.0, 0),
+    (1, 9, 12, 0.5, 0.6, 1.3, 0), (9, 1, 3, 0.5, 0.6, 0.7, 0), (13, 7, 40, 0.2, 1.5, 1.0, 0),
+    (37, 21, 0, 0.5, 0.6, 1.0, 0), (70, 3, 1, 0.0, 0.3, 2.0, 1), (33, 17, 12, 0.8, 0.0, 1.0, 0),
+    (300, 5, 32, 0.6, 0.8, 1.0, 0), (300, 5, 33, 0.6, 0.8, 1.0, 0)]
+
+
+def test_post_equals_oracle_on_host(tmp_path):
+    """The post kernels (post_kernels.cuh: the fused bright-pass + horizontal blur with its
+    swizzled shared window and four-output blur4, the vertical blur + resolve, the resolve
+    without bloom; exposure, ACES, gamma and the RGBA8 or RGBA f32 write; post.rs:36-115),
+    compiled for the host and run as blocks of POST_THREADS threads, on the oracle's own HDR image,
+    against the oracle's post of that image: every byte (RGBA8) or bit (f32) equal. The cases
+    cover 1x1, single rows and columns, radius 0, 1, 12, 32 and 33 (the latter two on either
+    side of the shared window's halo) and 40, a threshold of 0 and bloom with intensity 0."""
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    flags = ["-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE, "-I", CSRC, "-I",
+             HOST_DIR]
+    r = subprocess.run(["g++"] + flags + ["-c", os.path.join(CSRC, "lower.cpp"), "-o", str(tmp_path / "lower.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    (tmp_path / "main.cpp").write_text(POST_MAIN)
+    exe = tmp_path / "post"
+    r = subprocess.run(["g++"] + flags + ["-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"),
+                                          str(tmp_path / "lower.o"), "-pthread", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    failed = []
+    for k, (w, h, radius, thr, inten, exposure, fmt) in enumerate(POST_CASES):
+        scene, cam = scenes.gallery_scene(w, h)
+        scene.post.bloom = True
+        scene.post.bloom_radius = radius
+        scene.post.bloom_threshold = thr
+        scene.post.bloom_intensity = inten
+        scene.post.exposure = exposure
+        handle = scene.desc()
+        _, hdr = oracle_py.render(handle, cam, threads=2, want_hdr=True)
+        ref = oracle_py.post(handle, hdr)
+        hdr.astype(np.float32).tofile(tmp_path / f"hdr{k}.bin")
+        post = scene.post
+        subprocess.run([str(exe), str(tmp_path / f"hdr{k}.bin"), str(tmp_path / f"out{k}.bin"), str(w), str(h),
+                        repr(float(post.exposure)), "1", repr(float(post.bloom_threshold)),
+                        repr(float(post.bloom_intensity)), str(radius), str(fmt)], check=True)
+        if fmt == 0:
+            got = np.fromfile(tmp_path / f"out{k}.bin", np.uint8).reshape(h, w, 4)
+            bad = int((got != mm3e_cuda.to_rgba8(ref)).any(-1).sum())
+        else:
+            got = np.fromfile(tmp_path / f"out{k}.bin", np.float32).reshape(h, w, 4)
+            bad = int((got.view(np.uint32) != ref.view(np.uint32)).any(-1).sum())
+        if bad:
+            failed.append(((w, h, radius, thr, inten, exposure, fmt), bad))
+    assert not failed, failed
