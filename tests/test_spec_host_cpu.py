@@ -1420,3 +1420,39 @@ def test_post_equals_oracle_on_host(tmp_path):
         if bad:
             failed.append(((w, h, radius, thr, inten, exposure, fmt), bad))
     assert not failed, failed
+
+
+def test_degenerate_cameras_equal_oracle_on_host(frame_harnesses, tmp_path):
+    """Cameras the C ABI takes without checks, as the reference's render does: a NaN or infinite
+    eye, an eye 1e7 away, zero basis vectors, and a zero, negative, NaN or huge field-of-view
+    scale. Whole frames through the device pass sequence equal the oracle's render bit for bit
+    (NaN for NaN) over both fields; every march ends within its step budget."""
+    from mm3e_cuda.abi import Camera
+    scene, cam = FRAME_SCENES["gallery"]()
+    exe = frame_harnesses[mm3e_cuda.spec_source(scene)]
+    nan, inf = float("nan"), float("inf")
+
+    def variant(eye=None, fwd=None, right=None, up=None, fov=None):
+        c = Camera()
+        c.eye[:] = eye or list(cam.eye)
+        c.forward[:] = fwd or list(cam.forward)
+        c.right[:] = right or list(cam.right)
+        c.up[:] = up or list(cam.up)
+        c.fov_scale = cam.fov_scale if fov is None else fov
+        return c
+
+    cases = {"nan_eye": variant(eye=[nan, 1.0, 1.0]), "inf_eye": variant(eye=[inf, 1.0, -5.0]),
+             "far_eye": variant(eye=[1e7, 2.0, -1e7]), "zero_forward": variant(fwd=[0.0, 0.0, 0.0]),
+             "zero_basis": variant(fwd=[0.0, 0.0, 0.0], right=[0.0, 0.0, 0.0], up=[0.0, 0.0, 0.0]),
+             "fov_zero": variant(fov=0.0), "fov_negative": variant(fov=-1.0), "fov_nan": variant(fov=nan),
+             "fov_huge": variant(fov=1e30)}
+    failed = {}
+    for name, c in cases.items():
+        out, _ = _run_frame_harness(exe, scene, c, tmp_path)
+        _, ref = oracle_py.render(scene.desc(), c, threads=2, want_hdr=True)
+        for k in range(2):
+            dev = np.ascontiguousarray(out[k, :, :, :3])
+            same = (dev.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(dev) & np.isnan(ref))
+            if not same.all():
+                failed[(name, k)] = int((~same).any(axis=2).sum())
+    assert not failed, failed
