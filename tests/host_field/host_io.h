@@ -1,4 +1,4 @@
-// File readers of the host-compiled device-code checks (tests/test_spec_host_cpu.py): the
+// File readers of the host-compiled device-code checks (tests/host_checks.py): the
 // lowered tape and payloads as 16-byte words, float arrays (points, rays) and a camera, each read
 // whole from the files the test writes. Test infrastructure only.
 #pragma once

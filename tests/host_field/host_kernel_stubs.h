@@ -1,6 +1,6 @@
 // Host stand-ins for the device-only builtins that march_kernels.cuh references, so that its
 // per-lane march state machine (m_start / m_step) and the other kernels' bodies compile as plain
-// C++ and a host loop can drive them item by item (tests/test_spec_host_cpu.py): one thread of one
+// C++ and a host loop can drive them item by item (tests/host_checks.py): one thread of one
 // block, so a warp vote sees one lane and an atomic is a plain read-modify-write. Test
 // infrastructure only.
 #pragma once

@@ -1,4 +1,4 @@
-// The device pass sequence of a frame, run on the host item by item (tests/test_spec_host_cpu.py):
+// The device pass sequence of a frame, run on the host item by item (tests/host_checks.py):
 // for each reflection level, the march (march_kernels.cuh m_start / m_step), the next level's
 // reflection rays, AO, soft shadows and shading (shade_kernels.cuh), as the engine launches them.
 // Every level keeps its own queue and hit records, as the device keeps the primary level's apart

@@ -1,6 +1,6 @@
 // Host definitions of the CUDA device intrinsics that device_math.cuh uses, so that the world
 // field (the tape interpreter and a scene-specialised program) compiles as plain C++ for a host
-// comparison (tests/test_spec_host_cpu.py). Every definition is exact: bit reinterpretations,
+// comparison (tests/host_checks.py). Every definition is exact: bit reinterpretations,
 // a correctly rounded fused multiply-add, an upward-rounded binary32 sum, a saturating
 // truncation. Test infrastructure only.
 #pragma once
