@@ -211,3 +211,24 @@ def spec_namespace(scene):
     ns = src[src.index("namespace spec {") + len("namespace spec {"):src.index("}  // namespace spec")]
     defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
     return defines, ns
+
+
+GXX = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w"]
+
+
+def compile_harnesses(jobs, exe_name):
+    """Compile each job's main.cpp in parallel. jobs: name -> (directory, extra g++ flags);
+    returns name -> executable path."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(job):
+        d, flags = job
+        exe = d / exe_name
+        r = subprocess.run(GXX + ["-I", CUDA_INCLUDE, "-I", CSRC, "-I", HOST_DIR] + flags + [str(d / "main.cpp"), "-o", str(exe)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-3000:]
+        return exe
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+        exes = list(pool.map(one, jobs.values()))
+    return dict(zip(jobs, exes))

@@ -18,7 +18,8 @@ import pytest
 
 import mm3e_cuda
 import oracle_py
-from host_checks import CSRC, CUDA_INCLUDE, HOST_DIR, SCENES, SHIM, STUBS, harness_source, spec_namespace
+from host_checks import (CSRC, CUDA_INCLUDE, HOST_DIR, SCENES, SHIM, STUBS, compile_harnesses, harness_source,
+                         spec_namespace)
 
 MAIN = harness_source("field_check.inc")
 
@@ -41,21 +42,29 @@ def _points(scene, cam, rng, n=6000):
     return np.concatenate([on_rays, box, special]).astype(np.float32)
 
 
-@pytest.mark.parametrize("name", list(SCENES))
-def test_specialised_field_equals_interpreter_on_host(name, tmp_path):
+@pytest.fixture(scope="module")
+def field_exes(tmp_path_factory):
+    """The field check of every scene, compiled in parallel."""
     if not shutil.which("g++"):
         pytest.skip("no host C++ compiler")
+    root = tmp_path_factory.mktemp("field")
+    jobs = {}
+    for name, make in SCENES.items():
+        src = mm3e_cuda.spec_source(make()[0])
+        body = src[src.index("namespace spec {") + len("namespace spec {"):src.index("struct Field_")]
+        defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
+        d = root / name
+        d.mkdir()
+        (d / "field.inc").write_text(body)
+        (d / "main.cpp").write_text(defines + '#include "device_math.cuh"\n' + MAIN)
+        jobs[name] = (d, ["-I", str(d), "-include", SHIM])
+    return compile_harnesses(jobs, "field_check")
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_specialised_field_equals_interpreter_on_host(name, field_exes, tmp_path):
     scene, cam = SCENES[name]()
-    src = mm3e_cuda.spec_source(scene)
-    body = src[src.index("namespace spec {") + len("namespace spec {"):src.index("struct Field_")]
-    defines = "#define MM3E_SHARED_SINCOS 1\n" if "#define MM3E_SHARED_SINCOS 1" in src else ""
-    (tmp_path / "field.inc").write_text(body)
-    (tmp_path / "main.cpp").write_text(defines + '#include "device_math.cuh"\n' + MAIN)
-    exe = tmp_path / "field_check"
-    cmd = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE, "-I", CSRC, "-I", HOST_DIR,
-           "-I", str(tmp_path), "-include", SHIM, str(tmp_path / "main.cpp"), "-o", str(exe)]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
+    exe = field_exes[name]
     (tmp_path / "tape.bin").write_bytes(mm3e_cuda.scene_tape(scene))
     _points(scene, cam, np.random.default_rng(zlib.crc32(name.encode()))).tofile(tmp_path / "points.bin")
     r = subprocess.run([str(exe), str(tmp_path / "tape.bin"), str(tmp_path / "points.bin")], capture_output=True,
@@ -139,24 +148,39 @@ def test_shading_formulas_equal_oracle_on_host(tmp_path):
 MARCH_MAIN = harness_source("march_rays.inc")
 
 
-@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "csg_zoo", "unbounded_mix", "procedural3", "procedural8"])
-def test_march_state_machine_equals_oracle_on_host(name, tmp_path):
+MARCH_SCENES = ["gallery", "spheres", "cornell", "csg_zoo", "unbounded_mix", "procedural3", "procedural8"]
+SHADOW_SCENES = ["gallery", "spheres", "cornell", "procedural0", "procedural3", "procedural8", "procedural11"]
+
+
+def _state_machine_exes(root, names, main):
+    """Harnesses of the device march / shadow state machines with each scene's generated field."""
+    jobs = {}
+    for name in names:
+        defines, ns = spec_namespace(SCENES[name]()[0])
+        d = root / name
+        d.mkdir()
+        (d / "main.cpp").write_text(defines + '#include "march_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
+                                    "\n}}\n" + main)
+        jobs[name] = (d, ["-include", SHIM, "-include", STUBS])
+    return compile_harnesses(jobs, "harness")
+
+
+@pytest.fixture(scope="module")
+def march_exes(tmp_path_factory):
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    return _state_machine_exes(tmp_path_factory.mktemp("march"), MARCH_SCENES, MARCH_MAIN)
+
+
+@pytest.mark.parametrize("name", MARCH_SCENES)
+def test_march_state_machine_equals_oracle_on_host(name, march_exes, tmp_path):
     """The device march (march_kernels.cuh m_start / m_step: enhanced sphere tracing with its
     rollback, gap-cover and tetrahedral-normal phases, march.rs:120-223), compiled for the host and
     driven ray by ray over both the tape interpreter's field and the scene's generated field,
     against the oracle's march (oracle_march_rays): hit or miss, material, steps, and t and the
     normal of every hit, bit for bit, on rays from the scene's camera."""
-    if not shutil.which("g++"):
-        pytest.skip("no host C++ compiler")
     scene, cam = SCENES[name]()
-    defines, ns = spec_namespace(scene)
-    (tmp_path / "main.cpp").write_text(defines + '#include "march_kernels.cuh"\nnamespace mm3e { namespace spec {\n' + ns +
-                                       "\n}}\n" + MARCH_MAIN)
-    exe = tmp_path / "march"
-    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
+    exe = march_exes[name]
     rng = np.random.default_rng(zlib.crc32(name.encode()))
     n = 3000
     eye = np.array(cam.eye, np.float32)
@@ -186,8 +210,15 @@ def test_march_state_machine_equals_oracle_on_host(name, tmp_path):
 SHADOW_MAIN = harness_source("shadow_ao.inc")
 
 
-@pytest.mark.parametrize("name", ["gallery", "spheres", "cornell", "procedural0", "procedural3", "procedural8", "procedural11"])
-def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
+@pytest.fixture(scope="module")
+def shadow_exes(tmp_path_factory):
+    if not shutil.which("g++"):
+        pytest.skip("no host C++ compiler")
+    return _state_machine_exes(tmp_path_factory.mktemp("shadow"), SHADOW_SCENES, SHADOW_MAIN)
+
+
+@pytest.mark.parametrize("name", SHADOW_SCENES)
+def test_shadow_and_ao_equal_oracle_on_host(name, shadow_exes, tmp_path):
     """The device soft-shadow march (march_kernels.cuh s_start / s_step: the lifted origin, the
     light's direction, distance and k, the jittered start and the min(k h / t) fold with its
     division skip, march.rs:227-259 and lib.rs:1315-1333), compiled for the host and run over the
@@ -197,19 +228,10 @@ def test_shadow_and_ao_equal_oracle_on_host(name, tmp_path):
     oracle's, so the jitter is bit-equal here; on the device it is within sinf's error bound.
     The AO pass (ao_slot, march.rs:264-280) runs over the same hits against oracle_ambient_occlusion,
     bit for bit, and leaves 1 on a miss."""
-    if not shutil.which("g++"):
-        pytest.skip("no host C++ compiler")
     scene, cam = SCENES[name]()
     nl = scene.desc().desc.n_lights
     assert nl > 0
-    defines, ns = spec_namespace(scene)
-    (tmp_path / "main.cpp").write_text(defines + '#include <cstdlib>\n#include "march_kernels.cuh"\n'
-                                       'namespace mm3e { namespace spec {\n' + ns + "\n}}\n" + SHADOW_MAIN)
-    exe = tmp_path / "shadow"
-    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), "-o", str(exe)],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
+    exe = shadow_exes[name]
     rng = np.random.default_rng(zlib.crc32(name.encode()))
     n = 2000
     eye = np.array(cam.eye, np.float32)
