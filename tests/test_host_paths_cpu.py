@@ -136,7 +136,10 @@ def test_batched_wave_equals_oracle_on_host(tmp_path):
     sample by binary search over the table, each lane's own job's tape, AO for AO jobs only, the
     per-job resolve) over scenes of different kinds, sizes, AA, bounce and light counts, with and
     without AO and shadows, compiled for the host and run as one pass sequence through the tape
-    interpreter: every job's HDR pixels equal the oracle's render of its scene bit for bit."""
+    interpreter: every job's HDR pixels equal the oracle's render of its scene bit for bit. The
+    multi-job post that follows (post_kernels.cuh with the job table: each pixel's job by binary
+    search, each job's own bloom kernel, threshold, intensity and exposure, bloom off for some)
+    gives every job's RGBA8 bytes of the oracle's frame."""
     if not shutil.which("g++"):
         pytest.skip("no host C++ compiler")
     jobs = [scenes.gallery_scene(40, 24), scenes.spheres_scene(33, 17), scenes.hero_scene(24, 20, 2, 2),
@@ -146,11 +149,19 @@ def test_batched_wave_equals_oracle_on_host(tmp_path):
     no_shadow.shadows = False
     no_ao, _ = jobs[3]
     no_ao.ao = False
+    jobs[1][0].post.bloom_radius = 3
+    jobs[2][0].post.bloom = False
+    jobs[5][0].post.bloom_threshold, jobs[5][0].post.bloom_intensity, jobs[5][0].post.bloom_radius = 0.2, 0.8, 33
+    jobs[7][0].post.exposure = 1.5
     (tmp_path / "main.cpp").write_text('#include "shade_kernels.cuh"\n' + BATCH_MAIN)
     exe = tmp_path / "batch"
-    r = subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE,
-                        "-I", CSRC, "-I", HOST_DIR, "-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"),
-                        "-o", str(exe)], capture_output=True, text=True)
+    flags = ["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fno-fast-math", "-w", "-I", CUDA_INCLUDE, "-I", CSRC, "-I",
+             HOST_DIR]
+    r = subprocess.run(flags + ["-c", os.path.join(CSRC, "lower.cpp"), "-o", str(tmp_path / "lower.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run(flags + ["-include", SHIM, "-include", STUBS, str(tmp_path / "main.cpp"), str(tmp_path / "lower.o"),
+                                "-pthread", "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     args = [str(exe), str(tmp_path / "out.bin"), str(len(jobs))]
     for k, (s, cam) in enumerate(jobs):
@@ -159,17 +170,24 @@ def test_batched_wave_equals_oracle_on_host(tmp_path):
         d = s.desc().desc
         args += [str(tmp_path / f"tape{k}.bin"), str(tmp_path / f"cam{k}.bin"), str(d.width), str(d.height)]
     subprocess.run(args, check=True)
-    hdr = np.fromfile(tmp_path / "out.bin", np.float32).reshape(-1, 4)
+    raw = np.fromfile(tmp_path / "out.bin", np.uint8)
+    total = sum(s.desc().desc.width * s.desc().desc.height for s, _ in jobs)
+    hdr = raw[:total * 16].view(np.float32).reshape(-1, 4)
+    rgba8 = raw[total * 16:]
+    assert len(rgba8) == total * 4
     base = 0
     for k, (s, cam) in enumerate(jobs):
         d = s.desc().desc
         n = d.width * d.height
         got = np.ascontiguousarray(hdr[base:base + n, :3]).reshape(d.height, d.width, 3)
-        _, ref = oracle_py.render(s.desc(), cam, threads=2, want_hdr=True)
+        rgba, ref = oracle_py.render(s.desc(), cam, threads=2, want_hdr=True)
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), \
             (k, int((got.view(np.uint32) != ref.view(np.uint32)).any(axis=2).sum()), n)
+        got8 = rgba8[base * 4:(base + n) * 4].reshape(d.height, d.width, 4)
+        want8 = mm3e_cuda.to_rgba8(rgba)
+        assert np.array_equal(got8, want8), (k, "rgba8", int((got8 != want8).any(-1).sum()), n)
         base += n
-    assert base == len(hdr)
+    assert base == total
 
 
 POST_MAIN = harness_source("post.inc")
